@@ -1,0 +1,96 @@
+"""ctypes binding of the CPU restatement (oracle/restate.c).
+
+Test infrastructure only (checker and CPU-baseline port); never imported by
+the product path.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+from . import build as _build  # noqa: F401  (package-relative when imported as oracle.orc)
+
+_dp = ctypes.POINTER(ctypes.c_double)
+_L = None
+
+
+def lib():
+    global _L
+    if _L is None:
+        path = _build.build()
+        L = ctypes.CDLL(path)
+        L.orc_u01.restype = ctypes.c_double
+        L.orc_u01.argtypes = [ctypes.c_uint64, ctypes.c_uint64, ctypes.c_uint64]
+        L.orc_pairwise_sum.restype = ctypes.c_double
+        L.orc_pairwise_sum.argtypes = [_dp, ctypes.c_long]
+        L.orc_canon_sum.restype = ctypes.c_double
+        L.orc_canon_sum.argtypes = [_dp, ctypes.c_long, ctypes.c_long, ctypes.c_long]
+        L.orc_jacobi_init.argtypes = [ctypes.c_int, ctypes.c_long, ctypes.c_uint64, _dp, _dp]
+        L.orc_jacobi_step.restype = ctypes.c_double
+        L.orc_jacobi_step.argtypes = [ctypes.c_int, ctypes.c_long, _dp, _dp, ctypes.c_int]
+        L.orc_sor_init.argtypes = [ctypes.c_long, ctypes.c_uint64, _dp]
+        L.orc_sor_sweep.restype = ctypes.c_double
+        L.orc_sor_sweep.argtypes = [ctypes.c_long, ctypes.c_double, _dp, _dp]
+        L.orc_heat_side.restype = ctypes.c_long
+        L.orc_heat_side.argtypes = [ctypes.c_uint64, ctypes.c_long, ctypes.c_long, ctypes.c_long]
+        L.orc_heat_init.argtypes = [ctypes.c_long, ctypes.c_uint64, ctypes.c_long, _dp, _dp]
+        L.orc_heat_step.argtypes = [ctypes.c_long, ctypes.c_double, _dp, _dp, _dp, _dp, _dp,
+                                    ctypes.POINTER(ctypes.c_int)]
+        L.orc_max_threads.restype = ctypes.c_int
+        _L = L
+    return _L
+
+
+def P(a):
+    assert a.dtype == np.float64 and a.flags.c_contiguous
+    return a.ctypes.data_as(_dp)
+
+
+def jacobi_init(rank, n, seed):
+    A = np.zeros(n ** rank)
+    B = np.zeros(n ** rank)
+    lib().orc_jacobi_init(rank, n, seed, P(A), P(B))
+    return A, B
+
+
+def jacobi_run(rank, n, iters, seed, threads=1):
+    A, B = jacobi_init(rank, n, seed)
+    eps = [lib().orc_jacobi_step(rank, n, P(A), P(B), threads) for _ in range(iters)]
+    return np.array(eps), A, B
+
+
+def sor_run(n, sweeps, omega, seed):
+    """Returns (sequential-order residuals, canonical-tree residuals, A)."""
+    A = np.zeros(n ** 3)
+    lib().orc_sor_init(n, seed, P(A))
+    seq, can = [], []
+    for _ in range(sweeps):
+        c = ctypes.c_double()
+        seq.append(lib().orc_sor_sweep(n, omega, P(A), ctypes.byref(c)))
+        can.append(c.value)
+    return np.array(seq), np.array(can), A
+
+
+def heat_sides(count, lo, hi, seed):
+    return [int(lib().orc_heat_side(seed, k, lo, hi)) for k in range(count)]
+
+
+def heat_run(count, lo, hi, steps, coef, seed):
+    """Returns dict: sides, sums_seq, sums_canon, mins, locs ([steps][count]...), finals."""
+    sides = heat_sides(count, lo, hi, seed)
+    out = {"sides": sides, "sums_seq": np.zeros((steps, count)), "sums_canon": np.zeros((steps, count)),
+           "mins": np.zeros((steps, count)), "locs": np.zeros((steps, count, 2), dtype=np.int32), "finals": []}
+    for k, n in enumerate(sides):
+        U = np.zeros(n * n)
+        V = np.zeros(n * n)
+        lib().orc_heat_init(n, seed, k, P(U), P(V))
+        src, dst = U, V
+        for t in range(steps):
+            ss, sc, mn = ctypes.c_double(), ctypes.c_double(), ctypes.c_double()
+            lc = (ctypes.c_int * 2)()
+            lib().orc_heat_step(n, coef, P(src), P(dst), ctypes.byref(ss), ctypes.byref(sc), ctypes.byref(mn), lc)
+            out["sums_seq"][t, k], out["sums_canon"][t, k], out["mins"][t, k] = ss.value, sc.value, mn.value
+            out["locs"][t, k] = list(lc)
+            src, dst = dst, src
+        out["finals"].append(src)
+    return out

@@ -1,0 +1,126 @@
+/*
+ * Driver that runs a workload program (dvm-snapshot-r6603-fork_gb300/workloads/*.c,
+ * compiled with WL_NO_CUDA) on the REFERENCE runtime built by oracle/ref.mk, and
+ * writes its outputs as raw little-endian binary.  Test infrastructure only: it
+ * generates the golden fixtures under tests/golden/ (tests/golden/make_golden.py).
+ *
+ * usage: ref_driver <prog> <out.bin> <params...>
+ *   jac2d|jac3d  n iters seed          -> eps[iters], A[n^r], B[n^r]
+ *   sor3d        n sweeps omega seed   -> s[sweeps], A[n^3]
+ *   heat         count lo hi steps coef seed
+ *                -> sides[count] (int64), then per step: sums[count], mins[count],
+ *                   locs[count][2] (int32), then the final arrays in order
+ * Run with DVMH_NUM_THREADS=1 for the sequential (order-exact) oracle.
+ */
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include "dvmhlib2.h"
+#include "wl_common.h"
+
+int wl_jac2d_setup(const wl_jacobi_params *p);
+int wl_jac2d_run(long iters, double *eps_out);
+int wl_jac2d_fetch(double *a_out, double *b_out);
+int wl_jac3d_setup(const wl_jacobi_params *p);
+int wl_jac3d_run(long iters, double *eps_out);
+int wl_jac3d_fetch(double *a_out, double *b_out);
+int wl_sor3d_setup(const wl_sor_params *p);
+int wl_sor3d_run(long sweeps, double *s_out);
+int wl_sor3d_fetch(double *a_out);
+int wl_heat_setup(const wl_heat_params *p, long *sides_out);
+int wl_heat_run(long steps, double *sums_out, double *mins_out, int *locs_out);
+int wl_heat_fetch(long k, double *u_out);
+
+static void put(FILE *f, const void *p, size_t bytes) {
+    if (fwrite(p, 1, bytes, f) != bytes) {
+        fprintf(stderr, "write failed\n");
+        exit(2);
+    }
+}
+
+int main(int argc, char **argv) {
+    FILE *f;
+    if (argc < 3) {
+        fprintf(stderr, "usage: %s prog out.bin params...\n", argv[0]);
+        return 2;
+    }
+    dvmh_init_C(0, &argc, &argv);
+    f = fopen(argv[2], "wb");
+    if (!f)
+        return 2;
+    if (!strcmp(argv[1], "jac2d") || !strcmp(argv[1], "jac3d")) {
+        int r3 = !strcmp(argv[1], "jac3d");
+        wl_jacobi_params p;
+        size_t cells;
+        double *e, *a, *b;
+        p.n = atol(argv[3]);
+        p.iters = atol(argv[4]);
+        p.seed = strtoull(argv[5], 0, 10);
+        cells = (size_t)p.n * p.n * (r3 ? p.n : 1);
+        e = malloc(sizeof(double) * p.iters);
+        a = malloc(sizeof(double) * cells);
+        b = malloc(sizeof(double) * cells);
+        if (r3) {
+            wl_jac3d_setup(&p);
+            wl_jac3d_run(p.iters, e);
+            wl_jac3d_fetch(a, b);
+        } else {
+            wl_jac2d_setup(&p);
+            wl_jac2d_run(p.iters, e);
+            wl_jac2d_fetch(a, b);
+        }
+        put(f, e, sizeof(double) * p.iters);
+        put(f, a, sizeof(double) * cells);
+        put(f, b, sizeof(double) * cells);
+    } else if (!strcmp(argv[1], "sor3d")) {
+        wl_sor_params p;
+        size_t cells;
+        double *s, *a;
+        p.n = atol(argv[3]);
+        p.sweeps = atol(argv[4]);
+        p.omega = atof(argv[5]);
+        p.seed = strtoull(argv[6], 0, 10);
+        cells = (size_t)p.n * p.n * p.n;
+        s = malloc(sizeof(double) * p.sweeps);
+        a = malloc(sizeof(double) * cells);
+        wl_sor3d_setup(&p);
+        wl_sor3d_run(p.sweeps, s);
+        wl_sor3d_fetch(a);
+        put(f, s, sizeof(double) * p.sweeps);
+        put(f, a, sizeof(double) * cells);
+    } else if (!strcmp(argv[1], "heat")) {
+        wl_heat_params p;
+        long *sides, k;
+        double *sums, *mins, *u;
+        int *locs;
+        p.count = atol(argv[3]);
+        p.side_lo = atol(argv[4]);
+        p.side_hi = atol(argv[5]);
+        p.steps = atol(argv[6]);
+        p.coef = atof(argv[7]);
+        p.seed = strtoull(argv[8], 0, 10);
+        sides = malloc(sizeof(long) * p.count);
+        sums = malloc(sizeof(double) * p.count * p.steps);
+        mins = malloc(sizeof(double) * p.count * p.steps);
+        locs = malloc(sizeof(int) * 2 * p.count * p.steps);
+        wl_heat_setup(&p, sides);
+        wl_heat_run(p.steps, sums, mins, locs);
+        put(f, sides, sizeof(long) * p.count);
+        put(f, sums, sizeof(double) * p.count * p.steps);
+        put(f, mins, sizeof(double) * p.count * p.steps);
+        put(f, locs, sizeof(int) * 2 * p.count * p.steps);
+        for (k = 0; k < p.count; k++) {
+            u = malloc(sizeof(double) * sides[k] * sides[k]);
+            wl_heat_fetch(k, u);
+            put(f, u, sizeof(double) * sides[k] * sides[k]);
+            free(u);
+        }
+    } else {
+        fprintf(stderr, "unknown program %s\n", argv[1]);
+        return 2;
+    }
+    fclose(f);
+    dvmh_exit_C(0);
+    return 0;
+}

@@ -1,0 +1,294 @@
+/*
+ * oracle/restate.c -- CPU restatement of the DVMH loop-execution path for the
+ * workloads this repository runs.  TEST INFRASTRUCTURE ONLY: tests/, the smoke
+ * check and bench.py's CPU-baseline leg load it as the checker / the timed
+ * CPU port.  The GPU product never links or calls it.
+ *
+ * Pinned against the reference runtime itself: tests/golden/ holds outputs of
+ * the same workload programs run on the reference's host handlers (built from
+ * its sources by oracle/ref.mk, DVMH_NUM_THREADS=1), and tests/test_oracle.py
+ * checks this file against those fixtures bit for bit.
+ *
+ * What it restates (reference file:line):
+ *  - loop bodies: examples/Performance/jac3d_perf.c:56-73 (3-D Jacobi, FP64),
+ *    examples/Jacobi/jac2d.c:49-64 (2-D Jacobi), examples/Sor/sor.c:45-53 made
+ *    3-D with a sum-of-squares residual; the batched heat step is the body of
+ *    dvm-snapshot-r6603-fork_gb300/workloads/heat.c.
+ *  - reduction semantics: per-thread init (DvmhReduction::initValues,
+ *    rts/dvmh/loop.cpp:37-100), combine rules incl. strict '<'/'>' for MAX/MIN
+ *    so the first value in loop order wins a tie (RED_MAX/RED_MIN, loop.cpp:117-118),
+ *    final result = (identity (+) loop value) (+) initial value
+ *    (initGlobalValues + postValues + addInitialValues, rts/dvmh/dvmh2.cpp:3848-3851,3950-3953).
+ *  - sequential order = the reference with one host thread.
+ *
+ * Canonical tree (the GPU's deterministic order for floating SUM/PROD, restated
+ * here so GPU results can be checked bit for bit): the loop's iteration box is
+ * cut into rows (all indices but the innermost) in loop order; each row into
+ * 64-wide chunks aligned to multiples of 64 of the innermost ARRAY index.  A
+ * chunk's value is the pairwise tree over its 64 positions (position p pairs
+ * with p^1, then p^2, ...), with the identity (-0.0 for SUM, 1.0 for PROD) at
+ * positions outside the loop.  Chunks, in row-major order, are then combined by
+ * a pairwise tree over their indices padded with the identity to a power of two.
+ *
+ * Compile with -O2 -ffp-contract=off (no FMA contraction) so every cell's
+ * arithmetic is the source program's.
+ */
+#include <math.h>
+#include <stdint.h>
+#include <stdlib.h>
+#include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+#define Max(a, b) ((a) > (b) ? (a) : (b))
+#define CHUNK 64
+
+static uint64_t mix64(uint64_t z) {
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ULL;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBULL;
+    return z ^ (z >> 31);
+}
+
+/* splitmix64 stream `stream` of `seed`, element n, as a double in [0,1) */
+double orc_u01(uint64_t seed, uint64_t stream, uint64_t n) {
+    uint64_t s0 = seed ^ (0xD1B54A32D192ED03ULL * (stream + 1));
+    return (double)(mix64(s0 + (n + 1) * 0x9E3779B97F4A7C15ULL) >> 11) * (1.0 / 9007199254740992.0);
+}
+
+/* ------------------------------------------------------------ canonical tree */
+
+/* pairwise sum of v[0..n) padded with -0.0 to a power of two (in place, destroys v) */
+double orc_pairwise_sum(double *v, long n) {
+    long p = 1, len, i;
+    if (n <= 0)
+        return -0.0;
+    while (p < n)
+        p <<= 1;
+    for (len = p; len > 1; len >>= 1) {
+        long half = len >> 1;
+        for (i = 0; i < half; i++) {
+            double a = (2 * i < n) ? v[2 * i] : -0.0;
+            double b = (2 * i + 1 < n) ? v[2 * i + 1] : -0.0;
+            v[i] = a + b;
+        }
+        n = half;
+    }
+    return v[0];
+}
+
+/*
+ * Canonical SUM of terms over an iteration box.  terms is dense over the box
+ * (row-major, innermost extent = hi_in - lo_in + 1); rows = number of rows;
+ * the innermost loop index runs lo_in..hi_in (array index, step 1).
+ */
+double orc_canon_sum(const double *terms, long rows, long lo_in, long hi_in) {
+    long c_lo = lo_in / CHUNK, c_hi = hi_in / CHUNK, nck = c_hi - c_lo + 1, w = hi_in - lo_in + 1;
+    long nitems = rows * nck, r, c, p;
+    double *items = malloc(sizeof(double) * (nitems > 0 ? nitems : 1));
+    double leaf[CHUNK], res;
+    for (r = 0; r < rows; r++) {
+        const double *row = terms + r * w;
+        for (c = 0; c < nck; c++) {
+            long base = (c_lo + c) * CHUNK;
+            for (p = 0; p < CHUNK; p++) {
+                long k = base + p;
+                leaf[p] = (k >= lo_in && k <= hi_in) ? row[k - lo_in] : -0.0;
+            }
+            items[r * nck + c] = orc_pairwise_sum(leaf, CHUNK);
+        }
+    }
+    res = orc_pairwise_sum(items, nitems);
+    free(items);
+    return res;
+}
+
+/* ------------------------------------------------------------ Jacobi */
+
+void orc_jacobi_init(int rank, long n, uint64_t seed, double *A, double *B) {
+    long i, j, k;
+    if (rank == 2) {
+        for (i = 0; i < n; i++)
+            for (j = 0; j < n; j++) {
+                long lin = i * n + j;
+                A[lin] = 0.0;
+                B[lin] = (i == 0 || j == 0 || i == n - 1 || j == n - 1) ? 0.0 : orc_u01(seed, 1, (uint64_t)lin);
+            }
+    } else {
+        for (i = 0; i < n; i++)
+            for (j = 0; j < n; j++)
+                for (k = 0; k < n; k++) {
+                    long lin = (i * n + j) * n + k;
+                    A[lin] = 0.0;
+                    B[lin] = (i == 0 || j == 0 || k == 0 || i == n - 1 || j == n - 1 || k == n - 1)
+                                 ? 0.0
+                                 : orc_u01(seed, 1, (uint64_t)lin);
+                }
+    }
+}
+
+/*
+ * One Jacobi time step: the update loop (eps = max |B-A|, A = B) then the
+ * stencil loop, over the interior, with `nthreads` OpenMP threads (static
+ * schedule over the outermost index, like the reference host handler with
+ * OMP_SCHEDULE=static).  Returns eps = max(0.0 init, loop max); MAX is
+ * order-independent so every thread count gives the sequential result.
+ */
+double orc_jacobi_step(int rank, long n, double *A, double *B, int nthreads) {
+    double eps = 0.0;
+    long i;
+    if (nthreads < 1)
+        nthreads = 1;
+    if (rank == 2) {
+#pragma omp parallel for num_threads(nthreads) schedule(static) reduction(max : eps)
+        for (i = 1; i <= n - 2; i++) {
+            long j;
+            for (j = 1; j <= n - 2; j++) {
+                long c = i * n + j;
+                double tmp = fabs(B[c] - A[c]);
+                eps = Max(tmp, eps);
+                A[c] = B[c];
+            }
+        }
+#pragma omp parallel for num_threads(nthreads) schedule(static)
+        for (i = 1; i <= n - 2; i++) {
+            long j;
+            for (j = 1; j <= n - 2; j++) {
+                long c = i * n + j;
+                B[c] = (A[c - n] + A[c - 1] + A[c + 1] + A[c + n]) / 4.0;
+            }
+        }
+    } else {
+        long nn = n * n;
+#pragma omp parallel for num_threads(nthreads) schedule(static) reduction(max : eps)
+        for (i = 1; i <= n - 2; i++) {
+            long j, k;
+            for (j = 1; j <= n - 2; j++)
+                for (k = 1; k <= n - 2; k++) {
+                    long c = (i * n + j) * n + k;
+                    double tmp = fabs(B[c] - A[c]);
+                    eps = Max(tmp, eps);
+                    A[c] = B[c];
+                }
+        }
+#pragma omp parallel for num_threads(nthreads) schedule(static)
+        for (i = 1; i <= n - 2; i++) {
+            long j, k;
+            for (j = 1; j <= n - 2; j++)
+                for (k = 1; k <= n - 2; k++) {
+                    long c = (i * n + j) * n + k;
+                    B[c] = (A[c - nn] + A[c - n] + A[c - 1] + A[c + 1] + A[c + n] + A[c + nn]) / 6.0;
+                }
+        }
+    }
+    /* (identity 0.0 max loop value) max initial value 0.0 */
+    return Max(eps, 0.0);
+}
+
+/* ------------------------------------------------------------ SOR (ACROSS) */
+
+void orc_sor_init(long n, uint64_t seed, double *A) {
+    long i, j, k;
+    for (i = 0; i < n; i++)
+        for (j = 0; j < n; j++)
+            for (k = 0; k < n; k++) {
+                long lin = (i * n + j) * n + k;
+                A[lin] = (i == 0 || j == 0 || k == 0 || i == n - 1 || j == n - 1 || k == n - 1)
+                             ? 0.0
+                             : orc_u01(seed, 1, (uint64_t)lin);
+            }
+}
+
+/*
+ * One SOR sweep in sequential loop order (the only order the ACROSS
+ * dependences allow on one thread).  Returns the sequential-order residual
+ * (0.0 + s_seq) + 0.0; *s_canon (may be NULL) receives the canonical-tree one.
+ */
+double orc_sor_sweep(long n, double w, double *A, double *s_canon) {
+    long nn = n * n, m = n - 2, i, j, k, t = 0;
+    double s = 0.0;
+    double *terms = s_canon ? malloc(sizeof(double) * m * m * m) : 0;
+    for (i = 1; i <= n - 2; i++)
+        for (j = 1; j <= n - 2; j++)
+            for (k = 1; k <= n - 2; k++) {
+                long c = (i * n + j) * n + k;
+                double old = A[c];
+                double nv = (1.0 - w) * old + w / 6.0 * (A[c - nn] + A[c + nn] + A[c - n] + A[c + n] + A[c - 1] +
+                                                         A[c + 1]);
+                A[c] = nv;
+                s += (nv - old) * (nv - old);
+                if (terms)
+                    terms[t++] = (nv - old) * (nv - old);
+            }
+    if (s_canon) {
+        *s_canon = (0.0 + orc_canon_sum(terms, m * m, 1, n - 2)) + 0.0;
+        free(terms);
+    }
+    return (0.0 + s) + 0.0;
+}
+
+/* ------------------------------------------------------------ batched heat */
+
+long orc_heat_side(uint64_t seed, long k, long lo, long hi) {
+    double u = orc_u01(seed, 1000, (uint64_t)k);
+    long n = (long)floor((double)lo * pow((double)hi / (double)lo, u));
+    if (n < 3)
+        n = 3;
+    if (n > hi)
+        n = hi;
+    return n;
+}
+
+void orc_heat_init(long n, uint64_t seed, long k, double *U, double *V) {
+    long i, j;
+    for (i = 0; i < n; i++)
+        for (j = 0; j < n; j++) {
+            long lin = i * n + j;
+            U[lin] = (i == 0 || j == 0 || i == n - 1 || j == n - 1) ? 0.0 : orc_u01(seed, 1 + (uint64_t)k, (uint64_t)lin);
+            V[lin] = 0.0;
+        }
+}
+
+/*
+ * One heat step of one array: dst = src + c * lap5(src) over the interior.
+ * Outputs: *sum_seq = (0.0 + sequential sum) + 0.0, *sum_canon = canonical-tree
+ * sum, *mn / loc = MINLOC with init (1e300, {-1,-1}) and first-in-loop-order ties.
+ */
+void orc_heat_step(long n, double c, const double *src, double *dst, double *sum_seq, double *sum_canon, double *mn,
+                   int loc[2]) {
+    long m = n - 2, i, j, t = 0;
+    double s = 0.0, best = 1e300;
+    int l0 = -1, l1 = -1;
+    double *terms = sum_canon ? malloc(sizeof(double) * (m > 0 ? m * m : 1)) : 0;
+    for (i = 1; i <= n - 2; i++)
+        for (j = 1; j <= n - 2; j++) {
+            long q = i * n + j;
+            double v = src[q] + c * (src[q - n] + src[q + n] + src[q - 1] + src[q + 1] - 4.0 * src[q]);
+            dst[q] = v;
+            s += v;
+            if (terms)
+                terms[t++] = v;
+            if (v < best) {
+                best = v;
+                l0 = (int)i;
+                l1 = (int)j;
+            }
+        }
+    if (sum_seq)
+        *sum_seq = (0.0 + s) + 0.0;
+    if (sum_canon) {
+        *sum_canon = (0.0 + orc_canon_sum(terms, m, 1, n - 2)) + 0.0;
+        free(terms);
+    }
+    *mn = best;
+    loc[0] = l0;
+    loc[1] = l1;
+}
+
+int orc_max_threads(void) {
+#ifdef _OPENMP
+    return omp_get_max_threads();
+#else
+    return 1;
+#endif
+}

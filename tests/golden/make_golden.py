@@ -1,0 +1,122 @@
+"""Generate tests/golden/golden.json from the REFERENCE runtime.
+
+Builds the reference DVM-system runtime from its sources (oracle/ref.mk, host
+handlers only) together with the workload programs, runs each case with
+DVMH_NUM_THREADS=1 (sequential loop order) and records the outputs: reduction
+values as exact float.hex strings, final arrays as SHA-256 of their dense
+little-endian float64 bytes (and in full for tiny cases).
+
+Run here (needs the reference sources):  python tests/golden/make_golden.py
+"""
+import hashlib
+import json
+import os
+import subprocess
+import sys
+import tempfile
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+REF = os.environ.get("DVMH_REF_SRC", "/root/reference/dvm_sys")
+DRIVER = os.path.join(ROOT, "oracle", "_ref", "ref_driver")
+
+# (name, program, params, keep full arrays)
+CASES = [
+    ("jac2d_n12_it4", "jac2d", [12, 4, 5], True),
+    ("jac2d_n3_it2", "jac2d", [3, 2, 9], True),
+    ("jac2d_n67_it7", "jac2d", [67, 7, 21], False),
+    ("jac2d_n1024_it100", "jac2d", [1024, 100, 20261203], False),
+    ("jac3d_n10_it3", "jac3d", [10, 3, 7], True),
+    ("jac3d_n3_it2", "jac3d", [3, 2, 3], True),
+    ("jac3d_n4_it3", "jac3d", [4, 3, 4], True),
+    ("jac3d_n67_it3", "jac3d", [67, 3, 20261204], False),
+    ("jac3d_n130_it2", "jac3d", [130, 2, 20261204], False),
+    ("sor3d_n10_sw3", "sor3d", [10, 3, 1.5, 11], True),
+    ("sor3d_n5_sw2", "sor3d", [5, 2, 1.5, 2], True),
+    ("sor3d_n35_sw3", "sor3d", [35, 3, 1.5, 20261205], False),
+    ("sor3d_n70_sw2", "sor3d", [70, 2, 1.5, 20261205], False),
+    ("heat_c5_s3", "heat", [5, 5, 40, 3, 0.2, 13], True),
+    ("heat_c24_s6", "heat", [24, 3, 150, 6, 0.2, 20261206], False),
+]
+
+
+def sha(a):
+    return hashlib.sha256(np.ascontiguousarray(a, dtype="<f8").tobytes()).hexdigest()
+
+
+def hx(a):
+    return [float(x).hex() for x in np.asarray(a, dtype=np.float64).ravel()]
+
+
+def build():
+    subprocess.check_call(["make", "-s", "-f", "oracle/ref.mk", "-j8", "REF=" + REF], cwd=ROOT)
+
+
+def run(prog, params):
+    with tempfile.TemporaryDirectory() as td:
+        out = os.path.join(td, "o.bin")
+        env = dict(os.environ, DVMH_NUM_THREADS="1", OMP_SCHEDULE="static")
+        subprocess.check_call([DRIVER, prog, out] + [str(p) for p in params], cwd=td, env=env,
+                              stdout=subprocess.DEVNULL)
+        return open(out, "rb").read()
+
+
+def case(name, prog, params, full):
+    raw = run(prog, params)
+    rec = {"prog": prog, "params": params}
+    if prog in ("jac2d", "jac3d"):
+        n, it = params[0], params[1]
+        cells = n ** (2 if prog == "jac2d" else 3)
+        d = np.frombuffer(raw, dtype="<f8")
+        rec["eps"] = hx(d[:it])
+        A, B = d[it:it + cells], d[it + cells:it + 2 * cells]
+        rec["A_sha256"], rec["B_sha256"] = sha(A), sha(B)
+        if full:
+            rec["A"], rec["B"] = hx(A), hx(B)
+    elif prog == "sor3d":
+        n, sw = params[0], params[1]
+        d = np.frombuffer(raw, dtype="<f8")
+        rec["s"] = hx(d[:sw])
+        A = d[sw:sw + n ** 3]
+        rec["A_sha256"] = sha(A)
+        if full:
+            rec["A"] = hx(A)
+    else:
+        cnt, steps = params[0], params[3]
+        off = 0
+        sides = np.frombuffer(raw[off:off + 8 * cnt], dtype="<i8")
+        off += 8 * cnt
+        sums = np.frombuffer(raw[off:off + 8 * cnt * steps], dtype="<f8")
+        off += 8 * cnt * steps
+        mins = np.frombuffer(raw[off:off + 8 * cnt * steps], dtype="<f8")
+        off += 8 * cnt * steps
+        locs = np.frombuffer(raw[off:off + 8 * cnt * steps], dtype="<i4")
+        off += 8 * cnt * steps
+        rec["sides"] = [int(s) for s in sides]
+        rec["sums"], rec["mins"] = hx(sums), hx(mins)
+        rec["locs"] = [int(x) for x in locs]
+        finals = []
+        for s in sides:
+            a = np.frombuffer(raw[off:off + 8 * int(s) * int(s)], dtype="<f8")
+            off += 8 * int(s) * int(s)
+            finals.append(sha(a) if not full else hx(a))
+        rec["final_sha256" if not full else "final"] = finals
+    return rec
+
+
+def main():
+    build()
+    out = {"generator": "tests/golden/make_golden.py", "runtime": "reference host handlers, DVMH_NUM_THREADS=1",
+           "cases": {}}
+    for name, prog, params, full in CASES:
+        print("case", name, file=sys.stderr)
+        out["cases"][name] = case(name, prog, params, full)
+    path = os.path.join(ROOT, "tests", "golden", "golden.json")
+    with open(path, "w") as f:
+        json.dump(out, f, indent=0, sort_keys=True)
+    print("wrote", path, os.path.getsize(path), "bytes", file=sys.stderr)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,120 @@
+"""The CPU restatement (oracle/restate.c) against outputs of the reference
+runtime itself (tests/golden/golden.json, made by tests/golden/make_golden.py
+from the reference's host handlers, sequential order)."""
+import hashlib
+import os
+
+import numpy as np
+import pytest
+
+from oracle import orc
+
+
+def sha(a):
+    return hashlib.sha256(np.ascontiguousarray(a, dtype="<f8").tobytes()).hexdigest()
+
+
+def unhex(xs):
+    return np.array([float.fromhex(x) for x in xs])
+
+
+def jac_cases(golden):
+    return [k for k, v in golden.items() if v["prog"] in ("jac2d", "jac3d") and v["params"][0] <= 130]
+
+
+def test_golden_present(golden):
+    progs = {v["prog"] for v in golden.values()}
+    assert progs == {"jac2d", "jac3d", "sor3d", "heat"}
+
+
+@pytest.mark.parametrize("rank", [2, 3])
+def test_jacobi_vs_reference(golden, rank):
+    for name, c in golden.items():
+        if c["prog"] != "jac%dd" % rank or c["params"][0] > 130:
+            continue
+        n, it, seed = c["params"]
+        eps, A, B = orc.jacobi_run(rank, n, it, seed)
+        assert np.array_equal(eps, unhex(c["eps"])), name
+        assert sha(A) == c["A_sha256"] and sha(B) == c["B_sha256"], name
+        if "A" in c:
+            assert np.array_equal(A, unhex(c["A"])) and np.array_equal(B, unhex(c["B"])), name
+
+
+def test_jacobi2d_full_config_vs_reference(golden):
+    """The CPU-runnable configuration: 1024^2, 100 iterations (about 1 s)."""
+    c = golden["jac2d_n1024_it100"]
+    n, it, seed = c["params"]
+    eps, A, B = orc.jacobi_run(2, n, it, seed, threads=4)
+    assert np.array_equal(eps, unhex(c["eps"]))
+    assert sha(A) == c["A_sha256"] and sha(B) == c["B_sha256"]
+
+
+def test_jacobi_thread_count_invariant():
+    e1, A1, B1 = orc.jacobi_run(3, 21, 3, 99, threads=1)
+    e4, A4, B4 = orc.jacobi_run(3, 21, 3, 99, threads=4)
+    assert np.array_equal(e1, e4) and np.array_equal(A1, A4) and np.array_equal(B1, B4)
+
+
+def test_sor_vs_reference(golden):
+    for name, c in golden.items():
+        if c["prog"] != "sor3d":
+            continue
+        n, sw, omega, seed = c["params"]
+        seq, can, A = orc.sor_run(n, sw, omega, seed)
+        assert np.array_equal(seq, unhex(c["s"])), name
+        assert sha(A) == c["A_sha256"], name
+        # canonical tree: same value up to the forward error bound of summation
+        assert np.allclose(can, seq, rtol=1e-12, atol=0), name
+
+
+def test_heat_vs_reference(golden):
+    for name, c in golden.items():
+        if c["prog"] != "heat":
+            continue
+        cnt, lo, hi, steps, coef, seed = c["params"]
+        r = orc.heat_run(cnt, lo, hi, steps, coef, seed)
+        assert r["sides"] == c["sides"], name
+        assert np.array_equal(r["sums_seq"].ravel(), unhex(c["sums"])), name
+        assert np.array_equal(r["mins"].ravel(), unhex(c["mins"])), name
+        assert r["locs"].ravel().tolist() == c["locs"], name
+        key = "final" if "final" in c else "final_sha256"
+        for k, f in enumerate(r["finals"]):
+            if key == "final":
+                assert np.array_equal(f, unhex(c["final"][k])), name
+            else:
+                assert sha(f) == c["final_sha256"][k], name
+
+
+def test_pairwise_tree_identity():
+    """-0.0 padding is exact: a tree over n leaves equals the tree over the next power of two."""
+    rng = np.random.default_rng(1)
+    v = rng.standard_normal(37)
+    a = orc.lib().orc_pairwise_sum(orc.P(v.copy()), 37)
+    w = np.concatenate([v, np.full(27, -0.0)])
+    b = orc.lib().orc_pairwise_sum(orc.P(w.copy()), 64)
+    assert a == b
+    z = np.array([-0.0, -0.0, -0.0])
+    assert np.signbit(orc.lib().orc_pairwise_sum(orc.P(z), 3))
+
+
+def test_canonical_chunking_matches_manual():
+    rng = np.random.default_rng(2)
+    rows, lo, hi = 5, 1, 130
+    t = rng.standard_normal((rows, hi - lo + 1))
+    got = orc.lib().orc_canon_sum(orc.P(t.copy()), rows, lo, hi)
+    items = []
+    for r in range(rows):
+        for c in range(lo // 64, hi // 64 + 1):
+            leaf = [t[r, k - lo] if lo <= k <= hi else -0.0 for k in range(64 * c, 64 * c + 64)]
+            leaf = np.array(leaf)
+            items.append(orc.lib().orc_pairwise_sum(orc.P(leaf), 64))
+    items = np.array(items)
+    assert got == orc.lib().orc_pairwise_sum(orc.P(items), len(items))
+
+
+@pytest.mark.skipif(not os.path.isdir(os.environ.get("DVMH_REF_SRC", "/root/reference/dvm_sys")),
+                    reason="reference sources not present (GPU box)")
+def test_reference_runtime_builds():
+    from oracle import build
+    drv = build.build_reference()
+    assert drv and os.path.exists(drv)
