@@ -1,0 +1,710 @@
+// Jacobi loop kernels (2-D 5-point and 3-D 7-point, FP64) for sm_103a.
+//
+// The loops are those of examples/Performance/jac3d_perf.c:56-73 and
+// examples/Jacobi/jac2d.c:49-64 with FP64 data:
+//   update : tmp = fabs(B-A); eps = Max(tmp, eps); A = B
+//   stencil: B = (A[i-1][j][k] + A[i][j-1][k] + A[i][j][k-1] + A[i][j][k+1]
+//                 + A[i][j+1][k] + A[i+1][j][k]) / 6.0          (3-D)
+//            B = (A[i-1][j] + A[i][j-1] + A[i][j+1] + A[i+1][j]) / 4.0  (2-D)
+// Sums are evaluated left to right exactly as written; the build uses
+// -fmad=false so no product is contracted into an FMA.
+//
+// GB300 executes 2 FP64 thread-operations per clock per SM, so FP64 issue --
+// not HBM -- bounds these loops when every operation is a native FP64 one.
+// Here the division is done exactly on the integer pipe (sf::div3p2 /
+// sf::scale_down), MAX compares bit patterns as integers, and `native` of a
+// cell's FP64 additions run on the FP64 unit while the rest run on the
+// integer pipe (sf::add), bit for bit the same (softfp64.cuh).  `native` is a
+// launch parameter the tuner chooses.
+//
+// Layout: innermost axis contiguous, rows 16-byte aligned (the runtime pads
+// device rows), so element pairs (2p, 2p+1) are loaded and stored as one
+// 128-bit access.  The stencil kernels stream the outermost axis through
+// registers (plane i-1, i, i+1 per thread) and stage plane i with its halo in
+// shared memory (2.5-D blocking): every A element comes from HBM once.
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "../../../include/dvmh_gb.h"
+#include "../../../include/dvmh_gb_kernels.h"
+#include "softfp64.cuh"
+
+namespace {
+
+constexpr int UPD_THREADS = 256;
+constexpr int UPD_CTAS_PER_SM = 8;
+
+int smCount() {
+    static int n = 0;
+    if (!n) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+        if (n <= 0) n = 152;
+    }
+    return n;
+}
+
+__device__ __forceinline__ double2 ld2cs(const double *p) { return __ldcs(reinterpret_cast<const double2 *>(p)); }
+__device__ __forceinline__ double2 ld2(const double *p) { return *reinterpret_cast<const double2 *>(p); }
+__device__ __forceinline__ void st2(double *p, double2 v) { *reinterpret_cast<double2 *>(p) = v; }
+__device__ __forceinline__ void st2cs(double *p, double2 v) { __stcs(reinterpret_cast<double2 *>(p), v); }
+
+__device__ __forceinline__ double maxOf(double tmp, double eps) { return tmp > eps ? tmp : eps; }  // Max(tmp, eps)
+
+// CTA-wide maximum (any order: MAX is order-independent); thread 0 gets it
+__device__ __forceinline__ double ctaMax(double m, double *sh) {
+    for (int o = 16; o > 0; o >>= 1) m = maxOf(__shfl_xor_sync(0xffffffffu, m, o), m);
+    const int warp = (threadIdx.x + threadIdx.y * blockDim.x) >> 5, lane = threadIdx.x & 31;
+    const int nw = (blockDim.x * blockDim.y) >> 5;
+    if (lane == 0) sh[warp] = m;
+    __syncthreads();
+    if (warp == 0) {
+        m = lane < nw ? sh[lane] : -__builtin_huge_val();
+        for (int o = 16; o > 0; o >>= 1) m = maxOf(__shfl_xor_sync(0xffffffffu, m, o), m);
+    }
+    return m;
+}
+
+// ---------------------------------------------------------------- update loop (2-D and 3-D)
+
+// Rows are (i, j) pairs of the box (nj = 1 and s1 = 0 in 2-D); a warp handles
+// 32 element pairs of one row per unit; units are strided over the grid.
+__global__ void __launch_bounds__(UPD_THREADS) kUpdate(double *A, const double *__restrict__ B, long s0, long s1,
+                                                       long lo0, long lo1, long lo2, long hi2, unsigned nj,
+                                                       unsigned units, unsigned nseg, long p0, long p1,
+                                                       double *items, int native) {
+    __shared__ double sh[UPD_THREADS / 32];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    uint64_t mb = 0;
+    bool seen = false;
+    const unsigned wstride = gridDim.x * (UPD_THREADS / 32);
+#pragma unroll 2
+    for (unsigned u = blockIdx.x * (UPD_THREADS / 32) + warp; u < units; u += wstride) {
+        unsigned row = u / nseg, seg = u - row * nseg;
+        unsigned ri = row / nj, rj = row - ri * nj;
+        long p = p0 + (long)seg * 32 + lane;
+        if (p <= p1) {
+            long k0 = 2 * p;
+            long off = (lo0 + ri) * s0 + (lo1 + rj) * s1 + k0;
+            double2 b = ld2cs(B + off), a = ld2cs(A + off);
+            bool in0 = k0 >= lo2 && k0 <= hi2, in1 = k0 + 1 >= lo2 && k0 + 1 <= hi2;
+            if (in0) mb = sf::absmax_bits(native ? sf::nadd(b.x, -a.x) : sf::sub(b.x, a.x), mb);
+            if (in1) mb = sf::absmax_bits(native ? sf::nadd(b.y, -a.y) : sf::sub(b.y, a.y), mb);
+            seen = seen || in0 || in1;
+            if (in0 && in1) st2cs(A + off, b);
+            else if (in0) A[off] = b.x;
+            else if (in1) A[off + 1] = b.y;
+        }
+    }
+    double m = seen ? sf::from(mb) : -__builtin_huge_val();
+    m = ctaMax(m, sh);
+    if (threadIdx.x == 0) items[blockIdx.x] = m;
+}
+
+struct UpdGeom {
+    unsigned units, nseg, nj;
+    long p0, p1;
+    long blocks;
+    bool ok;
+};
+
+UpdGeom updGeom(long ni, long nj, long lo2, long hi2) {
+    UpdGeom g{};
+    g.p0 = lo2 >> 1;
+    g.p1 = hi2 >> 1;
+    long nseg = (g.p1 - g.p0 + 1 + 31) / 32;
+    long units = ni * nj * nseg;
+    g.ok = ni > 0 && nj > 0 && hi2 >= lo2 && lo2 >= 0 && units < (1L << 31);
+    g.units = (unsigned)units;
+    g.nseg = (unsigned)nseg;
+    g.nj = (unsigned)nj;
+    long want = (units + UPD_THREADS / 32 - 1) / (UPD_THREADS / 32);
+    long cap = (long)smCount() * UPD_CTAS_PER_SM;
+    g.blocks = want < cap ? want : cap;
+    if (g.blocks < 1) g.blocks = 1;
+    return g;
+}
+
+// ---------------------------------------------------------------- 3-D stencil / fused (2.5-D blocking)
+
+constexpr int TX = 32;  // lanes: element pairs along k (64 elements)
+constexpr int TY = 8;   // warps: rows along j
+// rows per thread: 2 for the stencil loop, 1 for the fused loops (register budget)
+constexpr int JT_PLAIN = 2, JT_FUSED = 1;
+constexpr int SW = 66;  // shared row: k = kb-1 .. kb+64
+
+struct Box3 {
+    long s0, s1;
+    long e0, e1, e2;
+    long lo0, lo1, lo2, hi0, hi1, hi2;
+};
+
+__device__ __forceinline__ bool inArr3(const Box3 &b, long i, long j, long k) {
+    return i >= 0 && i < b.e0 && j >= 0 && j < b.e1 && k >= 0 && k < b.e2;
+}
+__device__ __forceinline__ bool inBox3(const Box3 &b, long i, long j, long k) {
+    return i >= b.lo0 && i <= b.hi0 && j >= b.lo1 && j <= b.hi1 && k >= b.lo2 && k <= b.hi2;
+}
+
+// element pair (k, k+1), k even, guarded by the array bounds (0 outside)
+__device__ __forceinline__ double2 ldPair(const double *X, const Box3 &b, long i, long j, long k) {
+    double2 v = make_double2(0.0, 0.0);
+    if (i < 0 || i >= b.e0 || j < 0 || j >= b.e1) return v;
+    const double *p = X + i * b.s0 + j * b.s1 + k;
+    if (k >= 0 && k + 1 < b.e2) return ld2(p);
+    if (k >= 0 && k < b.e2) v.x = p[0];
+    if (k + 1 >= 0 && k + 1 < b.e2) v.y = p[1];
+    return v;
+}
+__device__ __forceinline__ double ldOne(const double *X, const Box3 &b, long i, long j, long k) {
+    return inArr3(b, i, j, k) ? X[i * b.s0 + j * b.s1 + k] : 0.0;
+}
+
+// FUSED = false: plain stencil, source = A.
+// FUSED = true : source of the stencil is A_new = (x in box ? B : A) (the update
+// loop's A = B applied), own cells also update A and eps; output goes to Bnew.
+// (((((a + b) + c) + d) + e) + f) / 6.0: the first N additions on the FP64
+// unit, the others and the division on the integer pipe (fast paths)
+template <int N>
+__device__ __forceinline__ double stencil7(double a, double b, double c, double d, double e, double f, bool &spc) {
+    if (N >= 5)  // all additions native: the division's rare native fallback is a real branch
+        return sf::div3p2(sf::nadd(sf::nadd(sf::nadd(sf::nadd(sf::nadd(a, b), c), d), e), f), 1);
+    double t = N > 0 ? sf::nadd(a, b) : sf::add_fast(a, b, spc);
+    t = N > 1 ? sf::nadd(t, c) : sf::add_fast(t, c, spc);
+    t = N > 2 ? sf::nadd(t, d) : sf::add_fast(t, d, spc);
+    t = N > 3 ? sf::nadd(t, e) : sf::add_fast(t, e, spc);
+    t = N > 4 ? sf::nadd(t, f) : sf::add_fast(t, f, spc);
+    return sf::div3p2_fast(t, 1, spc);
+}
+
+// (((a + b) + c) + d) / 4.0 likewise (x / 4.0 == x * 0.25 exactly)
+template <int N>
+__device__ __forceinline__ double stencil5(double a, double b, double c, double d, bool &spc) {
+    double t = N > 0 ? sf::nadd(a, b) : sf::add_fast(a, b, spc);
+    t = N > 1 ? sf::nadd(t, c) : sf::add_fast(t, c, spc);
+    t = N > 2 ? sf::nadd(t, d) : sf::add_fast(t, d, spc);
+    return sf::scale_down_fast(t, 2, spc);
+}
+
+template <bool FUSED, int NATIVE, int JT>
+__global__ void __launch_bounds__(TX *TY, 3) kStencil3(double *A, const double *B, double *Out, Box3 b, long p0,
+                                                     int ichunk, double *items) {
+    constexpr int TJ = TY * JT;
+    __shared__ double sm[TJ + 2][SW];
+    __shared__ double shr[TX * TY / 32];
+    const int lane = threadIdx.x, ty = threadIdx.y;
+    const long kb = 2 * (p0 + (long)blockIdx.x * TX);
+    const long jb = b.lo1 + (long)blockIdx.y * TJ;
+    const long ib = b.lo0 + (long)blockIdx.z * ichunk;
+    long ie = ib + ichunk - 1;
+    if (ie > b.hi0) ie = b.hi0;
+    const long k = kb + 2 * lane;
+    const double *Src = FUSED ? B : A;
+
+    // source value of a pair: in the fused loop, cells outside the box keep A
+    auto srcPair = [&](long i, long j, long kk) -> double2 {
+        if (!FUSED) return ldPair(A, b, i, j, kk);
+        double2 v = ldPair(B, b, i, j, kk);
+        bool x0 = inBox3(b, i, j, kk), x1 = inBox3(b, i, j, kk + 1);
+        if (!(x0 && x1)) {
+            double2 a = ldPair(A, b, i, j, kk);
+            if (!x0) v.x = a.x;
+            if (!x1) v.y = a.y;
+        }
+        return v;
+    };
+    auto srcOne = [&](long i, long j, long kk) -> double {
+        if (!FUSED) return ldOne(A, b, i, j, kk);
+        return inBox3(b, i, j, kk) ? ldOne(B, b, i, j, kk) : ldOne(A, b, i, j, kk);
+    };
+    (void)Src;
+
+    double2 am[JT], ac[JT], ap[JT];
+    double hcc[JT], hcn[JT];
+    double2 hrc = make_double2(0.0, 0.0), hrn = hrc;
+    const long hrow = (ty == 0) ? jb - 1 : jb + TJ;  // halo row this thread may own
+    const bool ownsRowHalo = (ty == 0) || (ty == TY - 1);
+    const long hcol = (lane == 0) ? kb - 1 : kb + 2 * TX;
+    const bool ownsColHalo = (lane == 0) || (lane == TX - 1);
+
+#pragma unroll
+    for (int r = 0; r < JT; r++) {
+        long j = jb + ty + TY * r;
+        am[r] = srcPair(ib - 1, j, k);
+        ac[r] = srcPair(ib, j, k);
+        hcc[r] = ownsColHalo ? srcOne(ib, j, hcol) : 0.0;
+    }
+    if (ownsRowHalo) hrc = srcPair(ib, hrow, k);
+
+    uint64_t mb = 0;
+    bool seen = false;
+    for (long i = ib; i <= ie; i++) {
+        // prefetch plane i+1 and, in the fused loop, A_old of own cells in plane i
+        double2 aold[JT];
+#pragma unroll
+        for (int r = 0; r < JT; r++) {
+            long j = jb + ty + TY * r;
+            ap[r] = srcPair(i + 1, j, k);
+            hcn[r] = ownsColHalo ? srcOne(i + 1, j, hcol) : 0.0;
+            if (FUSED) aold[r] = ldPair(A, b, i, j, k);
+        }
+        if (ownsRowHalo) hrn = srcPair(i + 1, hrow, k);
+
+        // stage plane i
+#pragma unroll
+        for (int r = 0; r < JT; r++) {
+            sm[1 + ty + TY * r][1 + 2 * lane] = ac[r].x;
+            sm[1 + ty + TY * r][2 + 2 * lane] = ac[r].y;
+            if (ownsColHalo) sm[1 + ty + TY * r][lane == 0 ? 0 : SW - 1] = hcc[r];
+        }
+        if (ty == 0) {
+            sm[0][1 + 2 * lane] = hrc.x;
+            sm[0][2 + 2 * lane] = hrc.y;
+        } else if (ty == TY - 1) {
+            sm[TJ + 1][1 + 2 * lane] = hrc.x;
+            sm[TJ + 1][2 + 2 * lane] = hrc.y;
+        }
+        __syncthreads();
+
+        // all cells of this thread first (fast paths), then one warp-uniform
+        // native recompute for lanes that met a special operand or result
+        double v[JT][2], dif[JT][2];
+        bool spc = false;
+#pragma unroll
+        for (int r = 0; r < JT; r++) {
+            const int row = 1 + ty + TY * r;
+#pragma unroll
+            for (int e = 0; e < 2; e++) {
+                const int c = 1 + 2 * lane + e;
+                double ame = e ? am[r].y : am[r].x, ape = e ? ap[r].y : ap[r].x;
+                v[r][e] = stencil7<FUSED ? NATIVE - 1 : NATIVE>(ame, sm[row - 1][c], sm[row][c - 1], sm[row][c + 1],
+                                                                sm[row + 1][c], ape, spc);
+                if (FUSED) {
+                    double bo = e ? ac[r].y : ac[r].x, ao = e ? aold[r].y : aold[r].x;
+                    dif[r][e] = NATIVE > 0 ? sf::nadd(bo, -ao) : sf::sub_fast(bo, ao, spc);
+                }
+            }
+        }
+        if (__any_sync(0xffffffffu, spc)) {
+            if (spc) {
+#pragma unroll
+                for (int r = 0; r < JT; r++) {
+                    const int row = 1 + ty + TY * r;
+#pragma unroll
+                    for (int e = 0; e < 2; e++) {
+                        const int c = 1 + 2 * lane + e;
+                        double ame = e ? am[r].y : am[r].x, ape = e ? ap[r].y : ap[r].x;
+                        v[r][e] = sf::ndiv(sf::nadd(sf::nadd(sf::nadd(sf::nadd(sf::nadd(ame, sm[row - 1][c]),
+                                                                           sm[row][c - 1]), sm[row][c + 1]),
+                                                             sm[row + 1][c]), ape), 6.0);
+                        if (FUSED) dif[r][e] = sf::nadd(e ? ac[r].y : ac[r].x, -(e ? aold[r].y : aold[r].x));
+                    }
+                }
+            }
+        }
+#pragma unroll
+        for (int r = 0; r < JT; r++) {
+            const long j = jb + ty + TY * r;
+            if (j > b.hi1) continue;
+            bool in[2];
+#pragma unroll
+            for (int e = 0; e < 2; e++) in[e] = (k + e) >= b.lo2 && (k + e) <= b.hi2;
+            const long off = i * b.s0 + j * b.s1 + k;
+            if (FUSED) {
+                // update loop on own cells: eps = Max(|B-A|, eps); A = B
+                if (in[0]) mb = sf::absmax_bits(dif[r][0], mb);
+                if (in[1]) mb = sf::absmax_bits(dif[r][1], mb);
+                seen = seen || in[0] || in[1];
+                if (in[0] && in[1]) st2cs(A + off, ac[r]);
+                else if (in[0]) A[off] = ac[r].x;
+                else if (in[1]) A[off + 1] = ac[r].y;
+            }
+            if (in[0] && in[1]) st2cs(Out + off, make_double2(v[r][0], v[r][1]));
+            else if (in[0]) Out[off] = v[r][0];
+            else if (in[1]) Out[off + 1] = v[r][1];
+        }
+        __syncthreads();
+#pragma unroll
+        for (int r = 0; r < JT; r++) {
+            am[r] = ac[r];
+            ac[r] = ap[r];
+            hcc[r] = hcn[r];
+        }
+        hrc = hrn;
+    }
+    if (FUSED) {
+        double m = ctaMax(seen ? sf::from(mb) : -__builtin_huge_val(), shr);
+        if (ty == 0 && lane == 0)
+            items[blockIdx.x + gridDim.x * ((long)blockIdx.y + (long)gridDim.y * blockIdx.z)] = m;
+    }
+}
+
+struct St3Geom {
+    dim3 grid;
+    long p0;
+    int ichunk;
+    bool ok;
+};
+
+St3Geom st3Geom(const long lo[3], const long hi[3], int TJ) {
+    St3Geom g{};
+    g.ok = hi[0] >= lo[0] && hi[1] >= lo[1] && hi[2] >= lo[2] && lo[2] >= 0;
+    g.p0 = lo[2] >> 1;
+    long p1 = hi[2] >> 1;
+    long gx = (p1 - g.p0 + TX) / TX;
+    long gy = (hi[1] - lo[1] + TJ) / TJ;
+    long ni = hi[0] - lo[0] + 1;
+    // split the streamed axis so the grid covers the GPU about four times
+    long target = (long)smCount() * 4 * 4;
+    long chunks = (target + gx * gy - 1) / (gx * gy);
+    if (chunks < 1) chunks = 1;
+    if (chunks > ni) chunks = ni;
+    long ichunk = (ni + chunks - 1) / chunks;
+    if (ichunk < 8 && ni >= 8) ichunk = 8;
+    g.ichunk = (int)ichunk;
+    long gz = (ni + ichunk - 1) / ichunk;
+    g.ok = g.ok && gx < 65536 && gy < 65536 && gz < 65536;
+    g.grid = dim3((unsigned)gx, (unsigned)gy, (unsigned)gz);
+    return g;
+}
+
+// ---------------------------------------------------------------- 2-D stencil / fused (1.5-D blocking)
+
+constexpr int T2Y = 8;  // independent column strips per CTA (one per warp)
+
+struct Box2 {
+    long s0;
+    long e0, e1;
+    long lo0, lo1, hi0, hi1;
+};
+
+__device__ __forceinline__ double2 ldPair2(const double *X, const Box2 &b, long i, long k) {
+    double2 v = make_double2(0.0, 0.0);
+    if (i < 0 || i >= b.e0) return v;
+    const double *p = X + i * b.s0 + k;
+    if (k >= 0 && k + 1 < b.e1) return ld2(p);
+    if (k >= 0 && k < b.e1) v.x = p[0];
+    if (k + 1 >= 0 && k + 1 < b.e1) v.y = p[1];
+    return v;
+}
+__device__ __forceinline__ double ldOne2(const double *X, const Box2 &b, long i, long k) {
+    return (i >= 0 && i < b.e0 && k >= 0 && k < b.e1) ? X[i * b.s0 + k] : 0.0;
+}
+__device__ __forceinline__ bool inBox2(const Box2 &b, long i, long k) {
+    return i >= b.lo0 && i <= b.hi0 && k >= b.lo1 && k <= b.hi1;
+}
+
+template <bool FUSED, int NATIVE>
+__global__ void __launch_bounds__(TX *T2Y) kStencil2(double *A, const double *B, double *Out, Box2 b, long p0,
+                                                      long nstrips, int ichunk, double *items) {
+    __shared__ double sm[T2Y][SW];
+    __shared__ double shr[T2Y];
+    const int lane = threadIdx.x, ty = threadIdx.y;
+    const long strip = (long)blockIdx.x * T2Y + ty;
+    const bool active = strip < nstrips;
+    const long kb = 2 * (p0 + strip * TX);
+    const long ib = b.lo0 + (long)blockIdx.y * ichunk;
+    long ie = ib + ichunk - 1;
+    if (ie > b.hi0) ie = b.hi0;
+    const long k = kb + 2 * lane;
+    auto srcPair = [&](long i, long kk) -> double2 {
+        if (!FUSED) return ldPair2(A, b, i, kk);
+        double2 v = ldPair2(B, b, i, kk);
+        bool x0 = inBox2(b, i, kk), x1 = inBox2(b, i, kk + 1);
+        if (!(x0 && x1)) {
+            double2 a = ldPair2(A, b, i, kk);
+            if (!x0) v.x = a.x;
+            if (!x1) v.y = a.y;
+        }
+        return v;
+    };
+    auto srcOne = [&](long i, long kk) -> double {
+        if (!FUSED) return ldOne2(A, b, i, kk);
+        return inBox2(b, i, kk) ? ldOne2(B, b, i, kk) : ldOne2(A, b, i, kk);
+    };
+    const long hcol = (lane == 0) ? kb - 1 : kb + 2 * TX;
+    const bool ownsColHalo = (lane == 0) || (lane == TX - 1);
+    double2 am = make_double2(0.0, 0.0), ac = am, ap = am;
+    double hcc = 0.0, hcn = 0.0;
+    if (active) {
+        am = srcPair(ib - 1, k);
+        ac = srcPair(ib, k);
+        if (ownsColHalo) hcc = srcOne(ib, hcol);
+    }
+    uint64_t mb = 0;
+    bool seen = false;
+    for (long i = ib; i <= ie; i++) {
+        double2 aold = make_double2(0.0, 0.0);
+        if (active) {
+            ap = srcPair(i + 1, k);
+            if (ownsColHalo) hcn = srcOne(i + 1, hcol);
+            if (FUSED) aold = ldPair2(A, b, i, k);
+        }
+        sm[ty][1 + 2 * lane] = ac.x;
+        sm[ty][2 + 2 * lane] = ac.y;
+        if (ownsColHalo) sm[ty][lane == 0 ? 0 : SW - 1] = hcc;
+        __syncwarp();
+        double v[2], dif[2];
+        bool spc = false;
+#pragma unroll
+        for (int e = 0; e < 2; e++) {
+            const int c = 1 + 2 * lane + e;
+            double ame = e ? am.y : am.x, ape = e ? ap.y : ap.x;
+            // (((A[i-1][j] + A[i][j-1]) + A[i][j+1]) + A[i+1][j]) / 4.0
+            v[e] = stencil5<FUSED ? NATIVE - 1 : NATIVE>(ame, sm[ty][c - 1], sm[ty][c + 1], ape, spc);
+            if (FUSED) {
+                double bo = e ? ac.y : ac.x, ao = e ? aold.y : aold.x;
+                dif[e] = NATIVE > 0 ? sf::nadd(bo, -ao) : sf::sub_fast(bo, ao, spc);
+            }
+        }
+        if (__any_sync(0xffffffffu, spc)) {
+            if (spc) {
+#pragma unroll
+                for (int e = 0; e < 2; e++) {
+                    const int c = 1 + 2 * lane + e;
+                    double ame = e ? am.y : am.x, ape = e ? ap.y : ap.x;
+                    v[e] = sf::ndiv(sf::nadd(sf::nadd(sf::nadd(ame, sm[ty][c - 1]), sm[ty][c + 1]), ape), 4.0);
+                    if (FUSED) dif[e] = sf::nadd(e ? ac.y : ac.x, -(e ? aold.y : aold.x));
+                }
+            }
+        }
+        if (active) {
+            bool in[2];
+#pragma unroll
+            for (int e = 0; e < 2; e++) in[e] = (k + e) >= b.lo1 && (k + e) <= b.hi1;
+            const long off = i * b.s0 + k;
+            if (FUSED) {
+                if (in[0]) mb = sf::absmax_bits(dif[0], mb);
+                if (in[1]) mb = sf::absmax_bits(dif[1], mb);
+                seen = seen || in[0] || in[1];
+                if (in[0] && in[1]) st2cs(A + off, ac);
+                else if (in[0]) A[off] = ac.x;
+                else if (in[1]) A[off + 1] = ac.y;
+            }
+            if (in[0] && in[1]) st2cs(Out + off, make_double2(v[0], v[1]));
+            else if (in[0]) Out[off] = v[0];
+            else if (in[1]) Out[off + 1] = v[1];
+        }
+        __syncwarp();
+        am = ac;
+        ac = ap;
+        hcc = hcn;
+    }
+    if (FUSED) {
+        double m = seen ? sf::from(mb) : -__builtin_huge_val();
+        for (int o = 16; o > 0; o >>= 1) m = maxOf(__shfl_xor_sync(0xffffffffu, m, o), m);
+        if (lane == 0) shr[ty] = m;
+        __syncthreads();
+        if (ty == 0 && lane == 0) {
+            double r = shr[0];
+            for (int w = 1; w < T2Y; w++) r = maxOf(shr[w], r);
+            items[blockIdx.x + (long)gridDim.x * blockIdx.y] = r;
+        }
+    }
+}
+
+struct St2Geom {
+    dim3 grid;
+    long p0, nstrips;
+    int ichunk;
+    bool ok;
+};
+
+St2Geom st2Geom(const long lo[2], const long hi[2]) {
+    St2Geom g{};
+    g.ok = hi[0] >= lo[0] && hi[1] >= lo[1] && lo[1] >= 0;
+    g.p0 = lo[1] >> 1;
+    long p1 = hi[1] >> 1;
+    g.nstrips = (p1 - g.p0 + TX) / TX;
+    long gx = (g.nstrips + T2Y - 1) / T2Y;
+    long ni = hi[0] - lo[0] + 1;
+    long target = (long)smCount() * 8 * 4;
+    long chunks = (target + gx - 1) / gx;
+    if (chunks < 1) chunks = 1;
+    if (chunks > ni) chunks = ni;
+    long ichunk = (ni + chunks - 1) / chunks;
+    if (ichunk < 16 && ni >= 16) ichunk = 16;
+    g.ichunk = (int)ichunk;
+    long gy = (ni + ichunk - 1) / ichunk;
+    g.ok = g.ok && gx < (1L << 31) && gy < 65536;
+    g.grid = dim3((unsigned)gx, (unsigned)gy, 1);
+    return g;
+}
+
+// ---------------------------------------------------------------- copy outside a box
+
+struct Slabs {
+    int n;
+    int rank;
+    long lo[6][3], cnt[6][3];
+    long start[7];
+    long st[3];
+};
+
+__global__ void kCopyOutside(const double *__restrict__ src, double *__restrict__ dst, Slabs s) {
+    long total = s.start[s.n];
+    for (long t = blockIdx.x * (long)blockDim.x + threadIdx.x; t < total; t += (long)gridDim.x * blockDim.x) {
+        int q = 0;
+        while (t >= s.start[q + 1]) q++;
+        long r = t - s.start[q], off = 0;
+        for (int d = s.rank - 1; d >= 0; d--) {
+            long c = r % s.cnt[q][d];
+            r /= s.cnt[q][d];
+            off += (s.lo[q][d] + c) * s.st[d];
+        }
+        dst[off] = src[off];
+    }
+}
+
+// native = FP64 operations per cell on the FP64 unit (clamped to the kernel's count)
+template <bool FUSED>
+void launch3(int native, const St3Geom &g, double *A, const double *B, double *Out, const Box3 &b, double *items,
+             cudaStream_t s) {
+    const int n = FUSED ? 6 : 5;
+    native = native < 0 ? 0 : (native > n ? n : native);
+    dim3 blk(TX, TY);
+    switch (native) {
+#define C3(N)                                                                                   \
+    case N: kStencil3<FUSED, (FUSED ? N : (N > 5 ? 5 : N)), (FUSED ? JT_FUSED : JT_PLAIN)><<<g.grid, blk, 0, s>>>(A, B, Out, b, g.p0, g.ichunk, items); break;
+        C3(0) C3(1) C3(2) C3(3) C3(4) C3(5) C3(6)
+#undef C3
+    }
+}
+
+template <bool FUSED>
+void launch2(int native, const St2Geom &g, double *A, const double *B, double *Out, const Box2 &b, double *items,
+             cudaStream_t s) {
+    const int n = FUSED ? 4 : 3;
+    native = native < 0 ? 0 : (native > n ? n : native);
+    dim3 blk(TX, T2Y);
+    switch (native) {
+#define C2(N)                                                                                          \
+    case N: kStencil2<FUSED, (FUSED ? N : (N > 3 ? 3 : N))><<<g.grid, blk, 0, s>>>(A, B, Out, b, g.p0, g.nstrips, g.ichunk, items); break;
+        C2(0) C2(1) C2(2) C2(3) C2(4)
+#undef C2
+    }
+}
+
+}  // namespace
+
+extern "C" {
+
+long dvmhgb_jac3d_update_items(const long lo[3], const long hi[3]) {
+    return updGeom(hi[0] - lo[0] + 1, hi[1] - lo[1] + 1, lo[2], hi[2]).blocks;
+}
+
+int dvmhgb_jac3d_update(double *A, const double *B, const long st[3], const long lo[3], const long hi[3],
+                        double *items, int native, void *stream) {
+    UpdGeom g = updGeom(hi[0] - lo[0] + 1, hi[1] - lo[1] + 1, lo[2], hi[2]);
+    if (!g.ok || !A || !B || !items || st[2] != 1) return -1;
+    kUpdate<<<(unsigned)g.blocks, UPD_THREADS, 0, (cudaStream_t)stream>>>(A, B, st[0], st[1], lo[0], lo[1], lo[2],
+                                                                          hi[2], g.nj, g.units, g.nseg, g.p0, g.p1,
+                                                                          items, native);
+    dvmhgb_count_launches(1);
+    return cudaGetLastError() == cudaSuccess ? 0 : -1;
+}
+
+int dvmhgb_jac3d_stencil(const double *A, double *B, const long st[3], const long ext[3], const long lo[3],
+                         const long hi[3], int native, void *stream) {
+    St3Geom g = st3Geom(lo, hi, TY * JT_PLAIN);
+    if (!g.ok || !A || !B || st[2] != 1) return -1;
+    Box3 b{st[0], st[1], ext[0], ext[1], ext[2], lo[0], lo[1], lo[2], hi[0], hi[1], hi[2]};
+    launch3<false>(native, g, (double *)A, nullptr, B, b, nullptr, (cudaStream_t)stream);
+    dvmhgb_count_launches(1);
+    return cudaGetLastError() == cudaSuccess ? 0 : -1;
+}
+
+long dvmhgb_jac3d_fused_items(const long lo[3], const long hi[3]) {
+    St3Geom g = st3Geom(lo, hi, TY * JT_FUSED);
+    return (long)g.grid.x * g.grid.y * g.grid.z;
+}
+
+int dvmhgb_jac3d_fused(double *A, const double *B, double *Bnew, const long st[3], const long ext[3],
+                       const long lo[3], const long hi[3], double *items, int native, void *stream) {
+    St3Geom g = st3Geom(lo, hi, TY * JT_FUSED);
+    if (!g.ok || !A || !B || !Bnew || !items || st[2] != 1) return -1;
+    Box3 b{st[0], st[1], ext[0], ext[1], ext[2], lo[0], lo[1], lo[2], hi[0], hi[1], hi[2]};
+    launch3<true>(native, g, A, B, Bnew, b, items, (cudaStream_t)stream);
+    dvmhgb_count_launches(1);
+    if (cudaGetLastError() != cudaSuccess) return -1;
+    return dvmhgb_copy_outside_box(3, B, Bnew, st, ext, lo, hi, stream);
+}
+
+long dvmhgb_jac2d_update_items(const long lo[2], const long hi[2]) {
+    return updGeom(hi[0] - lo[0] + 1, 1, lo[1], hi[1]).blocks;
+}
+
+int dvmhgb_jac2d_update(double *A, const double *B, const long st[2], const long lo[2], const long hi[2],
+                        double *items, int native, void *stream) {
+    UpdGeom g = updGeom(hi[0] - lo[0] + 1, 1, lo[1], hi[1]);
+    if (!g.ok || !A || !B || !items || st[1] != 1) return -1;
+    kUpdate<<<(unsigned)g.blocks, UPD_THREADS, 0, (cudaStream_t)stream>>>(A, B, st[0], 0, lo[0], 0, lo[1], hi[1],
+                                                                          g.nj, g.units, g.nseg, g.p0, g.p1, items, native);
+    dvmhgb_count_launches(1);
+    return cudaGetLastError() == cudaSuccess ? 0 : -1;
+}
+
+int dvmhgb_jac2d_stencil(const double *A, double *B, const long st[2], const long ext[2], const long lo[2],
+                         const long hi[2], int native, void *stream) {
+    St2Geom g = st2Geom(lo, hi);
+    if (!g.ok || !A || !B || st[1] != 1) return -1;
+    Box2 b{st[0], ext[0], ext[1], lo[0], lo[1], hi[0], hi[1]};
+    launch2<false>(native, g, (double *)A, nullptr, B, b, nullptr, (cudaStream_t)stream);
+    dvmhgb_count_launches(1);
+    return cudaGetLastError() == cudaSuccess ? 0 : -1;
+}
+
+long dvmhgb_jac2d_fused_items(const long lo[2], const long hi[2]) {
+    St2Geom g = st2Geom(lo, hi);
+    return (long)g.grid.x * g.grid.y;
+}
+
+int dvmhgb_jac2d_fused(double *A, const double *B, double *Bnew, const long st[2], const long ext[2],
+                       const long lo[2], const long hi[2], double *items, int native, void *stream) {
+    St2Geom g = st2Geom(lo, hi);
+    if (!g.ok || !A || !B || !Bnew || !items || st[1] != 1) return -1;
+    Box2 b{st[0], ext[0], ext[1], lo[0], lo[1], hi[0], hi[1]};
+    launch2<true>(native, g, A, B, Bnew, b, items, (cudaStream_t)stream);
+    dvmhgb_count_launches(1);
+    if (cudaGetLastError() != cudaSuccess) return -1;
+    return dvmhgb_copy_outside_box(2, B, Bnew, st, ext, lo, hi, stream);
+}
+
+int dvmhgb_copy_outside_box(int rank, const double *src, double *dst, const long *st, const long *ext,
+                            const long *lo, const long *hi, void *stream) {
+    if (rank < 1 || rank > 3) return -1;
+    Slabs s{};
+    s.rank = rank;
+    for (int d = 0; d < rank; d++) s.st[d] = st[d];
+    s.start[0] = 0;
+    // slab (d, side): axis d outside [lo_d, hi_d] on one side, axes < d inside, axes > d anything
+    for (int d = 0; d < rank; d++)
+        for (int side = 0; side < 2; side++) {
+            long a = side == 0 ? 0 : hi[d] + 1, z = side == 0 ? lo[d] - 1 : ext[d] - 1;
+            if (z < a) continue;
+            int q = s.n;
+            long cells = 1;
+            for (int e = 0; e < rank; e++) {
+                long l, h;
+                if (e < d) { l = lo[e]; h = hi[e]; }
+                else if (e == d) { l = a; h = z; }
+                else { l = 0; h = ext[e] - 1; }
+                s.lo[q][e] = l;
+                s.cnt[q][e] = h - l + 1;
+                cells *= h - l + 1;
+            }
+            s.start[q + 1] = s.start[q] + cells;
+            s.n++;
+        }
+    if (s.n == 0) return 0;
+    long total = s.start[s.n];
+    long blocks = (total + 255) / 256;
+    if (blocks > (long)smCount() * 8) blocks = (long)smCount() * 8;
+    kCopyOutside<<<(unsigned)blocks, 256, 0, (cudaStream_t)stream>>>(src, dst, s);
+    dvmhgb_count_launches(1);
+    return cudaGetLastError() == cudaSuccess ? 0 : -1;
+}
+
+}  // extern "C"

@@ -1,0 +1,315 @@
+// IEEE-754 binary64 arithmetic on the integer pipe, bit-exact with the FP64
+// unit in round-to-nearest-even.
+//
+// Why: a GB300 SM executes 2 FP64 thread-operations per clock but 128
+// integer/FP32 thread-operations per clock.  An FP64 stencil therefore runs
+// out of FP64 issue long before it runs out of HBM bandwidth.  Moving part of
+// the FP64 operations of a cell onto the integer pipe -- with results
+// identical bit for bit -- lets both pipes work at once.
+//
+// Method (standard binary floating-point arithmetic, e.g. Goldberg 1991,
+// "What every computer scientist should know about floating-point arithmetic";
+// Muller et al., Handbook of Floating-Point Arithmetic, ch. 7-8): unpack the
+// 53-bit significands, align with a sticky bit, add/multiply exactly in
+// 64/128-bit integers, normalise, round to nearest even on the guard bit and
+// the sticky OR of the rest, repack.  Only the common case is emulated: both
+// operands and the result normal and finite.  Zeros, subnormals, infinities,
+// NaNs and results that would overflow or underflow take the native FP64
+// instruction, so the edge semantics are the hardware's by construction.
+//
+// sf_div3p2(x, k) = RN(x / (3 * 2^k)) (k >= 0): the exact quotient
+// floor(m * 2^11 / 3) of the significand by the multiply-high reciprocal
+// identity floor(n / 3) = floor(mulhi(n, 0xAAAAAAAAAAAAAAAB) / 2) for 64-bit n,
+// the remainder for the sticky bit, then rounding.  A quotient by 3 is never
+// exactly half-way between two doubles (the denominator is odd), so ties do
+// not arise; the rounding code still implements ties-to-even.
+//
+// The same source compiles for the host (the self-tests check it against the
+// host FPU) and for the device.
+#pragma once
+
+#include <cstdint>
+#include <cstring>
+
+#ifdef __CUDACC__
+#define SF_HD __host__ __device__ __forceinline__
+#else
+#define SF_HD static inline
+#endif
+
+namespace sf {
+
+constexpr uint64_t SIGN = 0x8000000000000000ull;
+constexpr uint64_t MANT = 0x000FFFFFFFFFFFFFull;
+constexpr uint64_t HID = 0x0010000000000000ull;
+constexpr uint64_t EXPINF = 0x7FF0000000000000ull;
+
+SF_HD uint64_t bits(double x) {
+#ifdef __CUDA_ARCH__
+    return (uint64_t)__double_as_longlong(x);
+#else
+    uint64_t b;
+    memcpy(&b, &x, 8);
+    return b;
+#endif
+}
+
+SF_HD double from(uint64_t b) {
+#ifdef __CUDA_ARCH__
+    return __longlong_as_double((long long)b);
+#else
+    double x;
+    memcpy(&x, &b, 8);
+    return x;
+#endif
+}
+
+SF_HD int clz64(uint64_t x) {
+#ifdef __CUDA_ARCH__
+    return __clzll((long long)x);
+#else
+    return x ? __builtin_clzll(x) : 64;
+#endif
+}
+
+SF_HD uint64_t mulhi(uint64_t a, uint64_t b) {
+#ifdef __CUDA_ARCH__
+    return __umul64hi(a, b);
+#else
+    return (uint64_t)(((unsigned __int128)a * b) >> 64);
+#endif
+}
+
+// The FP64 unit's own operations, as volatile inline PTX: the compiler may not
+// execute them speculatively, so an emulated operation never also issues the
+// native instruction it replaces.
+SF_HD double nadd(double a, double b) {
+#ifdef __CUDA_ARCH__
+    double r;
+    asm volatile("add.rn.f64 %0, %1, %2;" : "=d"(r) : "d"(a), "d"(b));
+    return r;
+#else
+    return a + b;
+#endif
+}
+SF_HD double nmul(double a, double b) {
+#ifdef __CUDA_ARCH__
+    double r;
+    asm volatile("mul.rn.f64 %0, %1, %2;" : "=d"(r) : "d"(a), "d"(b));
+    return r;
+#else
+    return a * b;
+#endif
+}
+SF_HD double ndiv(double a, double b) {
+#ifdef __CUDA_ARCH__
+    double r;
+    asm volatile("div.rn.f64 %0, %1, %2;" : "=d"(r) : "d"(a), "d"(b));
+    return r;
+#else
+    return a / b;
+#endif
+}
+
+// RN(a + b)
+SF_HD double add(double a, double b) {
+    uint64_t A = bits(a), B = bits(b);
+    uint64_t ea = (A >> 52) & 0x7FF, eb = (B >> 52) & 0x7FF;
+    if (ea - 1 >= 0x7FE || eb - 1 >= 0x7FE) return nadd(a, b);  // zero, subnormal, inf, nan
+    uint64_t absA = A & ~SIGN, absB = B & ~SIGN;
+    if (absA < absB) {
+        uint64_t t = A; A = B; B = t;
+        t = ea; ea = eb; eb = t;
+    }
+    uint64_t d = ea - eb;
+    if (d > 63) return from(A);  // |b| < ulp(a)/2^10: RN(a+b) = a
+    uint64_t ma = ((A & MANT) | HID) << 8;  // leading one at bit 60
+    uint64_t mb = ((B & MANT) | HID) << 8;
+    if (d) {
+        uint64_t lost = mb << (64 - d);
+        mb = (mb >> d) | (uint64_t)(lost != 0);
+    }
+    uint64_t s = ((A ^ B) & SIGN) ? ma - mb : ma + mb;
+    if (s == 0) return 0.0;  // x + (-x) = +0 in round-to-nearest
+    int lz = clz64(s);
+    int64_t e = (int64_t)ea;
+    if (lz == 2) {
+        s = (s >> 1) | (s & 1);
+        e += 1;
+    } else if (lz > 3) {
+        // exact: either no bit was lost (d <= 1) or the shift is one place and
+        // the sticky bit stays below the guard bit
+        s <<= (lz - 3);
+        e -= (lz - 3);
+    }
+    if (e <= 0) return nadd(a, b);  // subnormal result
+    uint64_t m = s >> 8;
+    uint32_t rem = (uint32_t)(s & 0xFF);
+    m += (uint64_t)((rem > 0x80) | ((rem == 0x80) & (uint32_t)(m & 1)));
+    if (m >> 53) {
+        m >>= 1;
+        e += 1;
+    }
+    if (e >= 0x7FF) return nadd(a, b);  // overflow
+    return from((A & SIGN) | ((uint64_t)e << 52) | (m & MANT));
+}
+
+SF_HD double sub(double a, double b) { return add(a, from(bits(b) ^ SIGN)); }
+
+// RN(a * b)
+SF_HD double mul(double a, double b) {
+    uint64_t A = bits(a), B = bits(b);
+    uint64_t ea = (A >> 52) & 0x7FF, eb = (B >> 52) & 0x7FF;
+    if (ea - 1 >= 0x7FE || eb - 1 >= 0x7FE) return nmul(a, b);
+    uint64_t ma = (A & MANT) | HID, mb = (B & MANT) | HID;
+    uint64_t lo = ma * mb, hi = mulhi(ma, mb);  // product in [2^104, 2^106)
+    int64_t e = (int64_t)ea + (int64_t)eb - 1023;
+    uint64_t m, guard, sticky;
+    if (hi >> 41) {  // bit 105 set
+        m = (hi << 11) | (lo >> 53);
+        guard = (lo >> 52) & 1;
+        sticky = lo & ((1ull << 52) - 1);
+        e += 1;
+    } else {
+        m = (hi << 12) | (lo >> 52);
+        guard = (lo >> 51) & 1;
+        sticky = lo & ((1ull << 51) - 1);
+    }
+    if (e <= 0) return nmul(a, b);  // subnormal or zero result: rounded at a coarser position
+    m += guard & (uint64_t)((sticky != 0) | (m & 1));
+    if (m >> 53) {
+        m >>= 1;
+        e += 1;
+    }
+    if (e >= 0x7FF) return nmul(a, b);  // overflow
+    return from(((A ^ B) & SIGN) | ((uint64_t)e << 52) | (m & MANT));
+}
+
+// RN(x / (3 * 2^k)), k >= 0
+SF_HD double div3p2(double x, int k) {
+    uint64_t X = bits(x);
+    uint64_t ex = (X >> 52) & 0x7FF;
+    if (ex - 1 >= 0x7FE) return ndiv(x, 3.0 * (double)(1ull << k));
+    uint64_t n = ((X & MANT) | HID) << 11;  // in [2^63, 2^64)
+    uint64_t q = mulhi(n, 0xAAAAAAAAAAAAAAABull) >> 1;
+    uint64_t r = n - 3 * q;
+    int64_t e;
+    uint64_t m, guard, sticky;
+    if (q >> 62) {
+        m = q >> 10;
+        guard = (q >> 9) & 1;
+        sticky = (q & 0x1FF) | r;
+        e = (int64_t)ex - 1;
+    } else {
+        m = q >> 9;
+        guard = (q >> 8) & 1;
+        sticky = (q & 0xFF) | r;
+        e = (int64_t)ex - 2;
+    }
+    e -= k;
+    if (e <= 0) return ndiv(x, 3.0 * (double)(1ull << k));  // subnormal result
+    m += guard & (uint64_t)((sticky != 0) | (m & 1));
+    if (m >> 53) {
+        m >>= 1;
+        e += 1;
+    }
+    return from((X & SIGN) | ((uint64_t)e << 52) | (m & MANT));
+}
+
+// RN(x * 2^-k) for 0 < k < 64: exact exponent decrement while the result stays
+// normal (x / 4.0 and x * 0.25 are the same correctly rounded value)
+SF_HD double scale_down(double x, int k) {
+    uint64_t X = bits(x);
+    uint64_t ex = (X >> 52) & 0x7FF;
+    if (ex <= (uint64_t)k || ex == 0x7FF) return nmul(x, from((uint64_t)(1023 - k) << 52));
+    return from(X - ((uint64_t)k << 52));
+}
+
+// ---------------------------------------------------------------- branch-free fast paths
+//
+// add_fast / div3p2_fast / scale_down_fast compute the result with integer
+// operations only and never issue an FP64 instruction, including for a zero
+// operand (x + 0 = x) and far-apart exponents.  They OR `special` with true
+// when the result may be wrong: a subnormal, infinite or NaN operand, a sum of
+// two zeros, a subnormal or overflowing result.  The caller then recomputes
+// that element with the native operations in a warp-uniform branch (rare), so
+// the FP64 unit sees no predicated-off instruction in the common path.
+
+SF_HD uint32_t hi32(uint64_t x) { return (uint32_t)(x >> 32); }
+
+SF_HD double add_fast(double a, double b, bool &special) {
+    uint64_t A = bits(a), B = bits(b);
+    uint64_t absA = A & ~SIGN, absB = B & ~SIGN;
+    bool swp = absA < absB;
+    uint64_t X = swp ? B : A, Y = swp ? A : B;  // |X| >= |Y|
+    uint32_t ex = (hi32(X) >> 20) & 0x7FF, ey = (hi32(Y) >> 20) & 0x7FF;
+    bool yzero = (Y & ~SIGN) == 0;
+    // Y may be a zero (X + 0 = X); any other subnormal, inf or nan is special
+    special |= (ex - 1 >= 0x7FE) | ((ey - 1 >= 0x7FE) & !yzero);
+    uint32_t d = ex - ey;
+    bool far = yzero | (d > 63);  // RN(x + y) = x
+    uint32_t dd = far ? 0 : d;
+    uint64_t mx = ((X & MANT) | HID) << 8, my = ((Y & MANT) | HID) << 8;
+    uint64_t lost = dd ? (my << (64 - dd)) : 0;
+    my = (my >> dd) | (uint64_t)(lost != 0);
+    bool subtr = ((X ^ Y) & SIGN) != 0;
+    uint64_t s = subtr ? mx - my : mx + my;
+    int lz = clz64(s);
+    bool carry = lz == 2;
+    int sh = carry ? 0 : lz - 3;
+    uint64_t sn = carry ? ((s >> 1) | (s & 1)) : (s << (sh & 63));
+    int e = (int)ex + (carry ? 1 : -sh);
+    uint64_t m = sn >> 8;
+    uint32_t rem = (uint32_t)sn & 0xFF;
+    m += (uint64_t)((rem > 0x80) | ((rem == 0x80) & (uint32_t)(m & 1)));
+    uint32_t c = (uint32_t)(m >> 53);
+    m >>= c;
+    e += (int)c;
+    bool zero = s == 0;  // exact cancellation: +0 in round-to-nearest
+    special |= !far & !zero & ((e <= 0) | (e >= 0x7FF));
+    special |= yzero & ((X & ~SIGN) == 0);  // both zero: sign rules
+    uint64_t r = (X & SIGN) | ((uint64_t)(uint32_t)e << 52) | (m & MANT);
+    r = zero ? 0 : r;
+    return from(far ? X : r);
+}
+
+SF_HD double sub_fast(double a, double b, bool &special) { return add_fast(a, from(bits(b) ^ SIGN), special); }
+
+SF_HD double div3p2_fast(double x, int k, bool &special) {
+    uint64_t X = bits(x);
+    uint32_t ex = (hi32(X) >> 20) & 0x7FF;
+    bool zero = (X & ~SIGN) == 0;
+    uint64_t n = ((X & MANT) | HID) << 11;
+    uint64_t q = mulhi(n, 0xAAAAAAAAAAAAAAABull) >> 1;
+    uint64_t r = n - 3 * q;
+    bool top = (q >> 62) != 0;
+    int sh = top ? 10 : 9;
+    uint64_t m = q >> sh;
+    uint64_t guard = (q >> (sh - 1)) & 1;
+    uint64_t sticky = (q & ((1ull << (sh - 1)) - 1)) | r;
+    int e = (int)ex - (top ? 1 : 2) - k;
+    special |= !zero & ((ex - 1 >= 0x7FE) | (e <= 0));
+    m += guard & (uint64_t)((sticky != 0) | (m & 1));
+    uint32_t c = (uint32_t)(m >> 53);
+    m >>= c;
+    e += (int)c;
+    uint64_t res = (X & SIGN) | ((uint64_t)(uint32_t)e << 52) | (m & MANT);
+    return from(zero ? X : res);
+}
+
+SF_HD double scale_down_fast(double x, int k, bool &special) {
+    uint64_t X = bits(x);
+    uint32_t ex = (hi32(X) >> 20) & 0x7FF;
+    bool zero = (X & ~SIGN) == 0;
+    special |= !zero & ((ex <= (uint32_t)k) | (ex == 0x7FF));
+    return from(zero ? X : X - ((uint64_t)k << 52));
+}
+
+// Max(|t|, m) on bit patterns: for non-negative doubles the IEEE order is the
+// unsigned integer order.  A NaN t leaves m unchanged, as (t > m ? t : m) does.
+SF_HD uint64_t absmax_bits(double t, uint64_t m) {
+    uint64_t b = bits(t) & ~SIGN;
+    return (b <= EXPINF && b > m) ? b : m;
+}
+
+}  // namespace sf

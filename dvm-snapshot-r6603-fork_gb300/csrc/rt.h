@@ -1,0 +1,299 @@
+// Internal declarations of libdvmh_gb: the GB300 loop-execution runtime.
+//
+// One process, one GPU.  Device 0 is the host, device 1 the GPU (the
+// reference's numbering: rts/dvmh/dvmh_rts.cpp:487-520).  Distributed arrays
+// live in pinned host memory and in one device buffer each; actuality is kept
+// per array as two flags (host copy current / device copy current) because on
+// one device the reference's rectangle sets (rts/dvmh/dvmh_pieces.cpp) only
+// ever describe the whole local part.  Loops run through the CUDA handler the
+// program registered, on the runtime's stream, in one of three modes:
+//   plain    - each loop launched when performed, reduction results copied to
+//              the host variable and the stream synchronised at loop end (the
+//              reference's per-loop model, rts/dvmh/loop.cpp:2235-2240);
+//   async    - each loop launched when performed, reduction results stay on
+//              the device until get_actual, no per-loop synchronisation;
+//   batched  - loops are queued; at the next synchronisation point the queue
+//              (fused where a fusion rule applies) is captured once as a CUDA
+//              graph, cached by its signature and replayed afterwards.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdarg>
+#include <cstddef>
+#include <cstdint>
+#include <cstdio>
+#include <map>
+#include <string>
+#include <vector>
+
+#include "../../include/dvmhlib2.h"
+#include "../../include/dvmh_gb.h"
+
+namespace dvmhgb {
+
+constexpr int MAXR = 7;  // maximum array/loop rank (the reference's MAX_ARRAY_RANK)
+
+// ---------------------------------------------------------------- errors
+
+[[noreturn]] void fatal(const char *kind, const char *file, int line, const char *fmt, ...);
+#define GB_CHECK(cond, ...)                                                         \
+    do {                                                                            \
+        if (!(cond)) ::dvmhgb::fatal("error", __FILE__, __LINE__, __VA_ARGS__);     \
+    } while (0)
+#define GB_INTERNAL(cond, ...)                                                      \
+    do {                                                                            \
+        if (!(cond)) ::dvmhgb::fatal("internal", __FILE__, __LINE__, __VA_ARGS__);  \
+    } while (0)
+#define GB_CUDA(call)                                                               \
+    do {                                                                            \
+        cudaError_t e_ = (call);                                                    \
+        if (e_ != cudaSuccess)                                                      \
+            ::dvmhgb::fatal("cuda", __FILE__, __LINE__, "%s: %s", #call, cudaGetErrorString(e_)); \
+    } while (0)
+
+void logmsg(int level, const char *fmt, ...);
+enum { LOG_ERROR = 1, LOG_WARN = 2, LOG_INFO = 3, LOG_DEBUG = 4, LOG_TRACE = 5 };
+
+// ---------------------------------------------------------------- settings
+
+enum Mode { MODE_PLAIN = 0, MODE_ASYNC = 1, MODE_BATCHED = 2 };
+
+struct Settings {
+    int mode = MODE_BATCHED;
+    int logLevel = LOG_ERROR;
+    bool syncEachLoop = false;  // DVMH_SYNC_CUDA: synchronise after every loop
+    int tuneMode = 0;           // 0 off, 1 exhaustive, 2 model-guided (DVMH_OPT_PARAMS)
+    int graphCacheMax = 64;
+    bool fuse = true;
+};
+extern Settings settings;
+
+// ---------------------------------------------------------------- objects
+
+enum ObjKind : uint32_t {
+    K_ARRAY = 0x41525259u,
+    K_TEMPLATE = 0x54454d50u,
+    K_VAR = 0x56415220u,
+    K_REGION = 0x5245474eu,
+    K_LOOP = 0x4c4f4f50u,
+    K_SPEC = 0x53504543u,
+};
+
+struct Obj {
+    uint32_t kind;
+    explicit Obj(uint32_t k) : kind(k) {}
+    virtual ~Obj() { kind = 0; }
+};
+
+struct Array : Obj {
+    Array() : Obj(K_ARRAY) {}
+    int rank = 0;
+    int dtype = rt_UNKNOWN;  // rt_* or rt_UNKNOWN for sized types
+    size_t esize = 0;
+    long ext[MAXR] = {};
+    long shLo[MAXR] = {}, shHi[MAXR] = {};
+    bool distributed = false;
+    // host copy: dense, pinned
+    long hstride[MAXR] = {};
+    size_t helems = 0;
+    char *host = nullptr;
+    // device copy: innermost axis padded to 32 elements (256 B rows for FP64)
+    long dstride[MAXR] = {};
+    size_t delems = 0;
+    char *dev = nullptr;
+    char *devAlt = nullptr;  // second buffer for double-buffered (fused) loops
+    bool hostActual = true, devActual = false;
+    DvmType *desc = nullptr;
+    std::string name;
+    size_t hostBytes() const { return helems * esize; }
+    size_t devBytes() const { return delems * esize; }
+};
+
+struct Templ : Obj {
+    Templ() : Obj(K_TEMPLATE) {}
+    int rank = 0;
+    long ext[MAXR] = {};
+};
+
+// A regular (non-distributed) variable known to the runtime: scalars and
+// blobs registered in regions, reduction variables.
+struct Var : Obj {
+    Var() : Obj(K_VAR) {}
+    const char *addr = nullptr;
+    size_t size = 0;
+    char *dev = nullptr;
+    bool hostActual = true, devActual = false;
+    std::string name;
+};
+
+struct Region;
+struct Loop;
+
+struct HandlerRef {
+    DvmHandlerFunc func = nullptr;
+    int nparams = 0;
+    void *params[64];
+};
+
+struct Reduction {
+    int op = 0;        // rf_*
+    int vtype = 0;     // rt_*
+    size_t esize = 0;  // element size of the value type
+    long count = 1;    // array length of the reduction variable
+    char *addr = nullptr;
+    char *locAddr = nullptr;
+    long locSize = 0;
+    std::vector<char> init, initLoc;  // host snapshot (reference: DvmhReduction ctor, loop.cpp:17-35)
+    Var *var = nullptr;               // registered variable holding addr (device-resident result)
+    size_t varOff = 0;
+    Var *locVar = nullptr;
+    size_t locVarOff = 0;
+};
+
+struct Across {
+    Array *arr;
+    bool isOut;
+    long lo[MAXR], hi[MAXR];
+};
+
+struct Loop : Obj {
+    Loop() : Obj(K_LOOP) {}
+    Region *region = nullptr;
+    int rank = 0;
+    long lo[MAXR] = {}, hi[MAXR] = {}, step[MAXR] = {};
+    bool empty = false;
+    Array *mapArr = nullptr;
+    int arrAxisToLoop[MAXR] = {};  // array axis -> loop axis (1-based), 0 = none
+    std::vector<Reduction> reds;
+    std::vector<Across> across;
+    long depMask = 0;
+    int cudaBlock[3] = {0, 0, 0};
+    bool userBlock = false;
+    long stage = 0;
+    HandlerRef host, cuda;
+    bool hasHost = false, hasCuda = false;
+    std::string file;
+    long line = 0;
+};
+
+struct RegionVar {
+    Var *var;
+    long intent;
+};
+struct RegionArr {
+    Array *arr;
+    long intent;
+};
+
+struct Region : Obj {
+    Region() : Obj(K_REGION) {}
+    long flags = 0;
+    long targets = 0;
+    std::vector<RegionArr> arrays;
+    std::vector<RegionVar> vars;
+    bool started = false;
+};
+
+// Device-side storage of one registered reduction during a handler call.
+struct CudaRed {
+    int index = 0;  // 1-based
+    void **arrPtrSlot = nullptr, **locPtrSlot = nullptr;
+    char *items = nullptr, *locItems = nullptr;
+    long count = 0;
+    bool finished = false;
+};
+
+// The loop reference handed to a handler (the reference's DvmhLoopCuda, loop.h:420-473).
+struct SpecLoop : Obj {
+    SpecLoop() : Obj(K_SPEC) {}
+    Loop *loop = nullptr;
+    int device = 1;
+    cudaStream_t stream = nullptr;
+    int block[3] = {0, 0, 0};
+    int variant = -1;  // tuner's kernel variant, -1 = handler default
+    std::vector<CudaRed> reds;
+    std::vector<void *> scratch;  // device allocations owned by this execution
+    std::vector<void *> hostScratch;  // pinned host allocations owned by this execution
+    std::vector<Array *> swaps;   // arrays whose device buffers swap at loop end
+};
+
+// ---------------------------------------------------------------- device layer (rt_device.cu)
+
+struct Device {
+    int ordinal = -1;
+    cudaDeviceProp prop{};
+    cudaStream_t stream = nullptr;
+    int smCount = 0;
+    bool ready = false;
+    int *statusHost = nullptr;  // mapped pinned word: 0 = fine, else the error a kernel reported
+    int *statusDev = nullptr;
+};
+extern Device gpu;
+
+void deviceInit();
+void deviceFinish();
+void *devAlloc(size_t bytes);        // caching pool, 256-byte aligned
+void devFree(void *p);               // back to the pool
+void *hostAlloc(size_t bytes);       // pinned
+void hostFree(void *p);
+void copyH2D(Array *a);              // whole array, on the stream
+void copyD2H(Array *a);              // whole array, on the stream + sync
+void copyBoxH2D(Array *a, const long lo[], const long hi[]);
+void copyBoxD2H(Array *a, const long lo[], const long hi[]);
+void streamSync();
+
+// reduction fold (canonical tree) writing the final value to dst / dstLoc
+void launchRedFold(int op, int vtype, long count, long elemCount, const void *items, const void *locItems,
+                   long locSize, void *dst, void *dstLoc, cudaStream_t s, std::vector<void *> &scratch);
+void fillIdentity(int op, int vtype, void *items, long n, cudaStream_t s);
+// one deferred reduction fold (batched handlers): FP64, one element
+struct FoldJob {
+    int op;
+    long count;
+    const void *items, *locItems;
+    long locSize;
+    void *dst, *dstLoc;
+};
+bool foldBatchable(int op, int vtype, long count, long elemCount);
+void launchRedFoldBatch(const std::vector<FoldJob> &jobs, cudaStream_t s, std::vector<void *> &devScratch,
+                        std::vector<void *> &hostScratch);
+void identityValue(int op, int vtype, void *out);
+size_t typeSize(int vtype);
+
+// ---------------------------------------------------------------- runtime state (rt_core.cpp)
+
+struct State {
+    bool inited = false;
+    Region *curRegion = nullptr;
+    Loop *curLoop = nullptr;
+    std::map<const char *, Var *> vars;  // by start address
+    std::string file;
+    long line = 0;
+};
+extern State st;
+
+Array *arrayOf(const DvmType desc[], const char *what);
+Var *varAt(const void *addr, size_t *off);           // registered variable containing addr, or null
+Var *varGet(const void *addr, size_t size);          // existing or new variable for [addr, addr+size)
+void ensureDevBuffer(Array *a);
+void ensureDevActual(Array *a);
+void ensureHostActual(Array *a);
+void ensureVarDev(Var *v);
+void varH2D(Var *v);
+void varD2H(Var *v);
+void fillDesc(Array *a);
+
+// ---------------------------------------------------------------- loops / batching (rt_loop.cpp)
+
+void queueFlush();  // run or replay everything queued (batched mode)
+bool queueBusy();
+void loopsAtExit();
+
+// ---------------------------------------------------------------- tuner (rt_tuner.cpp)
+
+struct TuneKey;
+void tunerPick(Loop *l, int block[3]);
+void tunerRecord(Loop *l, const int block[3], double seconds);
+
+}  // namespace dvmhgb

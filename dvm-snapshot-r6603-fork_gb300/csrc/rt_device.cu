@@ -1,0 +1,594 @@
+// libdvmh_gb device layer: the GPU, its stream, a caching allocator, pinned
+// host memory, host<->device copies of arrays and variables, and the
+// reduction fold.
+//
+// The fold replaces the reference's two-stage finish (cuda_reduction.cu:168-312:
+// grid-stride kernel, per-warp partials copied to the host and folded there,
+// one more copy for the MINLOC record).  Here the items a loop kernel wrote are
+// folded on the device by a fixed pairwise tree over item indices (padded with
+// the identity to a power of two), the initial value of the reduction
+// variable is combined last as the reference does it
+// (initGlobalValues + postValues + addInitialValues, rts/dvmh/dvmh2.cpp:3848-3851,
+// 3950-3953: result = (identity (+) loop value) (+) initial), and the result is
+// written to the variable's device copy.  MINLOC/MAXLOC keep the strict
+// comparison of RED_MIN/RED_MAX (rts/dvmh/loop.cpp:117-118): of equal values the
+// lower item index -- the earlier one in loop order -- wins.
+#include <algorithm>
+#include <cstring>
+#include <map>
+
+#include "rt.h"
+
+namespace dvmhgb {
+
+Device gpu;
+
+// ---------------------------------------------------------------- allocator
+
+namespace {
+std::multimap<size_t, void *> freeDev;  // size class -> block
+std::map<void *, size_t> usedDev;
+size_t sizeClass(size_t b) {
+    if (b <= 4096) {
+        size_t c = 256;
+        while (c < b) c <<= 1;
+        return c;
+    }
+    return (b + 65535) / 65536 * 65536;
+}
+}  // namespace
+
+void *devAlloc(size_t bytes) {
+    size_t c = sizeClass(bytes);
+    auto it = freeDev.find(c);
+    void *p;
+    if (it != freeDev.end()) {
+        p = it->second;
+        freeDev.erase(it);
+    } else {
+        cudaError_t e = cudaMalloc(&p, c);
+        if (e != cudaSuccess) {
+            // give cached blocks back and retry once
+            cudaGetLastError();
+            for (auto &f : freeDev) cudaFree(f.second);
+            freeDev.clear();
+            GB_CUDA(cudaMalloc(&p, c));
+        }
+    }
+    usedDev[p] = c;
+    return p;
+}
+
+void devFree(void *p) {
+    if (!p) return;
+    auto it = usedDev.find(p);
+    GB_INTERNAL(it != usedDev.end(), "freeing unknown device block %p", p);
+    freeDev.emplace(it->second, p);
+    usedDev.erase(it);
+}
+
+void *hostAlloc(size_t bytes) {
+    void *p = nullptr;
+    GB_CUDA(cudaHostAlloc(&p, bytes, cudaHostAllocPortable));
+    return p;
+}
+
+void hostFree(void *p) {
+    if (p) cudaFreeHost(p);
+}
+
+// ---------------------------------------------------------------- device
+
+void deviceInit() {
+    int n = 0;
+    cudaError_t e = cudaGetDeviceCount(&n);
+    GB_CHECK(e == cudaSuccess && n > 0, "no CUDA device: this runtime executes parallel loops on the GPU only (%s)",
+             cudaGetErrorString(e));
+    int dev = 0;
+    if (const char *d = getenv("DVMH_GB_DEVICE")) dev = atoi(d);
+    GB_CHECK(dev >= 0 && dev < n, "DVMH_GB_DEVICE=%d out of range", dev);
+    GB_CUDA(cudaSetDevice(dev));
+    GB_CUDA(cudaGetDeviceProperties(&gpu.prop, dev));
+    GB_CHECK(gpu.prop.major >= 10, "device %s (sm_%d%d) is not a Blackwell GPU; this library is built for sm_103a",
+             gpu.prop.name, gpu.prop.major, gpu.prop.minor);
+    gpu.ordinal = dev;
+    gpu.smCount = gpu.prop.multiProcessorCount;
+    GB_CUDA(cudaStreamCreateWithFlags(&gpu.stream, cudaStreamNonBlocking));
+    // status word written by kernels whose bounded waits ran out; read at every sync
+    GB_CUDA(cudaHostAlloc((void **)&gpu.statusHost, sizeof(int), cudaHostAllocMapped | cudaHostAllocPortable));
+    *gpu.statusHost = 0;
+    GB_CUDA(cudaHostGetDevicePointer((void **)&gpu.statusDev, (void *)gpu.statusHost, 0));
+    gpu.ready = true;
+}
+
+void deviceFinish() {
+    if (!gpu.ready) return;
+    cudaStreamSynchronize(gpu.stream);
+}
+
+void streamSync() {
+    GB_CUDA(cudaStreamSynchronize(gpu.stream));
+    int code = *(volatile int *)gpu.statusHost;
+    GB_CHECK(code == 0, "a kernel gave up waiting for a dependency (status 0x%08x): results of the last loops are invalid",
+             (unsigned)code);
+}
+
+extern dvmhgb_stats_t stats;
+
+// ---------------------------------------------------------------- copies
+
+// Dense host layout <-> device layout whose innermost rows are padded: one 2-D
+// copy (rows = product of the outer extents).
+void copyH2D(Array *a) {
+    long rows = (long)(a->helems / a->ext[a->rank - 1]);
+    size_t w = a->ext[a->rank - 1] * a->esize;
+    size_t dp = (a->rank == 1 ? a->ext[0] : a->dstride[a->rank - 2]) * a->esize;
+    GB_CUDA(cudaMemcpy2DAsync(a->dev, dp, a->host, w, w, rows, cudaMemcpyHostToDevice, gpu.stream));
+    stats.h2d_bytes += (long)(w * rows);
+}
+
+void copyD2H(Array *a) {
+    long rows = (long)(a->helems / a->ext[a->rank - 1]);
+    size_t w = a->ext[a->rank - 1] * a->esize;
+    size_t dp = (a->rank == 1 ? a->ext[0] : a->dstride[a->rank - 2]) * a->esize;
+    GB_CUDA(cudaMemcpy2DAsync(a->host, w, a->dev, dp, w, rows, cudaMemcpyDeviceToHost, gpu.stream));
+    stats.d2h_bytes += (long)(w * rows);
+    streamSync();
+}
+
+// Box copies: the innermost axis is the row; rows are enumerated over the
+// outer axes (one 2-D copy per index of the second-innermost axis group).
+static void copyBox(Array *a, const long lo[], const long hi[], bool toDev) {
+    int r = a->rank;
+    size_t w = (hi[r - 1] - lo[r - 1] + 1) * a->esize;
+    if (r == 1) {
+        char *h = a->host + lo[0] * a->esize, *d = a->dev + lo[0] * a->esize;
+        GB_CUDA(cudaMemcpyAsync(toDev ? (void *)d : (void *)h, toDev ? (void *)h : (void *)d, w,
+                                toDev ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToHost, gpu.stream));
+    } else {
+        long idx[MAXR];
+        for (int i = 0; i < r - 1; i++) idx[i] = lo[i];
+        long nrows = hi[r - 2] - lo[r - 2] + 1;
+        while (true) {
+            long ho = 0, dof = 0;
+            for (int i = 0; i < r - 2; i++) {
+                ho += idx[i] * a->hstride[i];
+                dof += idx[i] * a->dstride[i];
+            }
+            ho += lo[r - 2] * a->hstride[r - 2] + lo[r - 1];
+            dof += lo[r - 2] * a->dstride[r - 2] + lo[r - 1];
+            size_t hp = a->hstride[r - 2] * a->esize, dp = a->dstride[r - 2] * a->esize;
+            if (toDev)
+                GB_CUDA(cudaMemcpy2DAsync(a->dev + dof * a->esize, dp, a->host + ho * a->esize, hp, w, nrows,
+                                          cudaMemcpyHostToDevice, gpu.stream));
+            else
+                GB_CUDA(cudaMemcpy2DAsync(a->host + ho * a->esize, hp, a->dev + dof * a->esize, dp, w, nrows,
+                                          cudaMemcpyDeviceToHost, gpu.stream));
+            int ax = r - 3;
+            while (ax >= 0 && ++idx[ax] > hi[ax]) {
+                idx[ax] = lo[ax];
+                ax--;
+            }
+            if (ax < 0) break;
+        }
+    }
+    long cells = 1;
+    for (int i = 0; i < r; i++) cells *= hi[i] - lo[i] + 1;
+    if (toDev) stats.h2d_bytes += cells * (long)a->esize;
+    else stats.d2h_bytes += cells * (long)a->esize;
+}
+
+void copyBoxH2D(Array *a, const long lo[], const long hi[]) { copyBox(a, lo, hi, true); }
+void copyBoxD2H(Array *a, const long lo[], const long hi[]) {
+    copyBox(a, lo, hi, false);
+    streamSync();
+}
+
+// Variables: through a pinned staging copy so the transfer is asynchronous
+// and capturable; the staging buffer is reused only after the copy ran.
+namespace {
+struct Staging {
+    char *buf = nullptr;
+    size_t size = 0;
+    cudaEvent_t done = nullptr;
+};
+std::map<const Var *, Staging> staging;
+Staging &stageFor(const Var *v) {
+    Staging &s = staging[v];
+    if (s.size < v->size) {
+        if (s.buf) {
+            if (s.done) cudaEventSynchronize(s.done);
+            hostFree(s.buf);
+        }
+        s.buf = (char *)hostAlloc(std::max<size_t>(v->size, 16));
+        s.size = v->size;
+    }
+    if (!s.done) GB_CUDA(cudaEventCreateWithFlags(&s.done, cudaEventDisableTiming));
+    return s;
+}
+}  // namespace
+
+void varH2D(Var *v) {
+    ensureVarDev(v);
+    queueFlush();
+    Staging &s = stageFor(v);
+    GB_CUDA(cudaEventSynchronize(s.done));
+    memcpy(s.buf, v->addr, v->size);
+    GB_CUDA(cudaMemcpyAsync(v->dev, s.buf, v->size, cudaMemcpyHostToDevice, gpu.stream));
+    GB_CUDA(cudaEventRecord(s.done, gpu.stream));
+    stats.h2d_bytes += (long)v->size;
+}
+
+void varD2H(Var *v) {
+    GB_INTERNAL(v->dev, "variable without a device copy");
+    queueFlush();
+    Staging &s = stageFor(v);
+    GB_CUDA(cudaEventSynchronize(s.done));
+    GB_CUDA(cudaMemcpyAsync(s.buf, v->dev, v->size, cudaMemcpyDeviceToHost, gpu.stream));
+    streamSync();
+    memcpy((void *)v->addr, s.buf, v->size);
+    stats.d2h_bytes += (long)v->size;
+}
+
+// ---------------------------------------------------------------- reduction identities
+
+template <typename T>
+struct Lim;
+#define LIM(T, LO, HI)                                             \
+    template <>                                                    \
+    struct Lim<T> {                                                \
+        __host__ __device__ static T lo() { return LO; }           \
+        __host__ __device__ static T hi() { return HI; }           \
+    };
+LIM(char, -128, 127)
+LIM(signed char, -128, 127)
+LIM(unsigned char, 0, 255)
+LIM(short, -32768, 32767)
+LIM(unsigned short, 0, 65535)
+LIM(int, (-2147483647 - 1), 2147483647)
+LIM(unsigned, 0u, 4294967295u)
+LIM(long, (-9223372036854775807L - 1), 9223372036854775807L)
+LIM(unsigned long, 0ul, 18446744073709551615ul)
+LIM(long long, (-9223372036854775807LL - 1), 9223372036854775807LL)
+LIM(unsigned long long, 0ull, 18446744073709551615ull)
+LIM(float, -__builtin_huge_valf(), __builtin_huge_valf())
+LIM(double, -__builtin_huge_val(), __builtin_huge_val())
+#undef LIM
+
+// identity of each operation; -0.0 is the exact additive identity of IEEE sums
+template <typename T>
+__host__ __device__ T identityOf(int op) {
+    switch (op) {
+        case rf_SUM: return (T)0 * (T)-1 == (T)0 ? (T)-0.0 : (T)0;
+        case rf_PROD: return (T)1;
+        case rf_MAX: case rf_MAXLOC: return Lim<T>::lo();
+        case rf_MIN: case rf_MINLOC: return Lim<T>::hi();
+        case rf_AND: return (T)~(T)0;
+        case rf_OR: case rf_XOR: case rf_NE: return (T)0;
+        case rf_EQU: case rf_EQ: return (T)1;
+        default: return (T)0;
+    }
+}
+template <>
+__host__ __device__ float identityOf<float>(int op) {
+    switch (op) {
+        case rf_SUM: return -0.0f;
+        case rf_PROD: return 1.0f;
+        case rf_MAX: case rf_MAXLOC: return Lim<float>::lo();
+        case rf_MIN: case rf_MINLOC: return Lim<float>::hi();
+        default: return 0.0f;
+    }
+}
+template <>
+__host__ __device__ double identityOf<double>(int op) {
+    switch (op) {
+        case rf_SUM: return -0.0;
+        case rf_PROD: return 1.0;
+        case rf_MAX: case rf_MAXLOC: return Lim<double>::lo();
+        case rf_MIN: case rf_MINLOC: return Lim<double>::hi();
+        default: return 0.0;
+    }
+}
+
+// dest (+)= src following loop.cpp:116-238; returns true when MIN/MAX replaced dest
+template <typename T>
+__host__ __device__ __forceinline__ bool combine(int op, T &d, T s) {
+    switch (op) {
+        case rf_SUM: d = d + s; return false;
+        case rf_PROD: d = d * s; return false;
+        case rf_MAX: case rf_MAXLOC: if (d < s) { d = s; return true; } return false;
+        case rf_MIN: case rf_MINLOC: if (d > s) { d = s; return true; } return false;
+        default: return false;
+    }
+}
+template <typename T>
+__host__ __device__ __forceinline__ bool combineInt(int op, T &d, T s) {
+    switch (op) {
+        case rf_AND: d &= s; return false;
+        case rf_OR: d |= s; return false;
+        case rf_XOR: d ^= s; return false;
+        case rf_EQU: case rf_EQ: d = (d == s); return false;
+        case rf_NE: d = (d != s); return false;
+        default: return combine<T>(op, d, s);
+    }
+}
+template <typename T, bool INT>
+struct Comb {
+    __host__ __device__ static bool f(int op, T &d, T s) { return combine<T>(op, d, s); }
+};
+template <typename T>
+struct Comb<T, true> {
+    __host__ __device__ static bool f(int op, T &d, T s) { return combineInt<T>(op, d, s); }
+};
+
+template <typename T>
+__global__ void kFill(T *p, long n, T v) {
+    for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) p[i] = v;
+}
+
+// ---------------------------------------------------------------- fold kernels
+
+constexpr int FOLD_THREADS = 512;
+constexpr int FOLD_SPAN = 2 * FOLD_THREADS;  // items per block per pass (a pairwise subtree)
+
+// One pass: block b folds items [b*SPAN, (b+1)*SPAN) of every element e by the
+// pairwise tree (item i pairs with i^1, then i^2, ...), padding with the
+// identity, and writes out[b] (and the winning loc index for LOC ops).
+// Items are laid out [item][elem]; locs [item][locSize bytes].
+// `final` > 0: a single block, whose result is combined with the initial value
+// read from dst and written to dst (+ loc bytes to dstLoc).
+template <typename T, bool INT>
+__global__ void __launch_bounds__(FOLD_THREADS) kFold(int op, long count, long elemCount, const T *items,
+                                                      const long *itemIdx, T *out, long *outIdx, int final,
+                                                      T *dst, const char *locItems, long locSize, char *dstLoc) {
+    __shared__ T sv[FOLD_SPAN];
+    __shared__ long si[FOLD_SPAN];
+    const bool loc = (op == rf_MINLOC || op == rf_MAXLOC);
+    const T ident = identityOf<T>(op);
+    for (long e = 0; e < elemCount; e++) {
+        for (int h = 0; h < 2; h++) {
+            long i = blockIdx.x * (long)FOLD_SPAN + h * FOLD_THREADS + threadIdx.x;
+            bool in = i < count;
+            sv[h * FOLD_THREADS + threadIdx.x] = in ? items[i * elemCount + e] : ident;
+            si[h * FOLD_THREADS + threadIdx.x] = in ? (itemIdx ? itemIdx[i * elemCount + e] : i) : -1;
+        }
+        __syncthreads();
+        for (int w = 1; w < FOLD_SPAN; w <<= 1) {
+            // node pairs (a, a + w) with a a multiple of 2w: pairwise by index
+            int pairs = FOLD_SPAN / (2 * w);
+            for (int p = threadIdx.x; p < pairs; p += FOLD_THREADS) {
+                int a = p * 2 * w, b = a + w;
+                T d = sv[a];
+                if (loc) {
+                    // of equal values the lower index wins; identity slots (index -1) never win
+                    T s = sv[b];
+                    long ia = si[a], ib = si[b];
+                    bool take = (ia < 0 && ib >= 0) || (ib >= 0 && Comb<T, INT>::f(op, d, s));
+                    if (take) {
+                        sv[a] = s;
+                        si[a] = ib;
+                    }
+                } else {
+                    Comb<T, INT>::f(op, d, sv[b]);
+                    sv[a] = d;
+                }
+            }
+            __syncthreads();
+        }
+        if (threadIdx.x == 0) {
+            if (!final) {
+                out[blockIdx.x * elemCount + e] = sv[0];
+                if (outIdx) outIdx[blockIdx.x * elemCount + e] = si[0];
+            } else {
+                // result = (global start (+) loop value) (+) initial value, where the
+                // global start is what DvmhReduction::initValues (loop.cpp:37-100) puts
+                // there: +0 for SUM/XOR/NE, 1 for PROD/EQU/EQ, the initial value otherwise
+                T init = dst[e];
+                T r;
+                switch (op) {
+                    case rf_SUM: case rf_XOR: case rf_NE: r = (T)0; break;
+                    case rf_PROD: case rf_EQU: case rf_EQ: r = (T)1; break;
+                    default: r = init;
+                }
+                long ri = si[0];
+                bool fromLoop = false;
+                if (loc) {
+                    if (ri >= 0) fromLoop = Comb<T, INT>::f(op, r, sv[0]);
+                } else {
+                    Comb<T, INT>::f(op, r, sv[0]);
+                    Comb<T, INT>::f(op, r, init);
+                }
+                dst[e] = r;
+                if (loc && fromLoop && dstLoc && locItems)
+                    for (long b = 0; b < locSize; b++) dstLoc[e * locSize + b] = locItems[(ri * elemCount + e) * locSize + b];
+            }
+        }
+        __syncthreads();
+    }
+}
+
+template <typename T, bool INT>
+static void foldT(int op, long count, long elemCount, const void *items, const void *locItems, long locSize, void *dst,
+                  void *dstLoc, cudaStream_t s, std::vector<void *> &scratch) {
+    const T *cur = (const T *)items;
+    const long *curIdx = nullptr;
+    long n = count;
+    while (n > FOLD_SPAN) {
+        long blocks = (n + FOLD_SPAN - 1) / FOLD_SPAN;
+        T *out = (T *)devAlloc(sizeof(T) * blocks * elemCount);
+        long *outIdx = (op == rf_MINLOC || op == rf_MAXLOC) ? (long *)devAlloc(sizeof(long) * blocks * elemCount) : nullptr;
+        scratch.push_back(out);
+        if (outIdx) scratch.push_back(outIdx);
+        kFold<T, INT><<<(unsigned)blocks, FOLD_THREADS, 0, s>>>(op, n, elemCount, cur, curIdx, out, outIdx, 0, nullptr,
+                                                               nullptr, 0, nullptr);
+        dvmhgb_count_launches(1);
+        cur = out;
+        curIdx = outIdx;
+        n = blocks;
+    }
+    kFold<T, INT><<<1, FOLD_THREADS, 0, s>>>(op, n, elemCount, cur, curIdx, nullptr, nullptr, 1, (T *)dst,
+                                            (const char *)locItems, locSize, (char *)dstLoc);
+    dvmhgb_count_launches(1);
+    GB_CUDA(cudaGetLastError());
+}
+
+#define DISPATCH_TYPES(vtype, FN, ...)                                                           \
+    switch (vtype) {                                                                             \
+        case rt_CHAR: FN<signed char, true>(__VA_ARGS__); break;                                 \
+        case rt_UCHAR: FN<unsigned char, true>(__VA_ARGS__); break;                              \
+        case rt_SHORT: FN<short, true>(__VA_ARGS__); break;                                      \
+        case rt_USHORT: FN<unsigned short, true>(__VA_ARGS__); break;                            \
+        case rt_INT: case rt_LOGICAL: FN<int, true>(__VA_ARGS__); break;                         \
+        case rt_UINT: FN<unsigned, true>(__VA_ARGS__); break;                                    \
+        case rt_LONG: FN<long, true>(__VA_ARGS__); break;                                        \
+        case rt_ULONG: FN<unsigned long, true>(__VA_ARGS__); break;                              \
+        case rt_LLONG: FN<long long, true>(__VA_ARGS__); break;                                  \
+        case rt_ULLONG: FN<unsigned long long, true>(__VA_ARGS__); break;                        \
+        case rt_FLOAT: FN<float, false>(__VA_ARGS__); break;                                     \
+        case rt_DOUBLE: FN<double, false>(__VA_ARGS__); break;                                   \
+        default: GB_CHECK(false, "reduction over type %d is not supported", vtype);              \
+    }
+
+void launchRedFold(int op, int vtype, long count, long elemCount, const void *items, const void *locItems,
+                   long locSize, void *dst, void *dstLoc, cudaStream_t s, std::vector<void *> &scratch) {
+    GB_CHECK(count > 0, "empty reduction buffer");
+    bool isFloat = vtype == rt_FLOAT || vtype == rt_DOUBLE;
+    GB_CHECK(!isFloat || (op >= rf_SUM && op <= rf_MIN) || op == rf_MINLOC || op == rf_MAXLOC,
+             "reduction %d is not defined for floating types", op);
+    DISPATCH_TYPES(vtype, foldT, op, count, elemCount, items, locItems, locSize, dst, dstLoc, s, scratch);
+}
+
+// ---------------------------------------------------------------- segmented fold (batches)
+
+// One CTA per reduction: blocks of FOLD_SPAN items are folded by the pairwise
+// tree (as kFold does), block results are kept in shared memory and folded by
+// the pairwise tree again -- the same tree as the multi-pass fold, so the
+// result is identical -- then combined with the initial value.
+__global__ void __launch_bounds__(FOLD_THREADS) kFoldSeg(const FoldJob *jobs) {
+    __shared__ double sv[FOLD_SPAN];
+    __shared__ long si[FOLD_SPAN];
+    __shared__ double bv[FOLD_SPAN];
+    __shared__ long bi[FOLD_SPAN];
+    const FoldJob &J = jobs[blockIdx.x];
+    const int op = J.op;
+    const bool loc = (op == rf_MINLOC || op == rf_MAXLOC);
+    const double ident = identityOf<double>(op);
+    const double *items = (const double *)J.items;
+    const long nblk = (J.count + FOLD_SPAN - 1) / FOLD_SPAN;
+    for (long blk = 0; blk < nblk; blk++) {
+        for (int h = 0; h < 2; h++) {
+            long i = blk * FOLD_SPAN + h * FOLD_THREADS + threadIdx.x;
+            bool in = i < J.count;
+            sv[h * FOLD_THREADS + threadIdx.x] = in ? items[i] : ident;
+            si[h * FOLD_THREADS + threadIdx.x] = in ? i : -1;
+        }
+        __syncthreads();
+        for (int w = 1; w < FOLD_SPAN; w <<= 1) {
+            int pairs = FOLD_SPAN / (2 * w);
+            for (int p = threadIdx.x; p < pairs; p += FOLD_THREADS) {
+                int a = p * 2 * w, b = a + w;
+                double d = sv[a];
+                if (loc) {
+                    bool take = (si[a] < 0 && si[b] >= 0) || (si[b] >= 0 && combine<double>(op, d, sv[b]));
+                    if (take) {
+                        sv[a] = sv[b];
+                        si[a] = si[b];
+                    }
+                } else {
+                    combine<double>(op, d, sv[b]);
+                    sv[a] = d;
+                }
+            }
+            __syncthreads();
+        }
+        if (threadIdx.x == 0) {
+            bv[blk] = sv[0];
+            bi[blk] = si[0];
+        }
+        __syncthreads();
+    }
+    // tree over the block results (padded with the identity)
+    for (int h = 0; h < 2; h++) {
+        int q = h * FOLD_THREADS + threadIdx.x;
+        if (q >= nblk) {
+            bv[q] = ident;
+            bi[q] = -1;
+        }
+    }
+    __syncthreads();
+    for (int w = 1; w < FOLD_SPAN; w <<= 1) {
+        int pairs = FOLD_SPAN / (2 * w);
+        for (int p = threadIdx.x; p < pairs; p += FOLD_THREADS) {
+            int a = p * 2 * w, b = a + w;
+            double d = bv[a];
+            if (loc) {
+                bool take = (bi[a] < 0 && bi[b] >= 0) || (bi[b] >= 0 && combine<double>(op, d, bv[b]));
+                if (take) {
+                    bv[a] = bv[b];
+                    bi[a] = bi[b];
+                }
+            } else {
+                combine<double>(op, d, bv[b]);
+                bv[a] = d;
+            }
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        double *dst = (double *)J.dst;
+        double init = dst[0];
+        double r = (op == rf_SUM) ? 0.0 : (op == rf_PROD ? 1.0 : init);
+        long ri = bi[0];
+        bool fromLoop = false;
+        if (loc) {
+            if (ri >= 0) fromLoop = combine<double>(op, r, bv[0]);
+        } else {
+            combine<double>(op, r, bv[0]);
+            combine<double>(op, r, init);
+        }
+        dst[0] = r;
+        if (loc && fromLoop && J.dstLoc && J.locItems)
+            for (long b = 0; b < J.locSize; b++) ((char *)J.dstLoc)[b] = ((const char *)J.locItems)[ri * J.locSize + b];
+    }
+}
+
+bool foldBatchable(int op, int vtype, long count, long elemCount) {
+    return vtype == rt_DOUBLE && elemCount == 1 && count <= (long)FOLD_SPAN * FOLD_SPAN &&
+           (op == rf_SUM || op == rf_PROD || op == rf_MAX || op == rf_MIN || op == rf_MINLOC || op == rf_MAXLOC);
+}
+
+void launchRedFoldBatch(const std::vector<FoldJob> &jobs, cudaStream_t s, std::vector<void *> &devScratch,
+                        std::vector<void *> &hostScratch) {
+    if (jobs.empty()) return;
+    size_t bytes = sizeof(FoldJob) * jobs.size();
+    FoldJob *h = (FoldJob *)hostAlloc(bytes);
+    hostScratch.push_back(h);
+    memcpy(h, jobs.data(), bytes);
+    FoldJob *d = (FoldJob *)devAlloc(bytes);
+    devScratch.push_back(d);
+    GB_CUDA(cudaMemcpyAsync(d, h, bytes, cudaMemcpyHostToDevice, s));
+    kFoldSeg<<<(unsigned)jobs.size(), FOLD_THREADS, 0, s>>>(d);
+    dvmhgb_count_launches(1);
+    GB_CUDA(cudaGetLastError());
+}
+
+template <typename T, bool INT>
+static void fillT(int op, void *items, long n, cudaStream_t s) {
+    long blocks = std::min<long>((n + 255) / 256, 4 * 152);
+    kFill<T><<<(unsigned)std::max<long>(blocks, 1), 256, 0, s>>>((T *)items, n, identityOf<T>(op));
+    dvmhgb_count_launches(1);
+}
+
+void fillIdentity(int op, int vtype, void *items, long n, cudaStream_t s) {
+    DISPATCH_TYPES(vtype, fillT, op, items, n, s);
+}
+
+template <typename T, bool INT>
+static void identT(int op, void *out) {
+    T v = identityOf<T>(op);
+    memcpy(out, &v, sizeof(T));
+}
+
+void identityValue(int op, int vtype, void *out) { DISPATCH_TYPES(vtype, identT, op, out); }
+
+}  // namespace dvmhgb

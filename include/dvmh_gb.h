@@ -1,0 +1,98 @@
+/*
+ * dvmh_gb.h -- entry points of libdvmh_gb.so that have no counterpart in the
+ * reference's dvmhlib2.h: execution-mode control, loop batching/fusion rules
+ * for generated CUDA handlers, runtime statistics, and the CUDA-block tuner.
+ * Plain C, plain pointers and sizes.
+ */
+#ifndef DVMH_GB_H
+#define DVMH_GB_H
+
+#include "dvmhlib2.h"
+
+#pragma GCC visibility push(default)
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- execution mode ------------------------------------------------------
+ * 0 plain   : every loop launched when performed; reduction results written to
+ *             the host variable with a stream synchronisation at loop end (the
+ *             reference's model: DvmhLoopCuda::syncAfterHandlerExec,
+ *             rts/dvmh/loop.cpp:2235-2240).
+ * 1 async   : every loop launched when performed; reduction results stay on
+ *             the device until get_actual; no per-loop synchronisation.
+ * 2 batched : loops are queued and run at the next synchronisation point
+ *             (get_actual, barrier, exit, dvmhgb_flush) as one CUDA graph that
+ *             is cached by the queue's signature and replayed; fusion rules
+ *             apply.  Default; environment DVMH_GB_MODE=plain|async|batched.
+ * Changing the mode flushes queued work. */
+void dvmhgb_set_mode(int mode);
+int dvmhgb_get_mode(void);
+void dvmhgb_flush(void);   /* run queued loops now (no host synchronisation) */
+void dvmhgb_sync(void);    /* flush and wait for the GPU */
+
+/* ---- fusion and batching rules for generated handlers ---------------------
+ * A fusion rule says: when loop X with CUDA handler `first` is followed in the
+ * queue by loop Y with handler `second` over the same region, run
+ * fused(DvmType refs[2], <X's parameters>, <Y's parameters>) instead of the
+ * two handlers.  The fused handler must compute exactly what X then Y compute.
+ * A batch rule says: consecutive queued loops whose CUDA handler is `single`
+ * and whose arrays are pairwise disjoint may run as one call of
+ * batched(DvmType refs[], DvmType count); parameters of each loop are read
+ * with dvmhgb_loop_param.  Both apply in batched mode only. */
+void dvmhgb_register_fusion(DvmHandlerFunc first, DvmHandlerFunc second, DvmHandlerFunc fused);
+void dvmhgb_register_batch(DvmHandlerFunc single, DvmHandlerFunc batched);
+void *dvmhgb_loop_param(DvmType loopRef, DvmType index);
+/* Device base (natural base) of a second buffer with the same layout as the
+ * array; when the loop ends the array's device buffer and this one swap. */
+void *dvmhgb_loop_alt_buffer(DvmType loopRef, const DvmType dvmDesc[]);
+
+/* Device scratch owned by this loop execution (pool memory; kept with a
+ * captured graph, returned to the pool otherwise).  Contents undefined. */
+void *dvmhgb_loop_scratch(DvmType loopRef, DvmType bytes);
+/* Pinned host memory owned by this loop execution (for descriptor tables a
+ * handler copies to the device on its stream); kept with a captured graph. */
+void *dvmhgb_loop_host_scratch(DvmType loopRef, DvmType bytes);
+/* Device address of the runtime's status word.  A kernel whose bounded wait
+ * runs out writes a nonzero code there; the runtime reports it as a fatal
+ * error at the next synchronisation. */
+int *dvmhgb_status_word(void);
+
+/* Kernel variant for this loop execution (0 <= result < nvariants): the
+ * generated handler's alternatives -- here the number of FP64 operations per
+ * cell executed on the FP64 unit rather than the integer pipe.  The tuner
+ * chooses it with the CUDA block; `dflt` applies when tuning is off.
+ * Environment DVMH_GB_VARIANT forces a value. */
+int dvmhgb_loop_variant(DvmType loopRef, int nvariants, int dflt);
+
+/* Self-test of the integer-pipe FP64 operations against the FP64 unit on n
+ * random operand pairs: mismatches[0..3] = add, sub, mul, division by 6. */
+int dvmhgb_selftest_softfp64(long n, unsigned long long seed, long mismatches[4]);
+
+/* ---- statistics --------------------------------------------------------- */
+typedef struct {
+    long loops_performed;   /* dvmh_loop_perform_C calls */
+    long handler_calls;     /* CUDA handler invocations (captures count once) */
+    long fused_pairs;       /* fusion-rule applications */
+    long batched_groups;    /* batch-rule applications */
+    long graphs_captured;
+    long graph_replays;
+    long flushes;
+    long h2d_bytes, d2h_bytes;
+    long kernel_launches;   /* launches issued by this library's launchers */
+} dvmhgb_stats_t;
+void dvmhgb_get_stats(dvmhgb_stats_t *out);
+void dvmhgb_reset_stats(void);
+/* Launch counter, incremented by every launcher of this library (also the
+ * kernels inside captured graphs, once per replay). */
+void dvmhgb_count_launches(long n);
+
+/* Stream the runtime launches on (a cudaStream_t). */
+void *dvmhgb_stream(void);
+
+#ifdef __cplusplus
+}
+#endif
+#pragma GCC visibility pop
+
+#endif

@@ -1,0 +1,89 @@
+/*
+ * dvmh_gb_kernels.h -- launchers of the hand-written sm_103a loop kernels in
+ * libdvmh_gb.so.  These are what cdvmh would emit as the body of a CUDA
+ * handler (cdvmh/src/converter_main.cpp:1861-2401 for parallel loops,
+ * cdvmh/src/across.cpp for ACROSS loops): the workload programs' CUDA
+ * handlers call them after the dvmh_loop_* queries.
+ *
+ * Conventions: arrays are device natural bases (element (i,j,k) at
+ * base[i*st[0] + j*st[1] + k*st[2]], strides in elements as returned by
+ * dvmh_fill_header_C for device 1); lo/hi are the loop's inclusive bounds
+ * (step 1); ext is the array extent per axis; stream is a cudaStream_t.
+ * Reduction launchers write `items` partial values that
+ * dvmh_loop_cuda_red_finish_C folds: *_items() gives the count to prepare.
+ * `native` (0..ops per cell): how many of a cell's FP64 additions/subtractions
+ * run on the FP64 unit; the others run bit-identically on the integer pipe
+ * (GB300 issues 2 FP64 thread-ops per clock per SM against 128 integer ones).
+ * Every launcher returns 0, or -1 on invalid arguments (nothing launched).
+ */
+#ifndef DVMH_GB_KERNELS_H
+#define DVMH_GB_KERNELS_H
+
+#pragma GCC visibility push(default)
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- Jacobi 3-D (examples/Performance/jac3d_perf.c:56-73, FP64) ---- */
+/* loop 1: eps = max |B-A|, A = B over the box; MAX partials, one per CTA */
+long dvmhgb_jac3d_update_items(const long lo[3], const long hi[3]);
+int dvmhgb_jac3d_update(double *A, const double *B, const long st[3], const long lo[3], const long hi[3],
+                        double *items, int native, void *stream);
+/* loop 2: B = (A[i-1]+A[j-1]+A[k-1]+A[k+1]+A[j+1]+A[i+1]) / 6 over the box */
+int dvmhgb_jac3d_stencil(const double *A, double *B, const long st[3], const long ext[3], const long lo[3],
+                         const long hi[3], int native, void *stream);
+/* loops 1+2 fused (same box): reads A, B; writes A = B and Bnew = stencil(A_new)
+ * into Bnew (a second buffer of B's layout), B's values outside the box copied
+ * into Bnew; MAX partials as loop 1 */
+long dvmhgb_jac3d_fused_items(const long lo[3], const long hi[3]);
+int dvmhgb_jac3d_fused(double *A, const double *B, double *Bnew, const long st[3], const long ext[3],
+                       const long lo[3], const long hi[3], double *items, int native, void *stream);
+
+/* ---- Jacobi 2-D (examples/Jacobi/jac2d.c:49-64, FP64) ---- */
+long dvmhgb_jac2d_update_items(const long lo[2], const long hi[2]);
+int dvmhgb_jac2d_update(double *A, const double *B, const long st[2], const long lo[2], const long hi[2],
+                        double *items, int native, void *stream);
+int dvmhgb_jac2d_stencil(const double *A, double *B, const long st[2], const long ext[2], const long lo[2],
+                         const long hi[2], int native, void *stream);
+long dvmhgb_jac2d_fused_items(const long lo[2], const long hi[2]);
+int dvmhgb_jac2d_fused(double *A, const double *B, double *Bnew, const long st[2], const long ext[2],
+                       const long lo[2], const long hi[2], double *items, int native, void *stream);
+
+/* ---- SOR 3-D ACROSS (1:1,1:1,1:1), FP64: one sweep as a persistent tiled
+ * wavefront; items = canonical row-chunk partials of SUM (nv-old)^2;
+ * wDev = device address of omega; scratch = dvmhgb_sor3d_scratch_bytes() bytes;
+ * status = dvmhgb_status_word() ---- */
+long dvmhgb_sor3d_items(const long lo[3], const long hi[3]);
+long dvmhgb_sor3d_scratch_bytes(const long lo[3], const long hi[3]);
+int dvmhgb_sor3d_sweep(double *A, const long st[3], const long ext[3], const long lo[3], const long hi[3],
+                       const double *wDev, double *items, void *scratch, int *status, void *stream);
+
+/* ---- explicit 2-D heat step, FP64 (workloads/heat.c), with SUM and MINLOC:
+ * per (row, 64-wide chunk) unit one SUM item (canonical pairwise tree), one
+ * MINLOC value item and its location {i, j} (two ints) ---- */
+typedef struct {
+    const double *src;
+    double *dst;
+    long s0;                 /* row stride of src and dst (elements, even) */
+    long lo0, hi0, lo1, hi1; /* loop box */
+    const double *coef;      /* device address of c */
+    long c0, nck, units, unitBase;
+    double *sumItems, *minItems;
+    int *locItems;
+} dvmhgb_heat_desc;
+int dvmhgb_heat_desc_fill(dvmhgb_heat_desc *d, const double *src, double *dst, long rowStride, const long lo[2],
+                          const long hi[2], const double *coefDev);
+int dvmhgb_heat(const dvmhgb_heat_desc *d, void *stream);
+/* dDev: device array of n descriptors with unitBase = prefix sums of units */
+int dvmhgb_heat_many(const dvmhgb_heat_desc *dDev, int n, long totalUnits, void *stream);
+
+/* copy src -> dst for every element of the array outside the box (both arrays share st/ext) */
+int dvmhgb_copy_outside_box(int rank, const double *src, double *dst, const long *st, const long *ext,
+                            const long *lo, const long *hi, void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+#pragma GCC visibility pop
+
+#endif

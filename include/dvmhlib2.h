@@ -178,6 +178,8 @@ DvmType dvmh_loop_autotransform_C(DvmType curLoop, DvmType dvmDesc[]);          
 void dvmh_loop_fill_bounds_C(DvmType curLoop, DvmType boundsLow[], DvmType boundsHigh[],
                              DvmType loopSteps[]);                                         /* :191 */
 DvmType dvmh_loop_get_slot_count_C(DvmType curLoop);                                       /* :193 */
+/* part[2*i], part[2*i+1]: the array's local part on axis i+1 on the handler's device */
+void dvmh_loop_fill_local_part_C(DvmType curLoop, const DvmType dvmDesc[], DvmType part[]);  /* :195 */
 DvmType dvmh_loop_guess_index_type_C(DvmType curLoop);                                     /* :197 */
 void dvmh_loop_cuda_register_red_C(DvmType curLoop, DvmType redIndex, void **arrayAddrPtr,
                                    void **locAddrPtr);                                     /* :202 */
