@@ -1,0 +1,316 @@
+"""Benchmark of the GB300 DVMH loop-execution path.
+
+Headline workload (N=1): the 3-D 7-point Jacobi program, FP64, 512^3 grid with
+shadow width 1 (510^3 interior cells), seeded uniform[0,1) interior, zero
+boundary.  One step = one time step of the program through the dvmh_* C ABI:
+the update loop (eps = max|B-A|, A = B) with its MAX reduction, shadow renew,
+the stencil loop, get_actual(eps) -- in the batched mode (loops captured as a
+cached CUDA graph, update+stencil fused).  --steps defaults to the
+configuration's 50 iterations.
+
+Printed as one JSON line:
+  value      cell-updates/s, device-timed (CUDA events on the runtime's stream),
+             arrays resident in HBM (2 x 1.07 GB, larger than L2: no flush needed)
+  e2e        the same metric through the C ABI from host arrays: every run loads
+             A and B from pinned host memory (H2D), runs the steps, reads A and B
+             back (D2H); bytes per step = those copies / steps
+  roofline   dominant kernel (the fused update+stencil handler): algorithmic
+             bytes 32 per cell x 510^3 cells per launch / its average duration
+             from the runtime's event timing over the timed region, against the
+             measured HBM copy bandwidth
+  cpu_baseline  the CPU port of the same loops (oracle/restate.c, OpenMP,
+             static schedule over the outermost loop like the reference host
+             handlers) on this machine's host cores, bounded sample
+  modes      the same step in plain (per-loop launches, per-loop synchronisation
+             and reduction write-back, as the reference runtime) and async modes
+  configs    SOR-3D ACROSS 384^3 x 20 sweeps and the batched uneven heat
+             program (256 arrays, 64..2048, 200 steps), batched vs plain
+`--impl reference` times the CPU port alone (the reference runtime itself
+cannot be built on this machine: its sources are not present here).
+"""
+import argparse
+import ctypes
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+N_DEFAULT = 512
+SEED = 20261203
+BYTES_PER_CELL = 32  # A and B each read once and written once per step
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class Clocks:
+    """nvidia-smi samples during the timed region."""
+
+    def __init__(self):
+        self.rows = []
+        self.p = None
+
+    def start(self):
+        q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+             "clocks_event_reasons.sw_power_cap")
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", "-i", os.environ.get("CUDA_VISIBLE_DEVICES", "0").split(",")[0],
+                                       "--query-gpu=" + q, "--format=csv,noheader,nounits", "-lms", "200"],
+                                      stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.p = None
+
+    def _read(self):
+        for line in self.p.stdout:
+            self.rows.append([x.strip() for x in line.split(",")])
+
+    def stop(self):
+        if not self.p:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.25)
+        self.p.terminate()
+        try:
+            self.p.wait(timeout=2)
+        except Exception:
+            self.p.kill()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in self.rows:
+            try:
+                sm.append(float(r[0]))
+                mx.append(float(r[1]))
+                for k, nm in enumerate(names):
+                    if r[3 + k].lower().startswith("active"):
+                        reasons.add(nm)
+            except Exception:
+                pass
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def cpu_port_rate(n, seconds=10.0, max_iters=40, threads=None):
+    """Jacobi-3D steps of the CPU port on the host cores: (cell-updates/s, iters, threads)."""
+    from oracle import orc
+    L = orc.lib()
+    threads = threads or L.orc_max_threads()
+    A, B = orc.jacobi_init(3, n, SEED)
+    L.orc_jacobi_step(3, n, orc.P(A), orc.P(B), threads)  # warm-up (first touch)
+    it, t0 = 0, time.time()
+    while it < max_iters and (it < 2 or time.time() - t0 < seconds):
+        L.orc_jacobi_step(3, n, orc.P(A), orc.P(B), threads)
+        it += 1
+    dt = time.time() - t0
+    return (n - 2) ** 3 * it / dt, it, threads
+
+
+def run_reference(args):
+    """The CPU port alone, on all host threads, same workload and metric."""
+    from oracle import orc
+    L = orc.lib()
+    n = args.grid
+    threads = L.orc_max_threads()
+    A, B = orc.jacobi_init(3, n, SEED)
+    for _ in range(args.warmup):
+        L.orc_jacobi_step(3, n, orc.P(A), orc.P(B), threads)
+    t0 = time.time()
+    for _ in range(args.steps):
+        L.orc_jacobi_step(3, n, orc.P(A), orc.P(B), threads)
+    dt = time.time() - t0
+    v = (n - 2) ** 3 * args.steps / dt
+    line = {"impl": "reference", "metric": "cell-updates/s", "value": v, "unit": "cell-updates/s",
+            "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000 * dt / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": "jacobi3d-7pt fp64 %d^3 (%d^3 interior), CPU port of the host handlers" % (n, n - 2),
+                       "grid": n},
+            "cpu_baseline": {"value": v, "unit": "cell-updates/s", "cores": threads, "kind": "port",
+                             "sample": "%d steps of the %d^3 workload" % (args.steps, n)},
+            "e2e": {"value": v, "unit": "cell-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "note": "reference runtime not buildable on this machine (its sources are absent); CPU port of its loops"}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=50)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300")
+    ap.add_argument("--grid", type=int, default=N_DEFAULT)
+    ap.add_argument("--quick", action="store_true", help="headline only (no extra modes/configs/cpu leg)")
+    args = ap.parse_args()
+    rank = int(os.environ.get("RANK", "0"))
+    if args.impl == "reference":
+        if rank == 0:
+            run_reference(args)
+        return
+    if args.gpus > 1:
+        # one GPU per rank, independent replicas (the path does not shard: one process, one GPU)
+        os.environ.setdefault("DVMH_GB_DEVICE", os.environ.get("LOCAL_RANK", "0"))
+
+    import torch
+    import __graft_entry__ as ge
+    ge.build()
+    _, g = ge.package()
+    g.init()
+    rt = g.runtime()
+    stream = torch.cuda.ExternalStream(rt.dvmhgb_stream())
+    wl = g.workloads()
+    n = args.grid
+    cells = (n - 2) ** 3
+
+    def timed_run(mode, steps, warmup, clocks=None):
+        g.set_mode(mode)
+        j = g.Jacobi(3, n, SEED)
+        j.run(warmup)
+        g.sync()
+        g.reset_stats()
+        rt.dvmhgb_timing_reset()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        if clocks:
+            clocks.start()
+        torch.cuda.synchronize()
+        e0.record(stream)
+        j.run(steps)
+        e1.record(stream)
+        g.sync()
+        torch.cuda.synchronize()
+        ck = clocks.stop() if clocks else None
+        ms = e0.elapsed_time(e1) / steps
+        st = g.stats()
+        j.close()
+        return ms, st, ck
+
+    # headline: batched mode with handler timing on (event nodes in the graph)
+    rt.dvmhgb_set_timing(1)
+    clocks = Clocks()
+    ms, st, ck = timed_run("batched", args.steps, args.warmup, clocks)
+    tot = ctypes.c_double()
+    cnt = ctypes.c_long()
+    fused = ctypes.cast(wl.loop_jac3d_fused_cuda, ctypes.c_void_p)
+    rt.dvmhgb_timing_get(fused, ctypes.byref(tot), ctypes.byref(cnt))
+    rt.dvmhgb_set_timing(0)
+    kern_ms = tot.value / max(cnt.value, 1)
+    peak, peak_kind = peaks()
+    achieved = BYTES_PER_CELL * cells / (kern_ms * 1e-3) / 1e9
+    value = cells / (ms * 1e-3)
+
+    # e2e: host arrays in, host arrays out, through the C ABI
+    e2e_runs = 2
+    g.set_mode("batched")
+    j = g.Jacobi(3, n, SEED)
+    A0, B0 = j.fetch()
+    j.run(3)  # graphs captured
+    g.sync()
+    t0 = time.time()
+    for _ in range(e2e_runs):
+        j.load(A0, B0)
+        j.run(args.steps)
+        A, B = j.fetch()
+    dt = time.time() - t0
+    j.close()
+    e2e = {"value": cells * args.steps * e2e_runs / dt, "unit": "cell-updates/s",
+           "h2d_bytes_per_step": int((2 * 8 * n ** 3 + 8 * args.steps) / args.steps),
+           "d2h_bytes_per_step": int((2 * 8 * n ** 3 + 8 * args.steps) / args.steps),
+           "note": "per run: load A,B from pinned host memory, %d steps, read A,B back" % args.steps}
+
+    line = {"metric": "cell-updates/s", "value": value, "unit": "cell-updates/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic: splitmix64-seeded uniform[0,1) interior, zero boundary",
+            "config": {"workload": "jacobi3d-7pt fp64 %d^3 (%d^3 interior), update+MAX, renew, stencil per step"
+                                   % (n, n - 2), "grid": n, "mode": "batched (captured graph, fused loops)",
+                       "l2": "no flush: inputs 2 x %.2f GB > 129 MB L2" % (8 * n ** 3 / 1e9),
+                       "parallelism": "replicas" if args.gpus > 1 else "single GPU"},
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "peak_kind": peak_kind,
+                         "traffic": None, "kernel": "loop_jac3d_fused_cuda (fused update+stencil, incl. its fold)",
+                         "bytes_per_launch": BYTES_PER_CELL * cells, "launch_ms": kern_ms,
+                         "hbm_frac_of_step": BYTES_PER_CELL * cells / (ms * 1e-3) / 1e9 / peak},
+            "clocks": ck, "e2e": e2e, "gpu_launches": st["kernel_launches"]}
+    traffic = os.path.join(ROOT, "profiles", "traffic.json")
+    if os.path.exists(traffic):
+        try:
+            tj = json.load(open(traffic))
+            line["roofline"]["traffic"] = tj.get("jac3d_fused_bytes_per_launch_512")
+        except Exception:
+            pass
+
+    if not args.quick and rank == 0:
+        modes = {}
+        for mode in ("plain", "async"):
+            mms, _, _ = timed_run(mode, min(args.steps, 20), 2)
+            modes[mode] = {"value": cells / (mms * 1e-3), "ms_per_step": mms}
+        modes["batched"] = {"value": value, "ms_per_step": ms}
+        line["modes"] = modes
+        line["configs"] = extra_configs(g, stream)
+        v, it, thr = cpu_port_rate(n)
+        line["cpu_baseline"] = {"value": v, "unit": "cell-updates/s", "cores": thr, "kind": "port",
+                                "sample": "%d Jacobi-3D steps at %d^3 on the host cores" % (it, n)}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
+def extra_configs(g, stream):
+    import torch
+    out = {}
+    # SOR 3-D ACROSS 384^3, 20 sweeps
+    n, sweeps = 384, 20
+    res = {}
+    for mode in ("batched", "plain"):
+        g.set_mode(mode)
+        s = g.Sor(n, 1.5, SEED + 2)
+        s.run(2)
+        g.sync()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        s.run(sweeps)
+        e1.record(stream)
+        g.sync()
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / sweeps
+        s.close()
+        res[mode] = {"value": (n - 2) ** 3 / (ms * 1e-3), "ms_per_sweep": ms}
+    out["sor3d_across_384"] = {"unit": "cell-updates/s", "bytes_per_cell": 16, **res}
+    # batched uneven heat: 256 arrays, sides log-uniform in [64, 2048], 200 steps
+    res = {}
+    for mode in ("batched", "plain"):
+        g.set_mode(mode)
+        h = g.Heat(256, 64, 2048, 0.2, SEED + 3)
+        cells = h.cells()
+        steps = 200 if mode == "batched" else 50
+        h.run(3)
+        g.sync()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        t0 = time.time()
+        e0.record(stream)
+        h.run(steps)
+        e1.record(stream)
+        g.sync()
+        torch.cuda.synchronize()
+        wall = (time.time() - t0) / steps
+        ms = e0.elapsed_time(e1) / steps
+        h.close()
+        res[mode] = {"value": cells / (ms * 1e-3), "ms_per_step": ms, "wall_ms_per_step": 1000 * wall, "steps": steps}
+    res["batched_over_plain"] = res["batched"]["value"] / res["plain"]["value"]
+    out["heat_batched_256"] = {"unit": "cell-updates/s", "bytes_per_cell": 16, "cells": cells, **res}
+    g.set_mode("batched")
+    return out
+
+
+if __name__ == "__main__":
+    main()

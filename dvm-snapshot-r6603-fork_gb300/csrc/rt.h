@@ -292,8 +292,8 @@ void loopsAtExit();
 
 // ---------------------------------------------------------------- tuner (rt_tuner.cpp)
 
-struct TuneKey;
-void tunerPick(Loop *l, int block[3]);
-void tunerRecord(Loop *l, const int block[3], double seconds);
+bool tunerWants(const Loop *l);  // record timings of this loop shape
+void tunerPick(Loop *l, int block[3], int *variant);
+void tunerRecord(const Loop *l, const int block[3], int variant, double seconds);
 
 }  // namespace dvmhgb

@@ -106,8 +106,10 @@ void deviceFinish() {
     cudaStreamSynchronize(gpu.stream);
 }
 
+void collectTimings();
 void streamSync() {
     GB_CUDA(cudaStreamSynchronize(gpu.stream));
+    collectTimings();
     int code = *(volatile int *)gpu.statusHost;
     GB_CHECK(code == 0, "a kernel gave up waiting for a dependency (status 0x%08x): results of the last loops are invalid",
              (unsigned)code);

@@ -42,9 +42,58 @@ static std::unordered_map<void *, DvmHandlerFunc> batchRules;
 
 static std::vector<Loop *> queue;
 
+// ---------------------------------------------------------------- handler timing
+// With timing on, every handler execution is bracketed by CUDA events on the
+// runtime stream (inside a captured graph they become event-record nodes and
+// fire on every replay).  Elapsed times are collected at the next stream
+// synchronisation and accumulated per handler: the runtime's timing database.
+struct TimedExec {
+    void *func;
+    cudaEvent_t e0, e1;
+    Loop *loopCopy;  // loop shape for the tuner (owned), may be null
+    int block[3];
+    int variant;
+    bool inGraph;  // owned by a cached graph (reused on every replay)
+};
+struct TimingTotal {
+    double ms = 0;
+    long count = 0;
+};
+static std::vector<TimedExec> pendingTimes;
+static std::unordered_map<void *, TimingTotal> timingTotals;
+static bool timingOn = false;
+
+static cudaEvent_t newEvent() {
+    cudaEvent_t e;
+    GB_CUDA(cudaEventCreate(&e));
+    return e;
+}
+
+void collectTimings() {  // called after a stream synchronisation
+    for (auto &t : pendingTimes) {
+        float ms = 0;
+        if (cudaEventElapsedTime(&ms, t.e0, t.e1) == cudaSuccess) {
+            TimingTotal &tt = timingTotals[t.func];
+            tt.ms += ms;
+            tt.count++;
+            if (t.loopCopy) tunerRecord(t.loopCopy, t.block, t.variant, ms * 1e-3);
+        }
+        if (!t.inGraph) {
+            cudaEventDestroy(t.e0);
+            cudaEventDestroy(t.e1);
+            delete t.loopCopy;
+        }
+    }
+    pendingTimes.clear();
+}
+
+static char graphTimingKey;  // handler key for graphs that ran several handlers
+
 struct CachedGraph {
     uint64_t key;
     std::vector<uint64_t> sig;
+    std::vector<TimedExec> times;  // handlers captured into the graph
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
     cudaGraphExec_t exec = nullptr;
     std::vector<void *> scratch;
     std::vector<void *> hostScratch;
@@ -96,6 +145,7 @@ static void loopArrays(const Loop *l, std::vector<const void *> &out) {
 // ---------------------------------------------------------------- execution of one loop's handler
 
 struct ExecCtx {
+    std::vector<TimedExec> *times = nullptr;  // capture: event pairs belong to the graph
     bool capturing = false;
     std::vector<void *> *keep = nullptr;      // scratch kept alive with a cached graph
     std::vector<void *> *keepHost = nullptr;  // pinned host scratch kept with it
@@ -145,11 +195,66 @@ static void finishSpec(SpecLoop *s) {
     delete s;
 }
 
+// Inside a capture no event is recorded (a timing event cannot be captured):
+// the handler is noted and the graph launch as a whole is timed instead.
+static void timeBegin(TimedExec &t, void *func) {
+    t.func = func;
+    t.e0 = t.e1 = nullptr;
+    t.loopCopy = nullptr;
+    t.block[0] = t.block[1] = t.block[2] = 0;
+    t.variant = -1;
+    t.inGraph = ctx.capturing;
+    if (ctx.capturing) return;
+    t.e0 = newEvent();
+    t.e1 = newEvent();
+    GB_CUDA(cudaEventRecord(t.e0, gpu.stream));
+}
+static void timeEnd(TimedExec &t) {
+    if (ctx.capturing) {
+        if (ctx.times) ctx.times->push_back(t);
+        return;
+    }
+    GB_CUDA(cudaEventRecord(t.e1, gpu.stream));
+    pendingTimes.push_back(t);
+}
+
+// a launch of a cached graph, timed as a whole when timing is on; the time
+// goes to its handler when it ran exactly one
+static void launchGraph(CachedGraph &g) {
+    bool timed = timingOn && !g.times.empty();
+    if (timed) {
+        if (!g.e0) {
+            g.e0 = newEvent();
+            g.e1 = newEvent();
+        }
+        GB_CUDA(cudaEventRecord(g.e0, gpu.stream));
+    }
+    GB_CUDA(cudaGraphLaunch(g.exec, gpu.stream));
+    if (timed) {
+        GB_CUDA(cudaEventRecord(g.e1, gpu.stream));
+        TimedExec t = g.times[0];
+        if (g.times.size() > 1) t.func = (void *)&graphTimingKey;
+        t.e0 = g.e0;
+        t.e1 = g.e1;
+        t.loopCopy = nullptr;
+        t.inGraph = true;
+        pendingTimes.push_back(t);
+    }
+}
+
 static void runSingle(Loop *l) {
     SpecLoop *s = newSpec(l);
     DvmType ref = (DvmType)s;
     stats.handler_calls++;
+    TimedExec t;
+    if (timingOn) timeBegin(t, (void *)l->cuda.func);
     callWithParams(l->cuda.func, &ref, l->cuda.nparams, l->cuda.params);
+    if (timingOn) {
+        memcpy(t.block, s->block, sizeof t.block);
+        t.variant = s->variant;
+        t.loopCopy = tunerWants(l) ? new Loop(*l) : nullptr;
+        timeEnd(t);
+    }
     finishSpec(s);
 }
 
@@ -162,7 +267,10 @@ static void runFused(DvmHandlerFunc fused, Loop *a, Loop *b) {
     for (int i = 0; i < b->cuda.nparams; i++) params[n++] = b->cuda.params[i];
     stats.handler_calls++;
     stats.fused_pairs++;
+    TimedExec t;
+    if (timingOn) timeBegin(t, (void *)fused);
     callWithParams(fused, refs, n, params);
+    if (timingOn) timeEnd(t);
     finishSpec(sa);
     finishSpec(sb);
 }
@@ -178,10 +286,13 @@ static void runBatch(DvmHandlerFunc batched, const std::vector<Loop *> &group) {
     stats.batched_groups++;
     deferFolds = true;
     deferred.clear();
+    TimedExec t;
+    if (timingOn) timeBegin(t, (void *)batched);
     ((void (*)(DvmType *, DvmType))batched)(refs.data(), (DvmType)refs.size());
     deferFolds = false;
     if (!deferred.empty()) launchRedFoldBatch(deferred, gpu.stream, specs[0]->scratch, specs[0]->hostScratch);
     deferred.clear();
+    if (timingOn) timeEnd(t);
     for (SpecLoop *s : specs) finishSpec(s);
 }
 
@@ -285,6 +396,10 @@ static uint64_t hashSig(const std::vector<uint64_t> &s) {
 
 static void dropGraph(CachedGraph &g) {
     streamSync();
+    if (g.e0) {
+        cudaEventDestroy(g.e0);
+        cudaEventDestroy(g.e1);
+    }
     if (g.exec) cudaGraphExecDestroy(g.exec);
     for (void *p : g.scratch) devFree(p);
     for (void *p : g.hostScratch) hostFree(p);
@@ -299,7 +414,7 @@ void queueFlush() {
     uint64_t key = hashSig(sig);
     for (auto it = graphCache.begin(); it != graphCache.end(); ++it) {
         if (it->key == key && it->sig == sig) {
-            GB_CUDA(cudaGraphLaunch(it->exec, gpu.stream));
+            launchGraph(*it);
             for (Array *a : it->swaps) std::swap(a->dev, a->devAlt);
             stats.graph_replays++;
             stats.kernel_launches += it->launches;
@@ -314,6 +429,7 @@ void queueFlush() {
     g.sig = sig;
     long launchesBefore = stats.kernel_launches;
     ctx.capturing = true;
+    ctx.times = &g.times;
     ctx.keep = &g.scratch;
     ctx.keepHost = &g.hostScratch;
     ctx.swaps = &g.swaps;
@@ -325,7 +441,7 @@ void queueFlush() {
     GB_CUDA(cudaGraphInstantiate(&g.exec, graph, 0));
     cudaGraphDestroy(graph);
     g.launches = stats.kernel_launches - launchesBefore;
-    GB_CUDA(cudaGraphLaunch(g.exec, gpu.stream));
+    launchGraph(g);
     stats.graphs_captured++;
     graphCache.push_front(std::move(g));
     while ((int)graphCache.size() > settings.graphCacheMax) {
@@ -642,7 +758,7 @@ void dvmh_loop_cuda_get_config_C(DvmType curLoop, DvmType sharedPerThread, DvmTy
     } else {
         defaultBlock(l->rank, b);
     }
-    if (!l->userBlock && settings.tuneMode) tunerPick(l, b);
+    if (!l->userBlock && settings.tuneMode) tunerPick(l, b, &s->variant);
     if (sharedPerThread < 0) sharedPerThread = 0;
     memcpy(s->block, b, sizeof b);
     if (t) {
@@ -852,6 +968,24 @@ void *dvmhgb_loop_host_scratch(DvmType loopRef, DvmType bytes) {
 }
 
 int *dvmhgb_status_word(void) { return gpu.statusDev; }
+
+void dvmhgb_set_timing(int on) {
+    queueFlush();
+    timingOn = on != 0;
+}
+
+int dvmhgb_timing_get(DvmHandlerFunc handler, double *totalMs, long *count) {
+    streamSync();
+    auto it = timingTotals.find((void *)handler);
+    if (totalMs) *totalMs = it == timingTotals.end() ? 0.0 : it->second.ms;
+    if (count) *count = it == timingTotals.end() ? 0 : it->second.count;
+    return it == timingTotals.end() ? -1 : 0;
+}
+
+void dvmhgb_timing_reset(void) {
+    streamSync();
+    timingTotals.clear();
+}
 
 void *dvmhgb_loop_param(DvmType loopRef, DvmType index) {
     SpecLoop *s = specOf(loopRef, "dvmhgb_loop_param");

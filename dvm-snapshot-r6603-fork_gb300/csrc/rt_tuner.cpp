@@ -1,6 +1,7 @@
 // placeholder, replaced by the tuner
 #include "rt.h"
 namespace dvmhgb {
-void tunerPick(Loop *, int[3]) {}
-void tunerRecord(Loop *, const int[3], double) {}
+bool tunerWants(const Loop *) { return false; }
+void tunerPick(Loop *, int[3], int *) {}
+void tunerRecord(const Loop *, const int[3], int, double) {}
 }  // namespace dvmhgb

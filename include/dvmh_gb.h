@@ -69,6 +69,15 @@ int dvmhgb_loop_variant(DvmType loopRef, int nvariants, int dflt);
  * random operand pairs: mismatches[0..3] = add, sub, mul, division by 6. */
 int dvmhgb_selftest_softfp64(long n, unsigned long long seed, long mismatches[4]);
 
+/* ---- handler timing (the runtime's timing database) -----------------------
+ * On: every handler execution is bracketed by CUDA events on the runtime
+ * stream (recorded inside captured graphs too) and accumulated per handler at
+ * each synchronisation.  dvmhgb_timing_get returns the total milliseconds and
+ * the number of executions recorded for a handler (0 on success, -1 if none). */
+void dvmhgb_set_timing(int on);
+int dvmhgb_timing_get(DvmHandlerFunc handler, double *totalMs, long *count);
+void dvmhgb_timing_reset(void);
+
 /* ---- statistics --------------------------------------------------------- */
 typedef struct {
     long loops_performed;   /* dvmh_loop_perform_C calls */
