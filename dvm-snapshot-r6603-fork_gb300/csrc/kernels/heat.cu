@@ -133,7 +133,10 @@ extern "C" {
 
 int dvmhgb_heat_desc_fill(dvmhgb_heat_desc *d, const double *src, double *dst, long rowStride, const long lo[2],
                           const long hi[2], const double *coefDev) {
-    if (!d || hi[0] < lo[0] || hi[1] < lo[1] || lo[0] < 1 || lo[1] < 1 || (rowStride & 1)) return -1;
+    // 128-bit accesses: even row stride and 16-byte aligned bases
+    if (!d || hi[0] < lo[0] || hi[1] < lo[1] || lo[0] < 1 || lo[1] < 1 || (rowStride & 1) ||
+        ((uintptr_t)src & 15) || ((uintptr_t)dst & 15))
+        return -1;
     d->src = src;
     d->dst = dst;
     d->s0 = rowStride;

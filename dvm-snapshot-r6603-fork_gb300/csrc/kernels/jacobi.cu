@@ -103,6 +103,14 @@ __global__ void __launch_bounds__(UPD_THREADS) kUpdate(double *A, const double *
     if (threadIdx.x == 0) items[blockIdx.x] = m;
 }
 
+// 128-bit accesses need 16-byte aligned rows: even outer strides, aligned bases
+bool aligned16(const void *p) { return ((uintptr_t)p & 15) == 0; }
+bool rows16(const long *st, int rank) {
+    for (int i = 0; i < rank - 1; i++)
+        if (st[i] & 1) return false;
+    return st[rank - 1] == 1;
+}
+
 struct UpdGeom {
     unsigned units, nseg, nj;
     long p0, p1;
@@ -598,7 +606,7 @@ long dvmhgb_jac3d_update_items(const long lo[3], const long hi[3]) {
 int dvmhgb_jac3d_update(double *A, const double *B, const long st[3], const long lo[3], const long hi[3],
                         double *items, int native, void *stream) {
     UpdGeom g = updGeom(hi[0] - lo[0] + 1, hi[1] - lo[1] + 1, lo[2], hi[2]);
-    if (!g.ok || !A || !B || !items || st[2] != 1) return -1;
+    if (!g.ok || !A || !B || !items || !rows16(st, 3) || !aligned16(A) || !aligned16(B)) return -1;
     kUpdate<<<(unsigned)g.blocks, UPD_THREADS, 0, (cudaStream_t)stream>>>(A, B, st[0], st[1], lo[0], lo[1], lo[2],
                                                                           hi[2], g.nj, g.units, g.nseg, g.p0, g.p1,
                                                                           items, native);
@@ -609,7 +617,7 @@ int dvmhgb_jac3d_update(double *A, const double *B, const long st[3], const long
 int dvmhgb_jac3d_stencil(const double *A, double *B, const long st[3], const long ext[3], const long lo[3],
                          const long hi[3], int native, void *stream) {
     St3Geom g = st3Geom(lo, hi, TY * JT_PLAIN);
-    if (!g.ok || !A || !B || st[2] != 1) return -1;
+    if (!g.ok || !A || !B || !rows16(st, 3) || !aligned16(A) || !aligned16(B)) return -1;
     Box3 b{st[0], st[1], ext[0], ext[1], ext[2], lo[0], lo[1], lo[2], hi[0], hi[1], hi[2]};
     launch3<false>(native, g, (double *)A, nullptr, B, b, nullptr, (cudaStream_t)stream);
     dvmhgb_count_launches(1);
@@ -624,7 +632,8 @@ long dvmhgb_jac3d_fused_items(const long lo[3], const long hi[3]) {
 int dvmhgb_jac3d_fused(double *A, const double *B, double *Bnew, const long st[3], const long ext[3],
                        const long lo[3], const long hi[3], double *items, int native, void *stream) {
     St3Geom g = st3Geom(lo, hi, TY * JT_FUSED);
-    if (!g.ok || !A || !B || !Bnew || !items || st[2] != 1) return -1;
+    if (!g.ok || !A || !B || !Bnew || !items || !rows16(st, 3) || !aligned16(A) || !aligned16(B) || !aligned16(Bnew))
+        return -1;
     Box3 b{st[0], st[1], ext[0], ext[1], ext[2], lo[0], lo[1], lo[2], hi[0], hi[1], hi[2]};
     launch3<true>(native, g, A, B, Bnew, b, items, (cudaStream_t)stream);
     dvmhgb_count_launches(1);
@@ -639,7 +648,7 @@ long dvmhgb_jac2d_update_items(const long lo[2], const long hi[2]) {
 int dvmhgb_jac2d_update(double *A, const double *B, const long st[2], const long lo[2], const long hi[2],
                         double *items, int native, void *stream) {
     UpdGeom g = updGeom(hi[0] - lo[0] + 1, 1, lo[1], hi[1]);
-    if (!g.ok || !A || !B || !items || st[1] != 1) return -1;
+    if (!g.ok || !A || !B || !items || !rows16(st, 2) || !aligned16(A) || !aligned16(B)) return -1;
     kUpdate<<<(unsigned)g.blocks, UPD_THREADS, 0, (cudaStream_t)stream>>>(A, B, st[0], 0, lo[0], 0, lo[1], hi[1],
                                                                           g.nj, g.units, g.nseg, g.p0, g.p1, items, native);
     dvmhgb_count_launches(1);
@@ -649,7 +658,7 @@ int dvmhgb_jac2d_update(double *A, const double *B, const long st[2], const long
 int dvmhgb_jac2d_stencil(const double *A, double *B, const long st[2], const long ext[2], const long lo[2],
                          const long hi[2], int native, void *stream) {
     St2Geom g = st2Geom(lo, hi);
-    if (!g.ok || !A || !B || st[1] != 1) return -1;
+    if (!g.ok || !A || !B || !rows16(st, 2) || !aligned16(A) || !aligned16(B)) return -1;
     Box2 b{st[0], ext[0], ext[1], lo[0], lo[1], hi[0], hi[1]};
     launch2<false>(native, g, (double *)A, nullptr, B, b, nullptr, (cudaStream_t)stream);
     dvmhgb_count_launches(1);
@@ -664,7 +673,8 @@ long dvmhgb_jac2d_fused_items(const long lo[2], const long hi[2]) {
 int dvmhgb_jac2d_fused(double *A, const double *B, double *Bnew, const long st[2], const long ext[2],
                        const long lo[2], const long hi[2], double *items, int native, void *stream) {
     St2Geom g = st2Geom(lo, hi);
-    if (!g.ok || !A || !B || !Bnew || !items || st[1] != 1) return -1;
+    if (!g.ok || !A || !B || !Bnew || !items || !rows16(st, 2) || !aligned16(A) || !aligned16(B) || !aligned16(Bnew))
+        return -1;
     Box2 b{st[0], ext[0], ext[1], lo[0], lo[1], hi[0], hi[1]};
     launch2<true>(native, g, A, B, Bnew, b, items, (cudaStream_t)stream);
     dvmhgb_count_launches(1);
