@@ -25,6 +25,7 @@
 #include <cuda_runtime.h>
 
 #include <cstdint>
+#include <cstdio>
 
 #include "../../../include/dvmh_gb.h"
 #include "../../../include/dvmh_gb_kernels.h"
@@ -680,6 +681,79 @@ int dvmhgb_jac2d_fused(double *A, const double *B, double *Bnew, const long st[2
     dvmhgb_count_launches(1);
     if (cudaGetLastError() != cudaSuccess) return -1;
     return dvmhgb_copy_outside_box(2, B, Bnew, st, ext, lo, hi, stream);
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------- update loop without allocation
+//
+// For callers that cannot allocate device memory: code running while a CUDA
+// stream is being captured into a graph in global capture mode (cudaMalloc is
+// illegal there and would also synchronise the device), hosts whose own
+// allocator owns all of the GPU's memory and forbids other allocations, or
+// code on a latency-critical path that must not block in the driver.  The
+// per-CTA partial maxima live in this file-scope array instead of a buffer the
+// caller or the runtime allocates.  Every GPU that loads the library holds it
+// (32 KB) until the process exits.  Every call uses the same array and leaves
+// its partials there; nothing in it needs to start at zero, because each call
+// writes every entry it later reads.  Calls whose GPU work overlaps in time
+// (different streams, or host threads without ordering) race on the array.
+namespace {
+
+constexpr long NOALLOC_PARTIALS = 4096;  // maximum CTAs of one call
+__device__ __align__(256) double noallocPartials[NOALLOC_PARTIALS];
+
+// eps = the largest partial (MAX is order-independent)
+__global__ void __launch_bounds__(256) kMaxPartials(const double *partials, long n, double *eps) {
+    __shared__ double sh[8];
+    double m = -__builtin_huge_val();
+    for (long i = threadIdx.x; i < n; i += blockDim.x) m = maxOf(partials[i], m);
+    m = ctaMax(m, sh);
+    if (threadIdx.x == 0) eps[0] = m;
+}
+
+// device address of noallocPartials on each device, looked up once per device
+constexpr int MAX_DEVICES = 64;
+double *noallocAddr[MAX_DEVICES];
+bool noallocReady[MAX_DEVICES];
+
+}  // namespace
+
+extern "C" {
+
+int dvmhgb_jac3d_update_noalloc(double *A, const double *B, const long st[3], const long lo[3], const long hi[3],
+                                double *epsDev, void *stream) {
+    if (!A || !B || !epsDev || !st || !lo || !hi || !rows16(st, 3) || !aligned16(A) || !aligned16(B)) return -1;
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= MAX_DEVICES) return -3;
+    if (!noallocReady[dev]) {
+        // first call on this device: take the array's address with the device current
+        void *p = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&p, noallocPartials);
+        if (e != cudaSuccess) {
+            fprintf(stderr, "dvmhgb_jac3d_update_noalloc: cudaGetSymbolAddress failed on device %d: %s\n", dev,
+                    cudaGetErrorString(e));
+            return -3;
+        }
+        noallocAddr[dev] = (double *)p;
+        noallocReady[dev] = true;
+    }
+    UpdGeom g = updGeom(hi[0] - lo[0] + 1, hi[1] - lo[1] + 1, lo[2], hi[2]);
+    if (!g.ok) return -1;
+    if (g.blocks > NOALLOC_PARTIALS) {
+        fprintf(stderr,
+                "dvmhgb_jac3d_update_noalloc: this launch needs %ld partial slots, the static array has %ld "
+                "(use dvmhgb_jac3d_update with a caller-provided buffer)\n",
+                g.blocks, NOALLOC_PARTIALS);
+        return -2;
+    }
+    cudaStream_t s = (cudaStream_t)stream;
+    double *partials = noallocAddr[dev];
+    kUpdate<<<(unsigned)g.blocks, UPD_THREADS, 0, s>>>(A, B, st[0], st[1], lo[0], lo[1], lo[2], hi[2], g.nj, g.units,
+                                                       g.nseg, g.p0, g.p1, partials, 1);
+    kMaxPartials<<<1, 256, 0, s>>>(partials, g.blocks, epsDev);
+    dvmhgb_count_launches(2);
+    return cudaGetLastError() == cudaSuccess ? 0 : -3;
 }
 
 int dvmhgb_copy_outside_box(int rank, const double *src, double *dst, const long *st, const long *ext,

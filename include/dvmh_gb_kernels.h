@@ -77,6 +77,23 @@ int dvmhgb_heat(const dvmhgb_heat_desc *d, void *stream);
 /* dDev: device array of n descriptors with unitBase = prefix sums of units */
 int dvmhgb_heat_many(const dvmhgb_heat_desc *dDev, int n, long totalUnits, void *stream);
 
+/* ---- no counterpart in the reference: the Jacobi-3D update loop for callers
+ * that cannot allocate device memory (inside a stream capture in global mode,
+ * under a host allocator that owns the whole GPU, on a path that must not
+ * block in the driver).  Same work as dvmhgb_jac3d_update with native = 1,
+ * then eps = max |B - A| over the box is written to epsDev (one double in
+ * device memory).  Partial maxima go to a file-scope static __device__ array
+ * of 4096 doubles (32 KB, held by every GPU that loads the library until the
+ * process exits), not to a caller buffer: nothing is allocated and no
+ * allocating library routine is called.  The first call on a device looks up
+ * the array's device address (cudaGetSymbolAddress) with that device current;
+ * make that first call before any stream capture.  All calls share the array:
+ * calls whose GPU work overlaps in time race.  Returns 0; -1 invalid
+ * arguments; -2 the launch would need more than 4096 partial slots (message
+ * on stderr); -3 CUDA error. ---- */
+int dvmhgb_jac3d_update_noalloc(double *A, const double *B, const long st[3], const long lo[3], const long hi[3],
+                                double *epsDev, void *stream);
+
 /* copy src -> dst for every element of the array outside the box (both arrays share st/ext) */
 int dvmhgb_copy_outside_box(int rank, const double *src, double *dst, const long *st, const long *ext,
                             const long *lo, const long *hi, void *stream);
