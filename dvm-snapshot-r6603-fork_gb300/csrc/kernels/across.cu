@@ -35,6 +35,7 @@ constexpr int SI = TI + 2, SJ = TJ + 2, SK = TK + 2;
 constexpr size_t SMEM = sizeof(double) * SI * SJ * SK;
 constexpr long SPIN_LIMIT = 1L << 24;    // ~1-4 s of polling before giving up
 constexpr int ERR_SOR_TIMEOUT = 0x50520001;
+constexpr long MAX_DIAGS = 2048;         // a + b diagonals (tile grid up to 1024 x 1024 in i, j)
 
 struct Geo {
     long s0, s1;
@@ -47,32 +48,28 @@ struct Geo {
 
 __device__ __forceinline__ long tileLinear(const Geo &g, long a, long b, long c) { return (a * g.nb + b) * g.nc + c; }
 
-// number of (b, c) with b + c = s, 0 <= b < nb, 0 <= c < nc
-__device__ __forceinline__ long pairsOnDiag(long s, long nb, long nc) {
-    if (s < 0) return 0;
-    long bmin = s - (nc - 1) > 0 ? s - (nc - 1) : 0;
-    long bmax = s < nb - 1 ? s : nb - 1;
-    return bmax >= bmin ? bmax - bmin + 1 : 0;
+// Tiles are handed out in the order (a + b, then c, then a): a topological
+// order -- (a-1,b,c) and (a,b-1,c) lie on the previous a+b diagonal, (a,b,c-1)
+// earlier on the same one -- that keeps whole 2-D diagonals in flight.
+// pre[s] = number of tiles before diagonal s (shared memory, built per CTA).
+__device__ __forceinline__ long diagLen(long s, long na, long nb) {  // #(a,b), a+b = s
+    long amin = s - (nb - 1) > 0 ? s - (nb - 1) : 0;
+    long amax = s < na - 1 ? s : na - 1;
+    return amax >= amin ? amax - amin + 1 : 0;
 }
 
-// the idx-th tile in diagonal order (d = a+b+c ascending, then a, then b)
-__device__ void tileAt(const Geo &g, long idx, long &a, long &b, long &c) {
-    for (long d = 0;; d++) {
-        long amin = d - (g.nb - 1) - (g.nc - 1) > 0 ? d - (g.nb - 1) - (g.nc - 1) : 0;
-        long amax = d < g.na - 1 ? d : g.na - 1;
-        for (long aa = amin; aa <= amax; aa++) {
-            long cnt = pairsOnDiag(d - aa, g.nb, g.nc);
-            if (idx < cnt) {
-                long s = d - aa;
-                long bmin = s - (g.nc - 1) > 0 ? s - (g.nc - 1) : 0;
-                a = aa;
-                b = bmin + idx;
-                c = s - b;
-                return;
-            }
-            idx -= cnt;
-        }
+__device__ void tileAt(const Geo &g, const long *pre, long ns, long idx, long &a, long &b, long &c) {
+    long lo = 0, hi = ns - 1;  // last s with pre[s] <= idx
+    while (lo < hi) {
+        long mid = (lo + hi + 1) >> 1;
+        if (pre[mid] <= idx) lo = mid;
+        else hi = mid - 1;
     }
+    long sd = lo, len = diagLen(sd, g.na, g.nb), rem = idx - pre[sd];
+    c = rem / len;
+    long amin = sd - (g.nb - 1) > 0 ? sd - (g.nb - 1) : 0;
+    a = amin + rem % len;
+    b = sd - a;
 }
 
 __device__ __forceinline__ int ldAcquire(const int *p) {
@@ -86,11 +83,22 @@ __device__ __forceinline__ void stRelease(int *p, int v) {
 
 __global__ void __launch_bounds__(NT) kSorWave(double *A, Geo g, const double *wPtr, int *done, unsigned *counter,
                                                double *items, int *status) {
-    extern __shared__ double sm[];  // [SI][SJ][SK]
+    extern __shared__ double sm[];  // [SI][SJ][SK], then pre[ns + 1]
     __shared__ long sIdx;
     __shared__ int sFail;
     const int tid = threadIdx.x, li = tid / TJ, lj = tid % TJ;
     const long ntiles = g.na * g.nb * g.nc;
+    const long ns = g.na + g.nb - 1;
+    long *pre = (long *)(sm + SI * SJ * SK);
+    if (tid == 0) {
+        long acc = 0;
+        for (long sd = 0; sd < ns; sd++) {
+            pre[sd] = acc;
+            acc += diagLen(sd, g.na, g.nb) * g.nc;
+        }
+        pre[ns] = acc;
+    }
+    __syncthreads();
     const double w = *wPtr;
     const double c1 = 1.0 - w, c2 = w / 6.0;  // loop invariants, rounded as in the source expression
     const long nck = g.nc;
@@ -103,7 +111,7 @@ __global__ void __launch_bounds__(NT) kSorWave(double *A, Geo g, const double *w
         const long idx = sIdx;
         if (idx >= ntiles) break;
         long a, b, c;
-        tileAt(g, idx, a, b, c);
+        tileAt(g, pre, ns, idx, a, b, c);
         // wait for the face predecessors (bounded)
         if (tid < 3) {
             long pa = a - (tid == 0), pb = b - (tid == 1), pc = c - (tid == 2);
@@ -229,11 +237,14 @@ int dvmhgb_sor3d_sweep(double *A, const long st[3], const long ext[3], const lon
     long ntiles = g.na * g.nb * g.nc;
     unsigned *counter = (unsigned *)scratch;
     int *done = (int *)scratch + 64;  // counter on its own 256-byte line
+    const long ns = g.na + g.nb - 1;
+    if (ns > MAX_DIAGS) return -1;
+    const size_t smem = SMEM + sizeof(long) * (MAX_DIAGS + 1);
     if (cudaMemsetAsync(scratch, 0, (size_t)(ntiles + 64) * sizeof(int), s) != cudaSuccess) return -1;
     static int occ = 0, sms = 0;
     if (!occ) {
-        cudaFuncSetAttribute(kSorWave, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM);
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kSorWave, NT, SMEM);
+        cudaFuncSetAttribute(kSorWave, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kSorWave, NT, smem);
         int dev = 0;
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
@@ -241,7 +252,7 @@ int dvmhgb_sor3d_sweep(double *A, const long st[3], const long ext[3], const lon
     }
     long grid = (long)occ * sms;  // all CTAs resident at once: waits always resolve
     if (grid > ntiles) grid = ntiles;
-    kSorWave<<<(unsigned)grid, NT, SMEM, s>>>(A, g, wDev, done, counter, items, status);
+    kSorWave<<<(unsigned)grid, NT, smem, s>>>(A, g, wDev, done, counter, items, status);
     dvmhgb_count_launches(1);
     return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }

@@ -293,6 +293,7 @@ void loopsAtExit();
 // ---------------------------------------------------------------- tuner (rt_tuner.cpp)
 
 bool tunerWants(const Loop *l);  // record timings of this loop shape
+int tunerVariant(const Loop *l, int nvariants, int dflt, bool bestOnly);
 void tunerPick(Loop *l, int block[3], int *variant);
 void tunerRecord(const Loop *l, const int block[3], int variant, double seconds);
 

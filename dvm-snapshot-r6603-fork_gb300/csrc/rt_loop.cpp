@@ -658,6 +658,7 @@ void dvmh_loop_register_handler_C(DvmType curLoop, DvmType deviceType, DvmType h
 
 void dvmh_loop_perform_C(DvmType curLoop) {
     Loop *l = loopOf(curLoop, "dvmh_loop_perform");
+    if (settings.tuneMode) timingOn = true;  // the tuner learns from recorded timings
     stats.loops_performed++;
     st.curLoop = nullptr;
     GB_CHECK(l->region && l->region->started,
@@ -947,8 +948,13 @@ int dvmhgb_loop_variant(DvmType loopRef, int nvariants, int dflt) {
     GB_CHECK(nvariants >= 1 && dflt >= 0 && dflt < nvariants, "invalid variant request");
     static int forced = getenv("DVMH_GB_VARIANT") ? atoi(getenv("DVMH_GB_VARIANT")) : -1;
     int v = s->variant >= 0 ? s->variant : dflt;
+    // online tuning explores only in immediate execution (a captured graph keeps its choice)
+    if (settings.tuneMode && !ctx.capturing) v = tunerVariant(s->loop, nvariants, dflt, false);
+    else if (settings.tuneMode) v = tunerVariant(s->loop, nvariants, dflt, true);
     if (forced >= 0) v = forced;
-    return v < nvariants ? v : nvariants - 1;
+    v = v < nvariants ? v : nvariants - 1;
+    s->variant = v;
+    return v;
 }
 
 void *dvmhgb_loop_scratch(DvmType loopRef, DvmType bytes) {

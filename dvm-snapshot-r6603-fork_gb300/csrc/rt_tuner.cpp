@@ -1,7 +1,270 @@
-// placeholder, replaced by the tuner
+// libdvmh_gb tuner: the CUDA-block / kernel-variant autotuner, its timing
+// database, and the learned cost model that prunes its search.
+//
+// Reference counterpart (rts/dvmh/loop.cpp): CudaHandlerOptimizationParams
+// (:1464-1575, default blocks 256 / 32x8 / 32x4x2, the serialised block list
+// of genParamsRanges :1487-1532), ParamDesc's online search (:1579-1640),
+// LoopHandlerPerformanceInfo (:1644-1971, timings recorded per execution),
+// DvmhLoopPersistentInfo keyed by the loop's source position (:1975-2062).
+// Here:
+//   * every timed execution is recorded (features of loop and candidate,
+//     seconds) -- the runtime's timing database, also exported for training;
+//   * exhaustive tuning (DVMH_OPT_PARAMS=1) tries every candidate of a loop
+//     signature once, in successive executions, then keeps the fastest;
+//   * model-guided tuning (DVMH_OPT_PARAMS=2) ranks the candidates with the
+//     FP32 MLP (csrc/kernels/mlp.cu) and tries only the top k;
+//   * for the hand-written kernels the candidates are their variants (how
+//     many FP64 operations run on the FP64 unit), chosen online per loop.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <map>
+#include <unordered_map>
+
 #include "rt.h"
+#include "../../include/dvmh_gb_kernels.h"
+
 namespace dvmhgb {
-bool tunerWants(const Loop *) { return false; }
-void tunerPick(Loop *, int[3], int *) {}
-void tunerRecord(const Loop *, const int[3], int, double) {}
+
+extern dvmhgb_stats_t stats;
+
+// ---------------------------------------------------------------- timing database
+
+struct Record {
+    float f[DVMHGB_TUNE_NF];
+    long loopId;
+    int cand;
+    double seconds;
+};
+static std::vector<Record> db;
+
+// ---------------------------------------------------------------- online variant tuning of ABI loops
+
+struct VariantState {
+    std::map<int, double> best;  // variant -> best seconds seen
+    int nvariants = 0;
+    int pending = -1;
+};
+static std::unordered_map<uint64_t, VariantState> vstate;
+
+static uint64_t loopKey(const Loop *l) {
+    uint64_t h = (uint64_t)l->cuda.func * 0x9E3779B97F4A7C15ull;
+    for (int i = 0; i < l->rank; i++) h = (h ^ (uint64_t)(l->hi[i] - l->lo[i] + 1)) * 1099511628211ull;
+    h ^= (uint64_t)l->depMask;
+    return h;
+}
+
+bool tunerWants(const Loop *l) { return settings.tuneMode != 0 && l->hasCuda; }
+
+void tunerPick(Loop *l, int block[3], int *variant) {
+    (void)l;
+    (void)block;
+    (void)variant;  // the variant is chosen when the handler asks (dvmhgb_loop_variant)
+}
+
+int tunerVariant(const Loop *l, int nvariants, int dflt, bool bestOnly) {
+    if (settings.tuneMode == 0) return dflt;
+    VariantState &vs = vstate[loopKey(l)];
+    vs.nvariants = nvariants;
+    if (!bestOnly)
+        for (int v = 0; v < nvariants; v++)
+            if (!vs.best.count(v)) return v;  // exhaustive: untried variants first
+    if (vs.best.empty()) return dflt;
+    int bestV = dflt;
+    double bestT = 1e300;
+    for (auto &kv : vs.best)
+        if (kv.second < bestT) {
+            bestT = kv.second;
+            bestV = kv.first;
+        }
+    return bestV;
+}
+
+void tunerRecord(const Loop *l, const int block[3], int variant, double seconds) {
+    (void)block;
+    if (variant < 0) return;
+    VariantState &vs = vstate[loopKey(l)];
+    auto it = vs.best.find(variant);
+    if (it == vs.best.end() || seconds < it->second) vs.best[variant] = seconds;
+}
+
+// ---------------------------------------------------------------- synthetic loops: candidates, features
+
+static const int BLOCKS[][3] = {{32, 1, 1},  {64, 1, 1},  {128, 1, 1}, {256, 1, 1}, {512, 1, 1}, {1024, 1, 1},
+                                {32, 2, 1},  {32, 4, 1},  {32, 8, 1},  {32, 16, 1}, {64, 2, 1},  {64, 4, 1},
+                                {64, 8, 1},  {128, 2, 1}, {128, 4, 1}, {16, 16, 1}, {8, 32, 1},  {16, 4, 1},
+                                {32, 4, 2},  {32, 8, 2},  {32, 2, 4},  {16, 8, 2},  {64, 2, 2},  {32, 4, 4},
+                                {16, 4, 4},  {8, 8, 4},   {64, 4, 2},  {128, 2, 2}};
+
+static int candidates(const dvmhgb_synth_loop *L, dvmhgb_synth_cand *out, int maxOut) {
+    int n = 0;
+    for (const auto &b : BLOCKS) {
+        if (b[1] > 1 && L->rank < 2) continue;
+        if (b[2] > 1 && L->rank < 3 && !L->across) continue;
+        for (int ept = 1; ept <= 2; ept++)
+            for (int xin = 1; xin >= 0; xin--) {
+                if (!xin && (L->rank == 1 || L->across)) continue;
+                dvmhgb_synth_cand c{b[0], b[1], b[2], xin, ept};
+                if (dvmhgb_synth_items(L, &c) < 0) continue;
+                if (n < maxOut) out[n] = c;
+                n++;
+            }
+    }
+    return std::min(n, maxOut);
+}
+
+static float lg(double v) { return (float)std::log2(v > 1 ? v : 1); }
+
+static void features(const dvmhgb_synth_loop *L, const dvmhgb_synth_cand *C, float *f) {
+    memset(f, 0, sizeof(float) * DVMHGB_TUNE_NF);
+    double total = 1, inner = (double)L->ext[L->rank - 1], outer = (double)L->ext[0];
+    for (int a = 0; a < L->rank; a++) total *= (double)L->ext[a];
+    int k = 0;
+    f[k++] = (float)L->rank;
+    for (int a = 0; a < 4; a++) f[k++] = a < L->rank ? lg((double)L->ext[a]) : 0.0f;
+    f[k++] = lg(total);
+    f[k++] = (float)L->radius;
+    f[k++] = (float)L->esize / 4.0f;
+    f[k++] = (float)L->isint;
+    f[k++] = (float)(L->red == 1);
+    f[k++] = (float)(L->red == 2);
+    f[k++] = (float)(L->red == 3);
+    f[k++] = (float)L->across;
+    f[k++] = lg(C->bx);
+    f[k++] = lg(C->by);
+    f[k++] = lg(C->bz);
+    f[k++] = lg((double)C->bx * C->by * C->bz);
+    f[k++] = (float)C->ept;
+    f[k++] = (float)C->xinner;
+    double xext = C->xinner ? inner : outer;
+    f[k++] = lg(xext / ((double)C->bx * C->ept));                                 // blocks along x
+    f[k++] = lg(std::max(1.0, total / ((double)C->bx * C->by * C->bz * C->ept)));  // blocks in all
+    f[k++] = lg(xext) - lg((double)C->bx * C->ept);                               // x fill (waste)
+    f[k++] = (float)((long)xext % (C->bx * C->ept) == 0);
+    f[k++] = lg(total * (1 + 2 * L->radius * L->rank) * L->esize);                 // bytes touched
+}
+
+// ---------------------------------------------------------------- learned model
+
+static std::vector<float> model;  // packed MLP parameters (host copy)
+static std::vector<float> fmean, fstd;
+static float *modelDev = nullptr;
+
+static void rankByModel(const std::vector<std::vector<float>> &feats, std::vector<int> &order) {
+    int n = (int)feats.size();
+    order.resize(n);
+    for (int i = 0; i < n; i++) order[i] = i;
+    if (model.empty() || n == 0) return;
+    std::vector<float> X((size_t)n * DVMHGB_TUNE_NF);
+    for (int i = 0; i < n; i++)
+        for (int j = 0; j < DVMHGB_TUNE_NF; j++)
+            X[(size_t)i * DVMHGB_TUNE_NF + j] = (feats[i][j] - fmean[j]) / fstd[j];
+    float *dX = (float *)devAlloc(X.size() * sizeof(float));
+    float *dY = (float *)devAlloc(n * sizeof(float));
+    float *work = (float *)devAlloc(dvmhgb_mlp_work_floats(n) * sizeof(float));
+    GB_CUDA(cudaMemcpyAsync(dX, X.data(), X.size() * sizeof(float), cudaMemcpyHostToDevice, gpu.stream));
+    GB_CHECK(dvmhgb_mlp_forward(modelDev, dX, n, dY, work, gpu.stream) == 0, "cost model forward failed");
+    std::vector<float> y(n);
+    GB_CUDA(cudaMemcpyAsync(y.data(), dY, n * sizeof(float), cudaMemcpyDeviceToHost, gpu.stream));
+    streamSync();
+    devFree(dX);
+    devFree(dY);
+    devFree(work);
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return y[a] < y[b]; });
+}
+
 }  // namespace dvmhgb
+
+using namespace dvmhgb;
+
+extern "C" {
+
+int dvmhgb_tuner_candidates(const dvmhgb_synth_loop *L, dvmhgb_synth_cand *out, int maxOut) {
+    return candidates(L, out, maxOut);
+}
+
+void dvmhgb_tuner_features(const dvmhgb_synth_loop *L, const dvmhgb_synth_cand *C, float *f) { features(L, C, f); }
+
+// Runs the synthetic loop with candidate C `reps` times on the runtime stream
+// (one untimed warm-up first) and records the fastest into the database.
+double dvmhgb_tuner_time_synth(const dvmhgb_synth_loop *L, const dvmhgb_synth_cand *C, long loopId, int cand,
+                               int reps) {
+    long elems = dvmhgb_synth_elems(L), items = dvmhgb_synth_items(L, C);
+    if (elems <= 0 || items < 0) return -1;
+    size_t bytes = (size_t)elems * L->esize;
+    void *in = devAlloc(bytes), *out = devAlloc(bytes);
+    void *it = devAlloc((size_t)std::max(items, 1L) * 8);
+    long *locs = (long *)devAlloc((size_t)std::max(items, 1L) * 8);
+    GB_CUDA(cudaMemsetAsync(in, 0, bytes, gpu.stream));
+    cudaEvent_t e0, e1;
+    GB_CUDA(cudaEventCreate(&e0));
+    GB_CUDA(cudaEventCreate(&e1));
+    double best = 1e300;
+    int rc = dvmhgb_synth_run(L, C, in, out, it, locs, gpu.stream);
+    for (int r = 0; rc == 0 && r < reps; r++) {
+        GB_CUDA(cudaEventRecord(e0, gpu.stream));
+        rc = dvmhgb_synth_run(L, C, in, out, it, locs, gpu.stream);
+        GB_CUDA(cudaEventRecord(e1, gpu.stream));
+        GB_CUDA(cudaEventSynchronize(e1));
+        float ms = 0;
+        GB_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+        best = std::min(best, (double)ms * 1e-3);
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    streamSync();
+    devFree(in);
+    devFree(out);
+    devFree(it);
+    devFree(locs);
+    if (rc != 0) return -1;
+    Record rec;
+    features(L, C, rec.f);
+    rec.loopId = loopId;
+    rec.cand = cand;
+    rec.seconds = best;
+    db.push_back(rec);
+    return best;
+}
+
+long dvmhgb_tuner_db_size(void) { return (long)db.size(); }
+
+long dvmhgb_tuner_db_export(float *X, double *seconds, long *loopIds, int *cands, long maxRows) {
+    long n = std::min(maxRows, (long)db.size());
+    for (long i = 0; i < n; i++) {
+        if (X) memcpy(X + i * DVMHGB_TUNE_NF, db[i].f, sizeof(float) * DVMHGB_TUNE_NF);
+        if (seconds) seconds[i] = db[i].seconds;
+        if (loopIds) loopIds[i] = db[i].loopId;
+        if (cands) cands[i] = db[i].cand;
+    }
+    return n;
+}
+
+void dvmhgb_tuner_db_clear(void) { db.clear(); }
+
+// Installs the cost model: packed MLP parameters (dvmhgb_mlp_nparams floats)
+// and the per-feature normalisation used in training.
+int dvmhgb_tuner_set_model(const float *params, const float *mean, const float *stdv) {
+    long np = dvmhgb_mlp_nparams();
+    model.assign(params, params + np);
+    fmean.assign(mean, mean + DVMHGB_TUNE_NF);
+    fstd.assign(stdv, stdv + DVMHGB_TUNE_NF);
+    for (auto &s : fstd)
+        if (s <= 0) s = 1;
+    if (modelDev) devFree(modelDev);
+    modelDev = (float *)devAlloc(np * sizeof(float));
+    GB_CUDA(cudaMemcpy(modelDev, model.data(), np * sizeof(float), cudaMemcpyHostToDevice));
+    return 0;
+}
+
+// Candidate order by predicted time (fastest first) for loop L.
+int dvmhgb_tuner_rank(const dvmhgb_synth_loop *L, const dvmhgb_synth_cand *cands, int n, int *order) {
+    std::vector<std::vector<float>> feats(n, std::vector<float>(DVMHGB_TUNE_NF));
+    for (int i = 0; i < n; i++) features(L, &cands[i], feats[i].data());
+    std::vector<int> o;
+    rankByModel(feats, o);
+    for (int i = 0; i < n; i++) order[i] = o[i];
+    return model.empty() ? -1 : 0;
+}
+
+}  // extern "C"

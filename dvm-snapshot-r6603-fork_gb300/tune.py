@@ -1,0 +1,198 @@
+"""The tuner's training and evaluation pipeline on synthetic parallel loops.
+
+1. Draw loops (seeded): rank 1-4, total extent log-uniform in [2^6, 2^24],
+   stencil radius 0-3, fp32/fp64/int32, reduction none/sum/max/minloc,
+   ACROSS on the outermost axis for some rank>=2 loops.
+2. Exhaustive tuning: the runtime times every candidate (CUDA block, axis on
+   threadIdx.x, elements per thread; 16-64 per loop) and records each timing
+   in its database (dvmhgb_tuner_time_synth).
+3. Training: the database's features and log-times (centred per loop, so the
+   model learns the ranking) train the FP32 MLP on the GPU with the library's
+   own kernels (dvmhgb_mlp_train).
+4. Evaluation on held-out loops: the model ranks the candidates, the top k
+   (about 10% of the candidates) are timed, the best of them is compared with
+   the exhaustive best; the tuning time is the summed time of the candidates
+   actually run.  Baselines: the reference's default block
+   (rts/dvmh/loop.cpp:1464-1485) and k random candidates.
+"""
+import ctypes
+import math
+import time
+
+import numpy as np
+
+MAXC = 64
+
+
+class SynthLoop(ctypes.Structure):
+    _fields_ = [("rank", ctypes.c_int), ("radius", ctypes.c_int), ("across", ctypes.c_int), ("red", ctypes.c_int),
+                ("esize", ctypes.c_int), ("isint", ctypes.c_int), ("ext", ctypes.c_long * 4)]
+
+
+class SynthCand(ctypes.Structure):
+    _fields_ = [("bx", ctypes.c_int), ("by", ctypes.c_int), ("bz", ctypes.c_int), ("xinner", ctypes.c_int),
+                ("ept", ctypes.c_int)]
+
+
+def draw_loops(count, seed, max_elems=1 << 25):
+    rng = np.random.default_rng(seed)
+    out = []
+    while len(out) < count:
+        rank = int(rng.integers(1, 5))
+        total = 2.0 ** rng.uniform(6, 24)
+        w = rng.dirichlet(np.ones(rank))
+        ext = [max(2, int(round(total ** wi))) for wi in w]
+        radius = int(rng.integers(0, 4))
+        dt = int(rng.integers(0, 3))  # fp32, fp64, int32
+        red = int(rng.integers(0, 4))
+        across = int(rank >= 2 and rng.uniform() < 0.2)
+        padded = 1
+        for e in ext:
+            padded *= e + 2 * radius
+        if padded > max_elems:
+            continue
+        out.append(make_loop(rank, ext, radius, dt, red, across))
+    return out
+
+
+def make_loop(rank, ext, radius, dt, red, across):
+    L = SynthLoop()
+    L.rank, L.radius, L.across, L.red = rank, radius, across, red
+    L.esize = 8 if dt == 1 else 4
+    L.isint = 1 if dt == 2 else 0
+    for a in range(4):
+        L.ext[a] = ext[a] if a < rank else 0
+    return L
+
+
+def config_loops():
+    """The workloads' loop shapes as synthetic loops: Jacobi-2D 1022^2 MAX,
+    Jacobi-3D 510^3 MAX, SOR 382^3 SUM with ACROSS (fp64, radius 1)."""
+    return {"jacobi2d_1024": make_loop(2, [1022, 1022], 1, 1, 2, 0),
+            "jacobi3d_512": make_loop(3, [510, 510, 510], 1, 1, 2, 0),
+            "sor3d_384": make_loop(3, [382, 382, 382], 1, 1, 1, 1)}
+
+
+def default_cand(L, cands):
+    """The reference's default block for the loop's rank: 256 / 32x8 / 32x4x2."""
+    want = {1: (256, 1, 1), 2: (32, 8, 1)}.get(L.rank, (32, 4, 2))
+    for i, c in enumerate(cands):
+        if (c.bx, c.by, c.bz, c.xinner, c.ept) == (*want, 1, 1):
+            return i
+    return 0
+
+
+class Tuner:
+    def __init__(self, rt):
+        self.rt = rt
+        rt.dvmhgb_tuner_time_synth.restype = ctypes.c_double
+        rt.dvmhgb_tuner_db_size.restype = ctypes.c_long
+        rt.dvmhgb_tuner_db_export.restype = ctypes.c_long
+        rt.dvmhgb_mlp_nparams.restype = ctypes.c_long
+
+    def candidates(self, L):
+        arr = (SynthCand * MAXC)()
+        n = self.rt.dvmhgb_tuner_candidates(ctypes.byref(L), arr, MAXC)
+        return [arr[i] for i in range(n)]
+
+    def exhaustive(self, L, loop_id, reps=2):
+        """Times every candidate; returns the seconds per candidate (recorded in the runtime's database)."""
+        cands = self.candidates(L)
+        ts = [self.rt.dvmhgb_tuner_time_synth(ctypes.byref(L), ctypes.byref(c), loop_id, i, reps)
+              for i, c in enumerate(cands)]
+        return cands, np.array(ts)
+
+    def features(self, L, cands):
+        F = np.zeros((len(cands), 24), dtype=np.float32)
+        row = (ctypes.c_float * 24)()
+        for i, c in enumerate(cands):
+            self.rt.dvmhgb_tuner_features(ctypes.byref(L), ctypes.byref(c), row)
+            F[i] = np.frombuffer(row, dtype=np.float32)
+        return F
+
+    def train(self, X, y, epochs=200, batch=4096, lr=1e-3, seed=1):
+        np_ = self.rt.dvmhgb_mlp_nparams()
+        params = np.zeros(np_, dtype=np.float32)
+        losses = np.zeros(epochs, dtype=np.float32)
+        fp = ctypes.POINTER(ctypes.c_float)
+        X = np.ascontiguousarray(X, dtype=np.float32)
+        y = np.ascontiguousarray(y, dtype=np.float32)
+        rc = self.rt.dvmhgb_mlp_train(X.ctypes.data_as(fp), y.ctypes.data_as(fp), ctypes.c_long(len(y)), epochs,
+                                      ctypes.c_long(batch), ctypes.c_float(lr), ctypes.c_ulonglong(seed),
+                                      params.ctypes.data_as(fp), losses.ctypes.data_as(fp))
+        assert rc == 0, "training failed"
+        return params, losses
+
+    def install(self, params, mean, std):
+        fp = ctypes.POINTER(ctypes.c_float)
+        self.rt.dvmhgb_tuner_set_model(np.ascontiguousarray(params, np.float32).ctypes.data_as(fp),
+                                       np.ascontiguousarray(mean, np.float32).ctypes.data_as(fp),
+                                       np.ascontiguousarray(std, np.float32).ctypes.data_as(fp))
+
+    def rank(self, L, cands):
+        arr = (SynthCand * len(cands))(*cands)
+        order = (ctypes.c_int * len(cands))()
+        assert self.rt.dvmhgb_tuner_rank(ctypes.byref(L), arr, len(cands), order) == 0
+        return list(order)
+
+
+def run(rt, n_loops=2000, n_test=200, seed=20261207, reps=2, epochs=200, frac=0.10, log=print):
+    """Returns a dict of the evaluation (the bench's TUNE line)."""
+    tu = Tuner(rt)
+    rt.dvmhgb_tuner_db_clear()
+    loops = draw_loops(n_loops, seed)
+    t0 = time.time()
+    times = []
+    cands_all = []
+    for q, L in enumerate(loops):
+        cands, ts = tu.exhaustive(L, q, reps)
+        cands_all.append(cands)
+        times.append(ts)
+    t_collect = time.time() - t0
+    n_train = n_loops - n_test
+    # training set: the database rows of the first n_train loops, log-time centred per loop
+    X, y = [], []
+    for q in range(n_train):
+        F = tu.features(loops[q], cands_all[q])
+        lt = np.log(np.maximum(times[q], 1e-9))
+        X.append(F)
+        y.append(lt - lt.mean())
+    X = np.concatenate(X)
+    y = np.concatenate(y)
+    mean, std = X.mean(0), X.std(0) + 1e-6
+    t1 = time.time()
+    params, losses = tu.train((X - mean) / std, y, epochs=epochs)
+    t_train = time.time() - t1
+    tu.install(params, mean, std)
+
+    def evaluate(L, cands, ts, rng):
+        nc = len(cands)
+        k = max(1, int(math.floor(frac * nc)))
+        order = tu.rank(L, cands)
+        top = order[:k]
+        best_model = ts[top].min()
+        best = ts.min()
+        rand = rng.choice(nc, size=k, replace=False)
+        return {"k": k, "n": nc, "ratio": best_model / best, "tune_frac": ts[top].sum() / ts.sum(),
+                "default_ratio": ts[default_cand(L, cands)] / best, "random_ratio": ts[rand].min() / best}
+
+    rng = np.random.default_rng(seed + 1)
+    res = [evaluate(loops[q], cands_all[q], times[q], rng) for q in range(n_train, n_loops)]
+    cfg = {}
+    for name, L in config_loops().items():
+        cands, ts = tu.exhaustive(L, -1, reps)
+        cfg[name] = evaluate(L, cands, ts, rng)
+    r = np.array([x["ratio"] for x in res])
+    out = {"loops": n_loops, "train": n_train, "test": n_test,
+           "candidates_mean": float(np.mean([x["n"] for x in res])),
+           "db_rows": int(rt.dvmhgb_tuner_db_size()),
+           "within_5pct": float(np.mean(r <= 1.05)), "ratio_geomean": float(np.exp(np.mean(np.log(r)))),
+           "ratio_p90": float(np.quantile(r, 0.9)),
+           "tuning_time_frac_mean": float(np.mean([x["tune_frac"] for x in res])),
+           "default_block_ratio_geomean": float(np.exp(np.mean(np.log([x["default_ratio"] for x in res])))),
+           "random_k_ratio_geomean": float(np.exp(np.mean(np.log([x["random_ratio"] for x in res])))),
+           "random_k_within_5pct": float(np.mean(np.array([x["random_ratio"] for x in res]) <= 1.05)),
+           "configs": {k: {kk: float(vv) for kk, vv in v.items()} for k, v in cfg.items()},
+           "loss_first_last": [float(losses[0]), float(losses[-1])],
+           "seconds": {"collect": t_collect, "train": t_train}}
+    return out

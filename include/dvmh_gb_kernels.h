@@ -94,6 +94,50 @@ int dvmhgb_heat_many(const dvmhgb_heat_desc *dDev, int n, long totalUnits, void 
 int dvmhgb_jac3d_update_noalloc(double *A, const double *B, const long st[3], const long lo[3], const long hi[3],
                                 double *epsDev, void *stream);
 
+/* ---- synthetic parallel loops (the tuner's training and evaluation set):
+ * rank 1..4 star stencil of radius 0..3 over float/double/int arrays padded
+ * by the radius, optional SUM/MAX/MINLOC reduction (1/2/3; one partial per
+ * CTA into items, MINLOC offsets into locs), optional ACROSS on the outermost
+ * axis; launch configuration = candidate (block, axis on x, elements per
+ * thread) ---- */
+typedef struct {
+    int rank, radius, across, red, esize, isint;
+    long ext[4];
+} dvmhgb_synth_loop;
+typedef struct {
+    int bx, by, bz, xinner, ept;
+} dvmhgb_synth_cand;
+long dvmhgb_synth_elems(const dvmhgb_synth_loop *L);
+long dvmhgb_synth_items(const dvmhgb_synth_loop *L, const dvmhgb_synth_cand *C);
+int dvmhgb_synth_run(const dvmhgb_synth_loop *L, const dvmhgb_synth_cand *C, const void *in, void *out, void *items,
+                     long *locs, void *stream);
+
+/* ---- the tuner's cost model: 3-layer FP32 MLP, DVMHGB_TUNE_NF -> 128 -> 128 -> 1
+ * (ReLU), parameters packed W1,b1,W2,b2,W3,b3; trained on the GPU by these
+ * kernels (MSE of log-time, Adam) ---- */
+#define DVMHGB_TUNE_NF 24
+long dvmhgb_mlp_nparams(void);
+long dvmhgb_mlp_work_floats(long n);
+int dvmhgb_mlp_init(float *params, unsigned long long seed, void *stream);
+int dvmhgb_mlp_forward(const float *params, const float *X, long n, float *pred, float *work, void *stream);
+int dvmhgb_mlp_loss_grad(const float *params, const float *X, const float *y, long n, float *grad, float *loss,
+                         float *work, void *stream);
+int dvmhgb_mlp_adam(float *params, const float *grad, float *m, float *v, long step, float lr, void *stream);
+int dvmhgb_mlp_train(const float *X, const float *y, long n, int epochs, long batch, float lr,
+                     unsigned long long seed, float *params, float *losses);
+
+/* ---- the tuner (runtime): candidates and features of a synthetic loop, its
+ * timing (recorded in the runtime's timing database), database export, and
+ * ranking by the installed cost model ---- */
+int dvmhgb_tuner_candidates(const dvmhgb_synth_loop *L, dvmhgb_synth_cand *out, int maxOut);
+void dvmhgb_tuner_features(const dvmhgb_synth_loop *L, const dvmhgb_synth_cand *C, float *f);
+double dvmhgb_tuner_time_synth(const dvmhgb_synth_loop *L, const dvmhgb_synth_cand *C, long loopId, int cand, int reps);
+long dvmhgb_tuner_db_size(void);
+long dvmhgb_tuner_db_export(float *X, double *seconds, long *loopIds, int *cands, long maxRows);
+void dvmhgb_tuner_db_clear(void);
+int dvmhgb_tuner_set_model(const float *params, const float *mean, const float *stdv);
+int dvmhgb_tuner_rank(const dvmhgb_synth_loop *L, const dvmhgb_synth_cand *cands, int n, int *order);
+
 /* copy src -> dst for every element of the array outside the box (both arrays share st/ext) */
 int dvmhgb_copy_outside_box(int rank, const double *src, double *dst, const long *st, const long *ext,
                             const long *lo, const long *hi, void *stream);

@@ -1,0 +1,82 @@
+"""The tuner's cost model on the GPU: forward and gradient of the hand-written
+MLP kernels against the float64 numpy oracle; Adam training reduces the loss;
+the learned tuner beats the methods without it on held-out synthetic loops
+while timing about a tenth of the candidates."""
+import ctypes
+import importlib.util
+import os
+
+import numpy as np
+import pytest
+
+import __graft_entry__ as ge
+from oracle import mlp_ref
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def rt():
+    ge.build()
+    _, g = ge.package()
+    g.init()
+    rt = g.runtime()
+    rt.dvmhgb_mlp_nparams.restype = ctypes.c_long
+    rt.dvmhgb_mlp_work_floats.restype = ctypes.c_long
+    return rt
+
+
+def test_mlp_forward_and_gradient_match_oracle(rt):
+    import torch
+    n = 301
+    P = rt.dvmhgb_mlp_nparams()
+    p = torch.empty(P, dtype=torch.float32, device="cuda")
+    assert rt.dvmhgb_mlp_init(ctypes.c_void_p(p.data_ptr()), ctypes.c_ulonglong(11), None) == 0
+    rng = np.random.default_rng(5)
+    X = torch.tensor(rng.standard_normal((n, 24)), dtype=torch.float32, device="cuda")
+    y = torch.tensor(rng.standard_normal(n), dtype=torch.float32, device="cuda")
+    g = torch.empty(P, dtype=torch.float32, device="cuda")
+    loss = torch.empty(1, dtype=torch.float32, device="cuda")
+    pred = torch.empty(n, dtype=torch.float32, device="cuda")
+    work = torch.empty(rt.dvmhgb_mlp_work_floats(n), dtype=torch.float32, device="cuda")
+    vp = lambda t: ctypes.c_void_p(t.data_ptr())
+    assert rt.dvmhgb_mlp_forward(vp(p), vp(X), ctypes.c_long(n), vp(pred), vp(work), None) == 0
+    assert rt.dvmhgb_mlp_loss_grad(vp(p), vp(X), vp(y), ctypes.c_long(n), vp(g), vp(loss), vp(work), None) == 0
+    torch.cuda.synchronize()
+    ph = p.cpu().numpy().astype(np.float64)
+    ref_pred, _ = mlp_ref.forward(ph, X.cpu().numpy())
+    ref_loss, ref_g = mlp_ref.loss_grad(ph, X.cpu().numpy(), y.cpu().numpy())
+    assert np.allclose(pred.cpu().numpy(), ref_pred, rtol=1e-4, atol=1e-5)
+    assert abs(loss.item() - ref_loss) <= 1e-4 * abs(ref_loss) + 1e-6
+    gg = g.cpu().numpy()
+    assert np.allclose(gg, ref_g, rtol=1e-3, atol=1e-6 * np.abs(ref_g).max())
+    assert np.linalg.norm(gg - ref_g) <= 1e-4 * np.linalg.norm(ref_g)
+
+
+def test_mlp_training_reduces_loss(rt):
+    rng = np.random.default_rng(8)
+    X = rng.standard_normal((4000, 24)).astype(np.float32)
+    y = (np.sin(X[:, 0]) + X[:, 1] * X[:, 2] - 0.5 * np.abs(X[:, 3])).astype(np.float32)
+    P = rt.dvmhgb_mlp_nparams()
+    params = np.zeros(P, dtype=np.float32)
+    losses = np.zeros(60, dtype=np.float32)
+    fp = ctypes.POINTER(ctypes.c_float)
+    assert rt.dvmhgb_mlp_train(X.ctypes.data_as(fp), y.ctypes.data_as(fp), ctypes.c_long(4000), 60,
+                               ctypes.c_long(500), ctypes.c_float(2e-3), ctypes.c_ulonglong(1),
+                               params.ctypes.data_as(fp), losses.ctypes.data_as(fp)) == 0
+    assert losses[-1] < 0.2 * losses[0], losses[[0, -1]]
+    pred, _ = mlp_ref.forward(params.astype(np.float64), X)
+    assert np.mean((pred - y) ** 2) < 0.25 * np.var(y)
+
+
+def test_learned_tuner_beats_untrained_methods(rt):
+    spec = importlib.util.spec_from_file_location(
+        "dvmhgb_tune", os.path.join(os.path.dirname(ge.__file__), "dvm-snapshot-r6603-fork_gb300", "tune.py"))
+    tune = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(tune)
+    r = tune.run(rt, n_loops=400, n_test=80, seed=99, reps=2, epochs=150)
+    # the model's top ~10% against the same budget spent at random, and the default block
+    assert r["tuning_time_frac_mean"] <= 0.15, r
+    assert r["ratio_geomean"] <= r["random_k_ratio_geomean"], r
+    assert r["ratio_geomean"] < r["default_block_ratio_geomean"], r
+    assert r["within_5pct"] >= r["random_k_within_5pct"], r
