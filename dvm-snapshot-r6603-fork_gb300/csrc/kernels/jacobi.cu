@@ -81,22 +81,36 @@ __global__ void __launch_bounds__(UPD_THREADS) kUpdate(double *A, const double *
     uint64_t mb = 0;
     bool seen = false;
     const unsigned wstride = gridDim.x * (UPD_THREADS / 32);
-#pragma unroll 2
-    for (unsigned u = blockIdx.x * (UPD_THREADS / 32) + warp; u < units; u += wstride) {
-        unsigned row = u / nseg, seg = u - row * nseg;
-        unsigned ri = row / nj, rj = row - ri * nj;
-        long p = p0 + (long)seg * 32 + lane;
-        if (p <= p1) {
-            long k0 = 2 * p;
-            long off = (lo0 + ri) * s0 + (lo1 + rj) * s1 + k0;
-            double2 b = ld2cs(B + off), a = ld2cs(A + off);
-            bool in0 = k0 >= lo2 && k0 <= hi2, in1 = k0 + 1 >= lo2 && k0 + 1 <= hi2;
-            if (in0) mb = sf::absmax_bits(native ? sf::nadd(b.x, -a.x) : sf::sub(b.x, a.x), mb);
-            if (in1) mb = sf::absmax_bits(native ? sf::nadd(b.y, -a.y) : sf::sub(b.y, a.y), mb);
+    // UNITS units per trip: all their loads are issued before any is used
+    constexpr int UNITS = 4;
+    for (unsigned u0 = blockIdx.x * (UPD_THREADS / 32) + warp; u0 < units; u0 += UNITS * wstride) {
+        long off[UNITS], k0[UNITS];
+        bool live[UNITS];
+        double2 a[UNITS], b[UNITS];
+#pragma unroll
+        for (int q = 0; q < UNITS; q++) {
+            unsigned u = u0 + q * wstride;
+            unsigned row = u / nseg, seg = u - row * nseg;
+            unsigned ri = row / nj, rj = row - ri * nj;
+            long p = p0 + (long)seg * 32 + lane;
+            live[q] = u < units && p <= p1;
+            k0[q] = 2 * p;
+            off[q] = (lo0 + ri) * s0 + (lo1 + rj) * s1 + k0[q];
+            if (live[q]) {
+                b[q] = ld2cs(B + off[q]);
+                a[q] = ld2cs(A + off[q]);
+            }
+        }
+#pragma unroll
+        for (int q = 0; q < UNITS; q++) {
+            if (!live[q]) continue;
+            bool in0 = k0[q] >= lo2 && k0[q] <= hi2, in1 = k0[q] + 1 >= lo2 && k0[q] + 1 <= hi2;
+            if (in0) mb = sf::absmax_bits(native ? sf::nadd(b[q].x, -a[q].x) : sf::sub(b[q].x, a[q].x), mb);
+            if (in1) mb = sf::absmax_bits(native ? sf::nadd(b[q].y, -a[q].y) : sf::sub(b[q].y, a[q].y), mb);
             seen = seen || in0 || in1;
-            if (in0 && in1) st2cs(A + off, b);
-            else if (in0) A[off] = b.x;
-            else if (in1) A[off + 1] = b.y;
+            if (in0 && in1) st2cs(A + off[q], b[q]);
+            else if (in0) A[off[q]] = b[q].x;
+            else if (in1) A[off[q] + 1] = b[q].y;
         }
     }
     double m = seen ? sf::from(mb) : -__builtin_huge_val();
@@ -198,7 +212,7 @@ __device__ __forceinline__ double stencil5(double a, double b, double c, double 
 }
 
 template <bool FUSED, int NATIVE, int JT>
-__global__ void __launch_bounds__(TX *TY, 3) kStencil3(double *A, const double *B, double *Out, Box3 b, long p0,
+__global__ void __launch_bounds__(TX *TY, (JT > 1 && FUSED) ? 2 : 3) kStencil3(double *A, const double *B, double *Out, Box3 b, long p0,
                                                      int ichunk, double *items) {
     constexpr int TJ = TY * JT;
     __shared__ double sm[TJ + 2][SW];
@@ -568,12 +582,19 @@ __global__ void kCopyOutside(const double *__restrict__ src, double *__restrict_
 }
 
 // native = FP64 operations per cell on the FP64 unit (clamped to the kernel's count)
+// fused variant 7: all six operations native, two rows per thread
+constexpr int FUSED_JT2 = 7;
+
 template <bool FUSED>
 void launch3(int native, const St3Geom &g, double *A, const double *B, double *Out, const Box3 &b, double *items,
              cudaStream_t s) {
     const int n = FUSED ? 6 : 5;
-    native = native < 0 ? 0 : (native > n ? n : native);
     dim3 blk(TX, TY);
+    if (FUSED && native == FUSED_JT2) {
+        kStencil3<true, 6, 2><<<g.grid, blk, 0, s>>>(A, B, Out, b, g.p0, g.ichunk, items);
+        return;
+    }
+    native = native < 0 ? 0 : (native > n ? n : native);
     switch (native) {
 #define C3(N)                                                                                   \
     case N: kStencil3<FUSED, (FUSED ? N : (N > 5 ? 5 : N)), (FUSED ? JT_FUSED : JT_PLAIN)><<<g.grid, blk, 0, s>>>(A, B, Out, b, g.p0, g.ichunk, items); break;
@@ -625,14 +646,14 @@ int dvmhgb_jac3d_stencil(const double *A, double *B, const long st[3], const lon
     return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }
 
-long dvmhgb_jac3d_fused_items(const long lo[3], const long hi[3]) {
-    St3Geom g = st3Geom(lo, hi, TY * JT_FUSED);
+long dvmhgb_jac3d_fused_items(const long lo[3], const long hi[3], int native) {
+    St3Geom g = st3Geom(lo, hi, TY * (native == FUSED_JT2 ? 2 : JT_FUSED));
     return (long)g.grid.x * g.grid.y * g.grid.z;
 }
 
 int dvmhgb_jac3d_fused(double *A, const double *B, double *Bnew, const long st[3], const long ext[3],
                        const long lo[3], const long hi[3], double *items, int native, void *stream) {
-    St3Geom g = st3Geom(lo, hi, TY * JT_FUSED);
+    St3Geom g = st3Geom(lo, hi, TY * (native == FUSED_JT2 ? 2 : JT_FUSED));
     if (!g.ok || !A || !B || !Bnew || !items || !rows16(st, 3) || !aligned16(A) || !aligned16(B) || !aligned16(Bnew))
         return -1;
     Box3 b{st[0], st[1], ext[0], ext[1], ext[2], lo[0], lo[1], lo[2], hi[0], hi[1], hi[2]};

@@ -227,6 +227,60 @@ double dvmhgb_tuner_time_synth(const dvmhgb_synth_loop *L, const dvmhgb_synth_ca
     return best;
 }
 
+// All candidates of one loop: buffers allocated once, every candidate run once
+// untimed and `reps` times timed back to back, one synchronisation at the end;
+// the fastest run of each candidate is recorded.  times[i] = -1 for a
+// candidate the launcher rejects.
+int dvmhgb_tuner_time_synth_all(const dvmhgb_synth_loop *L, const dvmhgb_synth_cand *cands, int n, long loopId,
+                                int reps, double *times) {
+    long elems = dvmhgb_synth_elems(L), maxItems = 1;
+    for (int i = 0; i < n; i++) maxItems = std::max(maxItems, dvmhgb_synth_items(L, &cands[i]));
+    if (elems <= 0 || n < 1 || reps < 1) return -1;
+    size_t bytes = (size_t)elems * L->esize;
+    void *in = devAlloc(bytes), *out = devAlloc(bytes);
+    void *it = devAlloc((size_t)maxItems * 8);
+    long *locs = (long *)devAlloc((size_t)maxItems * 8);
+    GB_CUDA(cudaMemsetAsync(in, 0, bytes, gpu.stream));
+    std::vector<cudaEvent_t> ev((size_t)n * reps * 2);
+    for (auto &e : ev) GB_CUDA(cudaEventCreate(&e));
+    std::vector<int> ok(n, 1);
+    for (int i = 0; i < n; i++) {
+        if (dvmhgb_synth_run(L, &cands[i], in, out, it, locs, gpu.stream) != 0) {
+            ok[i] = 0;
+            continue;
+        }
+        for (int r = 0; r < reps; r++) {
+            GB_CUDA(cudaEventRecord(ev[((size_t)i * reps + r) * 2], gpu.stream));
+            dvmhgb_synth_run(L, &cands[i], in, out, it, locs, gpu.stream);
+            GB_CUDA(cudaEventRecord(ev[((size_t)i * reps + r) * 2 + 1], gpu.stream));
+        }
+    }
+    streamSync();
+    for (int i = 0; i < n; i++) {
+        times[i] = -1;
+        if (!ok[i]) continue;
+        double best = 1e300;
+        for (int r = 0; r < reps; r++) {
+            float ms = 0;
+            GB_CUDA(cudaEventElapsedTime(&ms, ev[((size_t)i * reps + r) * 2], ev[((size_t)i * reps + r) * 2 + 1]));
+            best = std::min(best, (double)ms * 1e-3);
+        }
+        times[i] = best;
+        Record rec;
+        features(L, &cands[i], rec.f);
+        rec.loopId = loopId;
+        rec.cand = i;
+        rec.seconds = best;
+        db.push_back(rec);
+    }
+    for (auto &e : ev) cudaEventDestroy(e);
+    devFree(in);
+    devFree(out);
+    devFree(it);
+    devFree(locs);
+    return 0;
+}
+
 long dvmhgb_tuner_db_size(void) { return (long)db.size(); }
 
 long dvmhgb_tuner_db_export(float *X, double *seconds, long *loopIds, int *cands, long maxRows) {

@@ -98,8 +98,10 @@ class Tuner:
     def exhaustive(self, L, loop_id, reps=2):
         """Times every candidate; returns the seconds per candidate (recorded in the runtime's database)."""
         cands = self.candidates(L)
-        ts = [self.rt.dvmhgb_tuner_time_synth(ctypes.byref(L), ctypes.byref(c), loop_id, i, reps)
-              for i, c in enumerate(cands)]
+        arr = (SynthCand * len(cands))(*cands)
+        ts = (ctypes.c_double * len(cands))()
+        assert self.rt.dvmhgb_tuner_time_synth_all(ctypes.byref(L), arr, len(cands), ctypes.c_long(loop_id), reps,
+                                                   ts) == 0
         return cands, np.array(ts)
 
     def features(self, L, cands):
@@ -196,3 +198,29 @@ def run(rt, n_loops=2000, n_test=200, seed=20261207, reps=2, epochs=200, frac=0.
            "loss_first_last": [float(losses[0]), float(losses[-1])],
            "seconds": {"collect": t_collect, "train": t_train}}
     return out
+
+
+if __name__ == "__main__":
+    import argparse
+    import json
+    import os
+    import sys
+    ap = argparse.ArgumentParser(description="exhaustive + learned tuning of synthetic loops")
+    ap.add_argument("--loops", type=int, default=2000)
+    ap.add_argument("--test", type=int, default=200)
+    ap.add_argument("--reps", type=int, default=2)
+    ap.add_argument("--out", default=None)
+    a = ap.parse_args()
+    sys.path.insert(0, os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+    import __graft_entry__ as ge
+    ge.build()
+    _, g = ge.package()
+    g.init()
+    t0 = time.time()
+    res = run(g.runtime(), n_loops=a.loops, n_test=a.test, reps=a.reps)
+    res["wall_seconds"] = time.time() - t0
+    text = json.dumps(res, indent=1)
+    if a.out:
+        with open(a.out, "w") as f:
+            f.write(text + "\n")
+    print(text)

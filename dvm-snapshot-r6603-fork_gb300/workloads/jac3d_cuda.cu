@@ -111,13 +111,14 @@ extern "C" void loop_jac3d_fused_cuda(DvmType refs[2], DvmType A_hdr[], DvmType 
     cudaStream_t stream;
     dvmh_loop_cuda_get_config_C(upd, 0, 0, &threads, &stream, 0);
     dvmh_loop_cuda_get_config_C(stn, 0, 0, &threads, &stream, 0);
+    const int variant = dvmhgb_loop_variant(upd, NOPS_STN + 3, DEF_FUSED);
     double eps, *eps_grid = 0;
     dvmh_loop_cuda_register_red_C(upd, 1, (void **)&eps_grid, 0);
     dvmh_loop_red_init_C(upd, 1, &eps, 0);
-    dvmh_loop_cuda_red_prepare_C(upd, 1, dvmhgb_jac3d_fused_items(lo, hi), 0);
+    dvmh_loop_cuda_red_prepare_C(upd, 1, dvmhgb_jac3d_fused_items(lo, hi, variant), 0);
     double *Bnew = (double *)dvmhgb_loop_alt_buffer(stn, B_hdr);
-    check(dvmhgb_jac3d_fused(A.base, B.base, Bnew, A.st, A.ext, lo, hi, eps_grid,
-                             dvmhgb_loop_variant(upd, NOPS_STN + 2, DEF_FUSED), stream), "loop_jac3d_fused_cuda");
+    check(dvmhgb_jac3d_fused(A.base, B.base, Bnew, A.st, A.ext, lo, hi, eps_grid, variant, stream),
+          "loop_jac3d_fused_cuda");
     dvmh_loop_cuda_red_finish_C(upd, 1);
 }
 

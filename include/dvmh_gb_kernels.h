@@ -34,8 +34,9 @@ int dvmhgb_jac3d_stencil(const double *A, double *B, const long st[3], const lon
                          const long hi[3], int native, void *stream);
 /* loops 1+2 fused (same box): reads A, B; writes A = B and Bnew = stencil(A_new)
  * into Bnew (a second buffer of B's layout), B's values outside the box copied
- * into Bnew; MAX partials as loop 1 */
-long dvmhgb_jac3d_fused_items(const long lo[3], const long hi[3]);
+ * into Bnew; MAX partials, one per CTA (count depends on the variant: native
+ * 0..6 = FP64 operations on the FP64 unit, 7 = all native, two rows a thread) */
+long dvmhgb_jac3d_fused_items(const long lo[3], const long hi[3], int native);
 int dvmhgb_jac3d_fused(double *A, const double *B, double *Bnew, const long st[3], const long ext[3],
                        const long lo[3], const long hi[3], double *items, int native, void *stream);
 
@@ -50,7 +51,8 @@ int dvmhgb_jac2d_fused(double *A, const double *B, double *Bnew, const long st[2
                        const long lo[2], const long hi[2], double *items, int native, void *stream);
 
 /* ---- SOR 3-D ACROSS (1:1,1:1,1:1), FP64: one sweep as a persistent tiled
- * wavefront; items = canonical row-chunk partials of SUM (nv-old)^2;
+ * wavefront; items = canonical partials of SUM (nv-old)^2, one per row and
+ * 32-wide half of each 64-wide chunk (row, chunk, half order);
  * wDev = device address of omega; scratch = dvmhgb_sor3d_scratch_bytes() bytes;
  * status = dvmhgb_status_word() ---- */
 long dvmhgb_sor3d_items(const long lo[3], const long hi[3]);
@@ -132,6 +134,8 @@ int dvmhgb_mlp_train(const float *X, const float *y, long n, int epochs, long ba
 int dvmhgb_tuner_candidates(const dvmhgb_synth_loop *L, dvmhgb_synth_cand *out, int maxOut);
 void dvmhgb_tuner_features(const dvmhgb_synth_loop *L, const dvmhgb_synth_cand *C, float *f);
 double dvmhgb_tuner_time_synth(const dvmhgb_synth_loop *L, const dvmhgb_synth_cand *C, long loopId, int cand, int reps);
+int dvmhgb_tuner_time_synth_all(const dvmhgb_synth_loop *L, const dvmhgb_synth_cand *cands, int n, long loopId,
+                                int reps, double *times);
 long dvmhgb_tuner_db_size(void);
 long dvmhgb_tuner_db_export(float *X, double *seconds, long *loopIds, int *cands, long maxRows);
 void dvmhgb_tuner_db_clear(void);
