@@ -4,22 +4,34 @@
 // The reference runs such a loop as one kernel launch per hyperplane from the
 // host (cdvmh/src/across.cpp:2480-2760: three diagonal phases, ~3n launches per
 // sweep).  Here one launch covers the sweep:
-//   * the loop box is cut into 8 x 8 x 64 tiles (the 64-wide k range aligned to
-//     multiples of 64 of the array index);
+//   * the loop box is cut into 4 x 8 x TK tiles (TK = 32, 16 or 8: the loop
+//     variant), the k ranges aligned to 64 / TK parts of the 64-wide chunks of
+//     the array index; one warp works a tile (no CTA-wide barrier), several
+//     tile-warps share a CTA;
 //   * a tile depends only on its three face predecessors (a-1,b,c), (a,b-1,c),
 //     (a,b,c-1) -- the 7-point stencil touches face neighbours only;
-//   * tiles are handed out by an atomic counter in diagonal order (a topological
-//     order), the grid is no larger than the GPU holds at once, so every tile a
-//     CTA waits for is already owned by a running CTA: progress is guaranteed;
-//   * every wait is bounded: past the limit the CTA writes an error code to the
-//     runtime's status word and returns, the host reports it at the next sync;
-//   * inside a tile, thread (li, lj) owns row (i, j) and at step s updates
+//   * tiles are handed out by an atomic counter plane by plane (a + b + c, a
+//     topological order), the grid is no larger than the GPU holds at once, so
+//     every tile a warp waits for is already owned by a running warp: progress
+//     is guaranteed;
+//   * every wait is bounded: past the limit the warp writes an error code to the
+//     runtime's status word, stops the tile counter and returns; the host
+//     reports it at the next sync;
+//   * a tile stages its own cells and its +1 faces before it waits (no tile
+//     writes them earlier), and the -1 faces once its predecessors are done,
+//     each row with one coalesced load;
+//   * inside a tile, lane (li, lj) owns row (i, j) and at step s updates
 //     k = s - li - lj: cell (i,j,k) sees (i-1,j,k), (i,j-1,k), (i,j,k-1) already
 //     updated and (i+1,j,k), (i,j+1,k), (i,j,k+1) not yet -- exactly the values
 //     the sequential loop order gives it, so every cell is bit-identical.
-// The residual SUM of (nv - old)^2 is kept per row chunk as the pairwise tree
-// over the chunk's 64 positions (the canonical order the reduction engine
-// folds), accumulated in registers as the row advances.
+// The critical path of a sweep is (tiles along i + j + k) x (TK + TI + TJ - 2)
+// steps of a 7-deep FP64 chain; a smaller TK shortens it at the price of idle
+// lanes in the skew.  Only the update runs on the skewed steps: the residual
+// SUM of (nv - old)^2 of a row part (the pairwise tree over its TK positions)
+// is formed after the tile has released its successors, from the saved old
+// values.  Items are laid out (row, chunk, part), so the reduction engine's
+// pairwise fold over items first joins the parts of each 64-position chunk:
+// the result is the canonical chunk tree, then the canonical tree over chunks.
 #include <cuda_runtime.h>
 
 #include <cstdint>
@@ -29,46 +41,81 @@
 
 namespace {
 
-constexpr int TI = 8, TJ = 8, TK = 64;
-constexpr int NT = TI * TJ;              // threads per CTA: one per row of the tile
-constexpr int SI = TI + 2, SJ = TJ + 2, SK = TK + 2;
-constexpr size_t SMEM = sizeof(double) * SI * SJ * SK;
+// one warp works on one 4 x 8 x TK tile: lane (li, lj) owns row (i0+li, j0+lj)
+constexpr int TI = 4, TJ = 8;
+constexpr int WPB = 4;                   // independent tile-warps per CTA
+constexpr int NT = 32 * WPB;
+constexpr int SI = TI + 2, SJ = TJ + 2;
+template <int TK>
+struct Tile {
+    static constexpr int SK = TK + 2;
+    static constexpr int BOX = SI * SJ * SK;     // doubles of one warp's tile + halo
+    static constexpr int OSTR = TK + 1;          // a lane's saved old values (padded: no bank conflicts)
+    static constexpr int WSM = BOX + 32 * OSTR;  // doubles of shared memory per warp
+    static constexpr size_t SMEM = sizeof(double) * WSM * WPB;
+    static constexpr int PARTS = 64 / TK;        // items per 64-wide chunk
+    static constexpr int RPL = 32 / TK;          // rows per warp load
+    static constexpr int LOG = TK == 32 ? 5 : (TK == 16 ? 4 : 3);
+};
 constexpr long SPIN_LIMIT = 1L << 24;    // ~1-4 s of polling before giving up
 constexpr int ERR_SOR_TIMEOUT = 0x50520001;
-constexpr long MAX_DIAGS = 2048;         // a + b diagonals (tile grid up to 1024 x 1024 in i, j)
+constexpr int MAX_PLANES = 1536;         // a + b + c planes of the tile grid
 
 struct Geo {
     long s0, s1;
     long e0, e1, e2;
     long lo0, lo1, lo2, hi0, hi1, hi2;
     long na, nb, nc;  // tiles per axis
-    long kc0;         // first k chunk (lo2 / 64)
+    long kc0;         // first k tile (PARTS * (lo2 / 64): tiles are chunk parts)
     long nj;          // rows per i in the item layout
 };
 
 __device__ __forceinline__ long tileLinear(const Geo &g, long a, long b, long c) { return (a * g.nb + b) * g.nc + c; }
 
-// Tiles are handed out in the order (a + b, then c, then a): a topological
-// order -- (a-1,b,c) and (a,b-1,c) lie on the previous a+b diagonal, (a,b,c-1)
-// earlier on the same one -- that keeps whole 2-D diagonals in flight.
-// pre[s] = number of tiles before diagonal s (shared memory, built per CTA).
-__device__ __forceinline__ long diagLen(long s, long na, long nb) {  // #(a,b), a+b = s
-    long amin = s - (nb - 1) > 0 ? s - (nb - 1) : 0;
-    long amax = s < na - 1 ? s : na - 1;
-    return amax >= amin ? amax - amin + 1 : 0;
+// Tiles are handed out plane by plane, d = a + b + c (a topological order: the
+// three predecessors lie on plane d - 1), inside a plane by c, then a.  So the
+// tiles held at any time are those of the current wavefront, all close to
+// ready.  Plane sizes follow from inclusion-exclusion over the box
+// [0,na) x [0,nb) x [0,nc):
+//   #{x,y,z >= 0 : x+y+z = m} = (m+1)(m+2)/2,  #{... : x+y+z < m} = m(m+1)(m+2)/6.
+__device__ __forceinline__ long long below3(long long m) { return m > 0 ? m * (m + 1) * (m + 2) / 6 : 0; }
+__device__ __forceinline__ int on3(int m) { return m >= 0 ? (m + 1) * (m + 2) / 2 : 0; }
+
+// number of box points with a + b + c < d
+__device__ long long planesBefore(long long d, long long na, long long nb, long long nc) {
+    return below3(d) - below3(d - na) - below3(d - nb) - below3(d - nc) + below3(d - na - nb) + below3(d - na - nc) +
+           below3(d - nb - nc) - below3(d - na - nb - nc);
 }
 
-__device__ void tileAt(const Geo &g, const long *pre, long ns, long idx, long &a, long &b, long &c) {
-    long lo = 0, hi = ns - 1;  // last s with pre[s] <= idx
+// number of points (a, b, c') of plane d with c' < c
+__device__ __forceinline__ int onPlane(int d, int na, int nb, int c) {
+    return on3(d) - on3(d - na) - on3(d - nb) - on3(d - c) + on3(d - na - nb) + on3(d - na - c) + on3(d - nb - c) -
+           on3(d - na - nb - c);
+}
+
+// pre[d] = tiles before plane d (shared, built per CTA); all lanes of a warp call this
+__device__ void tileAt(const Geo &g, const int *pre, int np, long idx, int lane, long &a, long &b, long &c) {
+    int lo = 0, hi = np - 1;  // last plane with pre[d] <= idx
     while (lo < hi) {
-        long mid = (lo + hi + 1) >> 1;
+        int mid = (lo + hi + 1) >> 1;
         if (pre[mid] <= idx) lo = mid;
         else hi = mid - 1;
     }
-    long sd = lo, len = diagLen(sd, g.na, g.nb), rem = idx - pre[sd];
-    c = rem / len;
-    long amin = sd - (g.nb - 1) > 0 ? sd - (g.nb - 1) : 0;
-    a = amin + rem % len;
+    const int d = lo, rem = (int)(idx - pre[d]), na = (int)g.na, nb = (int)g.nb, nc = (int)g.nc;
+    // c = the last c with onPlane(d, c) <= rem, 32 candidates per round
+    int cc = 0;
+    for (int c0 = 0; c0 < nc; c0 += 32) {
+        const int cand = c0 + lane;
+        const bool past = cand >= nc || onPlane(d, na, nb, cand + 1) > rem;
+        const unsigned m = __ballot_sync(0xffffffffu, past);
+        if (m) {
+            cc = c0 + __ffs(m) - 1;
+            break;
+        }
+    }
+    c = cc;
+    const long sd = d - cc, amin = sd - (g.nb - 1) > 0 ? sd - (g.nb - 1) : 0;
+    a = amin + (rem - onPlane(d, na, nb, cc));
     b = sd - a;
 }
 
@@ -81,121 +128,167 @@ __device__ __forceinline__ void stRelease(int *p, int v) {
     asm volatile("st.release.gpu.global.b32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
 }
 
+__device__ __forceinline__ double ldCell(const double *A, const Geo &g, long i, long j, long k) {
+    return (i >= 0 && i < g.e0 && j >= 0 && j < g.e1 && k >= 0 && k < g.e2) ? __ldcg(A + i * g.s0 + j * g.s1 + k)
+                                                                             : 0.0;
+}
+
+// Box rows (qi, qj) are TK + 2 doubles along k; a warp load brings the TK
+// interior ones (k = kb + lane % TK) of 32 / TK rows, the k faces take one load
+// per lane.  Before the wait: the own rows and the +i / +j face rows (qi, qj >=
+// 1), and the +k face of the own rows -- no tile writes them before this one
+// is done.
+template <int TK>
+__device__ __forceinline__ void stageOwn(double *box, const double *A, const Geo &g, long i0, long j0, long kb,
+                                         int lane) {
+    using T = Tile<TK>;
+    constexpr int NR = (SI - 1) * (SJ - 1), NL = (NR + T::RPL - 1) / T::RPL;
+    const int sub = lane / TK, kk = lane % TK;
+    double v[NL];
+#pragma unroll
+    for (int u = 0; u < NL; u++) {
+        const int r = u * T::RPL + sub, qi = 1 + r / (SJ - 1), qj = 1 + r % (SJ - 1);
+        v[u] = r < NR ? ldCell(A, g, i0 - 1 + qi, j0 - 1 + qj, kb + kk) : 0.0;
+    }
+    const int li = lane / TJ, lj = lane % TJ;
+    const double kf = ldCell(A, g, i0 + li, j0 + lj, kb + TK);
+#pragma unroll
+    for (int u = 0; u < NL; u++) {
+        const int r = u * T::RPL + sub, qi = 1 + r / (SJ - 1), qj = 1 + r % (SJ - 1);
+        if (r < NR) box[(qi * SJ + qj) * T::SK + 1 + kk] = v[u];
+    }
+    box[((li + 1) * SJ + lj + 1) * T::SK + T::SK - 1] = kf;
+}
+
+// After the wait: the -i, -j and -k faces, written by the predecessors.
+template <int TK>
+__device__ __forceinline__ void stageFaces(double *box, const double *A, const Geo &g, long i0, long j0, long kb,
+                                           int lane) {
+    using T = Tile<TK>;
+    constexpr int NR = TJ + TI, NL = (NR + T::RPL - 1) / T::RPL;  // rows (0, 1..TJ), then (1..TI, 0)
+    const int sub = lane / TK, kk = lane % TK;
+    double v[NL];
+#pragma unroll
+    for (int u = 0; u < NL; u++) {
+        const int r = u * T::RPL + sub, qi = r < TJ ? 0 : r - TJ + 1, qj = r < TJ ? r + 1 : 0;
+        v[u] = r < NR ? ldCell(A, g, i0 - 1 + qi, j0 - 1 + qj, kb + kk) : 0.0;
+    }
+    const int li = lane / TJ, lj = lane % TJ;
+    const double kf = ldCell(A, g, i0 + li, j0 + lj, kb - 1);
+#pragma unroll
+    for (int u = 0; u < NL; u++) {
+        const int r = u * T::RPL + sub, qi = r < TJ ? 0 : r - TJ + 1, qj = r < TJ ? r + 1 : 0;
+        if (r < NR) box[(qi * SJ + qj) * T::SK + 1 + kk] = v[u];
+    }
+    box[((li + 1) * SJ + lj + 1) * T::SK] = kf;
+}
+
+template <int TK>
 __global__ void __launch_bounds__(NT) kSorWave(double *A, Geo g, const double *wPtr, int *done, unsigned *counter,
                                                double *items, int *status) {
-    extern __shared__ double sm[];  // [SI][SJ][SK], then pre[ns + 1]
-    __shared__ long sIdx;
-    __shared__ int sFail;
-    const int tid = threadIdx.x, li = tid / TJ, lj = tid % TJ;
+    using T = Tile<TK>;
+    constexpr int SK = T::SK;
+    extern __shared__ double sm[];  // per warp: box [SI][SJ][SK] + olds [32][OSTR]; then pre[np + 1]
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, li = lane / TJ, lj = lane % TJ;
     const long ntiles = g.na * g.nb * g.nc;
-    const long ns = g.na + g.nb - 1;
-    long *pre = (long *)(sm + SI * SJ * SK);
-    if (tid == 0) {
-        long acc = 0;
-        for (long sd = 0; sd < ns; sd++) {
-            pre[sd] = acc;
-            acc += diagLen(sd, g.na, g.nb) * g.nc;
-        }
-        pre[ns] = acc;
-    }
-    __syncthreads();
+    const int np = (int)(g.na + g.nb + g.nc - 2);
+    int *pre = (int *)(sm + (size_t)T::WSM * WPB);
+    for (int d = threadIdx.x; d <= np; d += NT) pre[d] = (int)planesBefore(d, g.na, g.nb, g.nc);
+    __syncthreads();  // the only CTA-wide barrier: from here every warp runs on its own
+    double *box = sm + (size_t)T::WSM * warp;
+    double *olds = box + T::BOX + lane * T::OSTR;
     const double w = *wPtr;
     const double c1 = 1.0 - w, c2 = w / 6.0;  // loop invariants, rounded as in the source expression
     const long nck = g.nc;
     while (true) {
-        if (tid == 0) {
-            sIdx = (long)atomicAdd(counter, 1u);
-            sFail = 0;
-        }
-        __syncthreads();
-        const long idx = sIdx;
+        long idx = 0;
+        if (lane == 0) idx = (long)atomicAdd(counter, 1u);  // >= 2^31 once a warp has failed
+        idx = __shfl_sync(0xffffffffu, idx, 0);
         if (idx >= ntiles) break;
         long a, b, c;
-        tileAt(g, pre, ns, idx, a, b, c);
-        // wait for the face predecessors (bounded)
-        if (tid < 3) {
-            long pa = a - (tid == 0), pb = b - (tid == 1), pc = c - (tid == 2);
+        tileAt(g, pre, np, idx, lane, a, b, c);
+        const long i0 = g.lo0 + a * TI, j0 = g.lo1 + b * TJ, kb = (g.kc0 + c) * TK;
+        // 1. own cells and the +1 faces: nobody writes them before this tile is done
+        stageOwn<TK>(box, A, g, i0, j0, kb, lane);
+        // 2. wait for the face predecessors (bounded)
+        int fail = 0;
+        if (lane < 3) {
+            long pa = a - (lane == 0), pb = b - (lane == 1), pc = c - (lane == 2);
             if (pa >= 0 && pb >= 0 && pc >= 0) {
                 const int *f = done + tileLinear(g, pa, pb, pc);
                 long n = 0;
                 while (ldAcquire(f) == 0) {
                     if (++n > SPIN_LIMIT) {
                         atomicExch(status, ERR_SOR_TIMEOUT);
-                        sFail = 1;
+                        atomicOr(counter, 0x80000000u);  // no warp takes another tile
+                        fail = 1;
                         break;
                     }
                     __nanosleep(64);
                 }
             }
         }
-        __syncthreads();
-        if (sFail) return;
-        const long i0 = g.lo0 + a * TI, j0 = g.lo1 + b * TJ, kb = (g.kc0 + c) * TK;
-        // stage tile + halo (reads through L2: producers are other SMs)
-        for (int q = tid; q < SI * SJ * SK; q += NT) {
-            int qk = q % SK, qj = (q / SK) % SJ, qi = q / (SK * SJ);
-            long i = i0 - 1 + qi, j = j0 - 1 + qj, k = kb - 1 + qk;
-            double v = 0.0;
-            if (i >= 0 && i < g.e0 && j >= 0 && j < g.e1 && k >= 0 && k < g.e2) v = __ldcg(A + i * g.s0 + j * g.s1 + k);
-            sm[q] = v;
-        }
-        __syncthreads();
+        if (__any_sync(0xffffffffu, fail)) return;
+        __syncwarp();  // orders the acquiring lanes' loads before every lane's face loads
+        // 3. the -1 faces, written by the predecessors (through L2)
+        stageFaces<TK>(box, A, g, i0, j0, kb, lane);
+        __syncwarp();
         const long i = i0 + li, j = j0 + lj;
         const bool row = i <= g.hi0 && j <= g.hi1;
-        double p0 = 0, p1 = 0, p2 = 0, p3 = 0, p4 = 0, p5 = 0, root = -0.0;  // pairwise-tree stack
-        double *cen = sm + ((li + 1) * SJ + (lj + 1)) * SK + 1;              // k = kb at cen[0]
-        for (int s = 0; s < TK + TI + TJ - 2; s++) {
-            const int p = s - li - lj;
-            if (row && p >= 0 && p < TK) {
-                const long k = kb + p;
-                double term = -0.0;  // identity of positions outside the loop
-                if (k >= g.lo2 && k <= g.hi2) {
-                    double *x = cen + p;
-                    double old = x[0];
-                    // A[i-1] + A[i+1] + A[j-1] + A[j+1] + A[k-1] + A[k+1], left to right
-                    double sum = ((((x[-SJ * SK] + x[SJ * SK]) + x[-SK]) + x[SK]) + x[-1]) + x[1];
-                    double nv = c1 * old + c2 * sum;
-                    x[0] = nv;
-                    double dlt = nv - old;
-                    term = dlt * dlt;
-                }
-                // pairwise tree over positions 0..63 of the chunk, in order
-                double v = term;
-                if (p & 1) {
-                    v = p0 + v;
-                    if (p & 2) {
-                        v = p1 + v;
-                        if (p & 4) {
-                            v = p2 + v;
-                            if (p & 8) {
-                                v = p3 + v;
-                                if (p & 16) {
-                                    v = p4 + v;
-                                    if (p & 32) root = p5 + v;
-                                    else p5 = v;
-                                } else p4 = v;
-                            } else p3 = v;
-                        } else p2 = v;
-                    } else p1 = v;
-                } else p0 = v;
+        double *cen = box + ((li + 1) * SJ + (lj + 1)) * SK + 1;  // k = kb at cen[0]
+        // the dependent chain: only the update itself runs on the skewed steps
+        for (int st = 0; st < TK + TI + TJ - 2; st++) {
+            const int p = st - li - lj;
+            const long k = kb + p;
+            if (row && p >= 0 && p < TK && k >= g.lo2 && k <= g.hi2) {
+                double *x = cen + p;
+                double old = x[0];
+                // A[i-1] + A[i+1] + A[j-1] + A[j+1] + A[k-1] + A[k+1], left to right
+                double sum = ((((x[-SJ * SK] + x[SJ * SK]) + x[-SK]) + x[SK]) + x[-1]) + x[1];
+                x[0] = c1 * old + c2 * sum;
+                olds[p] = old;
             }
-            __syncthreads();
+            __syncwarp();
         }
         // write the tile's updated cells (coalesced along k)
-        for (int q = tid; q < TI * TJ * TK; q += NT) {
+        for (int q = lane; q < TI * TJ * TK; q += 32) {
             int qk = q % TK, qj = (q / TK) % TJ, qi = q / (TK * TJ);
             long ii = i0 + qi, jj = j0 + qj, k = kb + qk;
             if (ii <= g.hi0 && jj <= g.hi1 && k >= g.lo2 && k <= g.hi2)
-                A[ii * g.s0 + jj * g.s1 + k] = sm[((qi + 1) * SJ + (qj + 1)) * SK + qk + 1];
+                A[ii * g.s0 + jj * g.s1 + k] = box[((qi + 1) * SJ + (qj + 1)) * SK + qk + 1];
+        }
+        __threadfence();
+        __syncwarp();
+        if (lane == 0) stRelease(done + tileLinear(g, a, b, c), 1);
+        // the residual, off the chain: successors already run.  Every lane is at
+        // the same position p, so the pairwise tree over the TK positions of the
+        // row part takes warp-uniform branches.
+        double stk[T::LOG], root = -0.0;
+#pragma unroll
+        for (int p = 0; p < TK; p++) {
+            const long k = kb + p;
+            double v = -0.0;  // identity of positions outside the loop
+            if (row && k >= g.lo2 && k <= g.hi2) {
+                double dlt = cen[p] - olds[p];
+                v = dlt * dlt;
+            }
+            // pairwise: position p closes the subtrees of its trailing one bits
+#pragma unroll
+            for (int l = 0; l < T::LOG; l++) {
+                if (!((p >> l) & 1)) {
+                    stk[l] = v;
+                    break;
+                }
+                v = stk[l] + v;
+            }
+            if (p == TK - 1) root = v;
         }
         if (row) items[((i - g.lo0) * g.nj + (j - g.lo1)) * nck + c] = root;
-        __threadfence();
-        __syncthreads();
-        if (tid == 0) stRelease(done + tileLinear(g, a, b, c), 1);
+        __syncwarp();  // the box and olds are reused by this warp's next tile
     }
 }
 
-bool geo(const long st[3], const long ext[3], const long lo[3], const long hi[3], Geo &g) {
+bool geo(const long st[3], const long ext[3], const long lo[3], const long hi[3], int parts, Geo &g) {
     if (hi[0] < lo[0] || hi[1] < lo[1] || hi[2] < lo[2] || lo[2] < 0 || st[2] != 1) return false;
     g.s0 = st[0];
     g.s1 = st[1];
@@ -210,51 +303,69 @@ bool geo(const long st[3], const long ext[3], const long lo[3], const long hi[3]
     g.hi2 = hi[2];
     g.na = (hi[0] - lo[0] + TI) / TI;
     g.nb = (hi[1] - lo[1] + TJ) / TJ;
-    g.kc0 = lo[2] / TK;
-    g.nc = hi[2] / TK - g.kc0 + 1;
+    g.kc0 = parts * (lo[2] / 64);
+    g.nc = parts * (hi[2] / 64 - lo[2] / 64 + 1);
     g.nj = hi[1] - lo[1] + 1;
     return true;
 }
 
-}  // namespace
+// variant -> TK: 0 -> 32, 1 -> 16, 2 -> 8
+int tkOf(int variant) { return variant == 0 ? 32 : (variant == 1 ? 16 : (variant == 2 ? 8 : 0)); }
 
-extern "C" {
-
-long dvmhgb_sor3d_items(const long lo[3], const long hi[3]) {
-    return (hi[0] - lo[0] + 1) * (hi[1] - lo[1] + 1) * (hi[2] / TK - lo[2] / TK + 1);
-}
-
-long dvmhgb_sor3d_scratch_bytes(const long lo[3], const long hi[3]) {
-    long ntiles = ((hi[0] - lo[0] + TI) / TI) * ((hi[1] - lo[1] + TJ) / TJ) * (hi[2] / TK - lo[2] / TK + 1);
-    return (ntiles + 64) * (long)sizeof(int);
-}
-
-int dvmhgb_sor3d_sweep(double *A, const long st[3], const long ext[3], const long lo[3], const long hi[3],
-                       const double *wDev, double *items, void *scratch, int *status, void *stream) {
-    Geo g;
-    if (!A || !wDev || !items || !scratch || !status || !geo(st, ext, lo, hi, g)) return -1;
-    cudaStream_t s = (cudaStream_t)stream;
-    long ntiles = g.na * g.nb * g.nc;
+template <int TK>
+int sweepT(double *A, const Geo &g, const double *wDev, double *items, void *scratch, int *status, cudaStream_t s) {
+    using T = Tile<TK>;
+    const long ntiles = g.na * g.nb * g.nc;
     unsigned *counter = (unsigned *)scratch;
     int *done = (int *)scratch + 64;  // counter on its own 256-byte line
-    const long ns = g.na + g.nb - 1;
-    if (ns > MAX_DIAGS) return -1;
-    const size_t smem = SMEM + sizeof(long) * (MAX_DIAGS + 1);
+    if (g.na + g.nb + g.nc - 2 > MAX_PLANES || ntiles >= (1L << 30)) return -1;
+    const size_t smem = T::SMEM + sizeof(int) * (MAX_PLANES + 1);  // one size for every launch (occupancy cached)
     if (cudaMemsetAsync(scratch, 0, (size_t)(ntiles + 64) * sizeof(int), s) != cudaSuccess) return -1;
     static int occ = 0, sms = 0;
     if (!occ) {
-        cudaFuncSetAttribute(kSorWave, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kSorWave, NT, smem);
+        cudaFuncSetAttribute(kSorWave<TK>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kSorWave<TK>, NT, smem);
         int dev = 0;
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
         if (occ < 1) occ = 1;
     }
     long grid = (long)occ * sms;  // all CTAs resident at once: waits always resolve
-    if (grid > ntiles) grid = ntiles;
-    kSorWave<<<(unsigned)grid, NT, smem, s>>>(A, g, wDev, done, counter, items, status);
+    long gridCap = (ntiles + WPB - 1) / WPB;
+    if (grid > gridCap) grid = gridCap;
+    kSorWave<TK><<<(unsigned)grid, NT, smem, s>>>(A, g, wDev, done, counter, items, status);
     dvmhgb_count_launches(1);
     return cudaGetLastError() == cudaSuccess ? 0 : -1;
+}
+
+}  // namespace
+
+extern "C" {
+
+long dvmhgb_sor3d_items(const long lo[3], const long hi[3], int variant) {
+    const int tk = tkOf(variant);
+    if (!tk) return -1;
+    return (hi[0] - lo[0] + 1) * (hi[1] - lo[1] + 1) * (64 / tk) * (hi[2] / 64 - lo[2] / 64 + 1);
+}
+
+long dvmhgb_sor3d_scratch_bytes(const long lo[3], const long hi[3], int variant) {
+    const int tk = tkOf(variant);
+    if (!tk) return -1;
+    long ntiles = ((hi[0] - lo[0] + TI) / TI) * ((hi[1] - lo[1] + TJ) / TJ) * (64 / tk) * (hi[2] / 64 - lo[2] / 64 + 1);
+    return (ntiles + 64) * (long)sizeof(int);
+}
+
+int dvmhgb_sor3d_sweep(double *A, const long st[3], const long ext[3], const long lo[3], const long hi[3],
+                       const double *wDev, double *items, void *scratch, int *status, int variant, void *stream) {
+    const int tk = tkOf(variant);
+    Geo g;
+    if (!tk || !A || !wDev || !items || !scratch || !status || !geo(st, ext, lo, hi, 64 / tk, g)) return -1;
+    cudaStream_t s = (cudaStream_t)stream;
+    switch (tk) {
+        case 32: return sweepT<32>(A, g, wDev, items, scratch, status, s);
+        case 16: return sweepT<16>(A, g, wDev, items, scratch, status, s);
+        default: return sweepT<8>(A, g, wDev, items, scratch, status, s);
+    }
 }
 
 }  // extern "C"

@@ -345,6 +345,9 @@ static void runQueued(const std::vector<Loop *> &q) {
 
 // ---------------------------------------------------------------- batched mode: flush
 
+// DVMH_GB_VARIANT / dvmhgb_force_variant: the value every variant query returns (-1: none)
+static int forcedVariant = getenv("DVMH_GB_VARIANT") ? atoi(getenv("DVMH_GB_VARIANT")) : -1;
+
 static void sigAdd(std::vector<uint64_t> &s, uint64_t v) { s.push_back(v); }
 
 static std::vector<uint64_t> signature(const std::vector<Loop *> &q) {
@@ -382,6 +385,7 @@ static std::vector<uint64_t> signature(const std::vector<Loop *> &q) {
         }
     }
     sigAdd(s, (uint64_t)settings.fuse);
+    sigAdd(s, (uint64_t)(int64_t)forcedVariant);  // a forced variant is captured anew
     return s;
 }
 
@@ -943,10 +947,12 @@ void dvmhgb_register_batch(DvmHandlerFunc single, DvmHandlerFunc batched) {
     batchRules[(void *)single] = batched;
 }
 
+void dvmhgb_force_variant(int v) { forcedVariant = v < 0 ? -1 : v; }
+
 int dvmhgb_loop_variant(DvmType loopRef, int nvariants, int dflt) {
     SpecLoop *s = specOf(loopRef, "dvmhgb_loop_variant");
     GB_CHECK(nvariants >= 1 && dflt >= 0 && dflt < nvariants, "invalid variant request");
-    static int forced = getenv("DVMH_GB_VARIANT") ? atoi(getenv("DVMH_GB_VARIANT")) : -1;
+    const int forced = forcedVariant;
     int v = s->variant >= 0 ? s->variant : dflt;
     // online tuning explores only in immediate execution (a captured graph keeps its choice)
     if (settings.tuneMode && !ctx.capturing) v = tunerVariant(s->loop, nvariants, dflt, false);

@@ -104,6 +104,11 @@ def set_mode(mode):
     init().dvmhgb_set_mode(MODES[mode] if isinstance(mode, str) else int(mode))
 
 
+def force_variant(v):
+    """Every loop variant query returns v from now on (v < 0: tuning / defaults again)."""
+    init().dvmhgb_force_variant(int(v))
+
+
 def sync():
     init().dvmhgb_sync()
 

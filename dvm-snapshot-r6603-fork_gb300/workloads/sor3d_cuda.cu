@@ -12,6 +12,8 @@
 #include "dvmh_gb.h"
 #include "dvmh_gb_kernels.h"
 
+#define SOR_DEFAULT_VARIANT 1
+
 extern "C" void loop_sor3d_cuda(DvmType *pLoopRef, DvmType A_hdr[], double *s_ptr, double *w_ptr) {
     (void)s_ptr;
     DvmType loop_ref = *pLoopRef;
@@ -40,9 +42,11 @@ extern "C" void loop_sor3d_cuda(DvmType *pLoopRef, DvmType A_hdr[], double *s_pt
     double s, *s_grid = 0;
     dvmh_loop_cuda_register_red_C(loop_ref, 1, (void **)&s_grid, 0);
     dvmh_loop_red_init_C(loop_ref, 1, &s, 0);
-    dvmh_loop_cuda_red_prepare_C(loop_ref, 1, dvmhgb_sor3d_items(lo, hi), 0);
-    void *scratch = dvmhgb_loop_scratch(loop_ref, dvmhgb_sor3d_scratch_bytes(lo, hi));
-    if (dvmhgb_sor3d_sweep(A, st, ext, lo, hi, w_dev, s_grid, scratch, dvmhgb_status_word(), stream) != 0) {
+    // tile depth along k (32, 16, 8): chosen by the runtime's variant tuner
+    const int variant = dvmhgb_loop_variant(loop_ref, DVMHGB_SOR3D_VARIANTS, SOR_DEFAULT_VARIANT);
+    dvmh_loop_cuda_red_prepare_C(loop_ref, 1, dvmhgb_sor3d_items(lo, hi, variant), 0);
+    void *scratch = dvmhgb_loop_scratch(loop_ref, dvmhgb_sor3d_scratch_bytes(lo, hi, variant));
+    if (dvmhgb_sor3d_sweep(A, st, ext, lo, hi, w_dev, s_grid, scratch, dvmhgb_status_word(), variant, stream) != 0) {
         fprintf(stderr, "loop_sor3d_cuda: kernel launch rejected its arguments\n");
         exit(1);
     }

@@ -64,6 +64,9 @@ int *dvmhgb_status_word(void);
  * chooses it with the CUDA block; `dflt` applies when tuning is off.
  * Environment DVMH_GB_VARIANT forces a value. */
 int dvmhgb_loop_variant(DvmType loopRef, int nvariants, int dflt);
+/* Force every later dvmhgb_loop_variant() to return v (clamped to the loop's
+ * variant count); v < 0 restores tuning / defaults.  Overrides DVMH_GB_VARIANT. */
+void dvmhgb_force_variant(int v);
 
 /* Self-test of the integer-pipe FP64 operations against the FP64 unit on n
  * random operand pairs: mismatches[0..3] = add, sub, mul, division by 6. */

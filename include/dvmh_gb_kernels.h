@@ -51,14 +51,16 @@ int dvmhgb_jac2d_fused(double *A, const double *B, double *Bnew, const long st[2
                        const long lo[2], const long hi[2], double *items, int native, void *stream);
 
 /* ---- SOR 3-D ACROSS (1:1,1:1,1:1), FP64: one sweep as a persistent tiled
- * wavefront; items = canonical partials of SUM (nv-old)^2, one per row and
- * 32-wide half of each 64-wide chunk (row, chunk, half order);
- * wDev = device address of omega; scratch = dvmhgb_sor3d_scratch_bytes() bytes;
- * status = dvmhgb_status_word() ---- */
-long dvmhgb_sor3d_items(const long lo[3], const long hi[3]);
-long dvmhgb_sor3d_scratch_bytes(const long lo[3], const long hi[3]);
+ * wavefront of 4 x 8 x TK tiles, TK = 32, 16, 8 for variant 0, 1, 2;
+ * items = canonical partials of SUM (nv-old)^2, one per row and TK-wide part
+ * of each 64-wide chunk (row, chunk, part order); wDev = device address of
+ * omega; scratch = dvmhgb_sor3d_scratch_bytes() bytes; status =
+ * dvmhgb_status_word().  -1 for an unknown variant or invalid arguments ---- */
+#define DVMHGB_SOR3D_VARIANTS 3
+long dvmhgb_sor3d_items(const long lo[3], const long hi[3], int variant);
+long dvmhgb_sor3d_scratch_bytes(const long lo[3], const long hi[3], int variant);
 int dvmhgb_sor3d_sweep(double *A, const long st[3], const long ext[3], const long lo[3], const long hi[3],
-                       const double *wDev, double *items, void *scratch, int *status, void *stream);
+                       const double *wDev, double *items, void *scratch, int *status, int variant, void *stream);
 
 /* ---- explicit 2-D heat step, FP64 (workloads/heat.c), with SUM and MINLOC:
  * per (row, 64-wide chunk) unit one SUM item (canonical pairwise tree), one

@@ -22,7 +22,14 @@ def g():
     _, g = ge.package()
     g.init()
     yield g
+    g.force_variant(-1)
     g.set_mode("batched")
+
+
+@pytest.fixture(autouse=True)
+def _no_forced_variant(g):
+    yield
+    g.force_variant(-1)
 
 
 def close_sum(a, b, n):
@@ -32,9 +39,11 @@ def close_sum(a, b, n):
     return np.all(np.abs(a - b) <= 2 * gamma * np.abs(b) + 1e-300)
 
 
+@pytest.mark.parametrize("variant", [0, 1, 2])
 @pytest.mark.parametrize("mode", MODES)
-def test_sor_golden(g, golden, mode):
+def test_sor_golden(g, golden, mode, variant):
     g.set_mode(mode)
+    g.force_variant(variant)  # tile depth along k: 32, 16, 8
     for name, c in golden.items():
         if c["prog"] != "sor3d":
             continue
@@ -49,9 +58,11 @@ def test_sor_golden(g, golden, mode):
         assert close_sum(res, unhex(c["s"]), (n - 2) ** 3), name
 
 
-@pytest.mark.parametrize("n", [4, 9, 17, 66, 75])
-def test_sor_sizes_vs_oracle(g, n):
+@pytest.mark.parametrize("variant", [0, 1, 2])
+@pytest.mark.parametrize("n", [4, 9, 17, 66, 75, 131])
+def test_sor_sizes_vs_oracle(g, n, variant):
     seq, canon, A_ref = orc.sor_run(n, 3, 1.5, 77 + n)
+    g.force_variant(variant)
     for mode in ("plain", "batched"):
         g.set_mode(mode)
         s = g.Sor(n, 1.5, 77 + n)
