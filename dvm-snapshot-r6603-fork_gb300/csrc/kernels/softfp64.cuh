@@ -305,6 +305,41 @@ SF_HD double scale_down_fast(double x, int k, bool &special) {
     return from(zero ? X : X - ((uint64_t)k << 52));
 }
 
+// ---------------------------------------------------------------- non-negative operands
+//
+// add_pos(x, y) = RN(x + y) for x, y each +0 or a positive normal double below
+// 2^1022 ("pos_ok" below) -- the caller checks its inputs once (a tile of a
+// stencil whose values are all non-negative), so the addition needs no sign,
+// cancellation, subnormal or overflow handling: align the smaller significand
+// with a sticky bit, add, renormalise by at most one bit, round to nearest
+// even, repack (the significand's hidden bit carries into the exponent field,
+// which also covers a rounding overflow to the next binade).  The sum of two
+// pos_ok values is pos_ok again or 2^1022 <= s < 2^1023 (normal), so chains of
+// additions stay exact as long as the partial sums stay below 2^1022.
+SF_HD bool pos_ok(double x) {
+    uint32_t h = hi32(bits(x));
+    return (h >> 20) - 1 < 0x7FDu || bits(x) == 0;  // exponent 1..0x7FD and sign clear, or +0
+}
+
+SF_HD double add_pos(double a, double b) {
+    uint64_t A = bits(a), B = bits(b);
+    bool ab = A >= B;                          // integer order = value order here
+    uint64_t X = ab ? A : B, Y = ab ? B : A;   // X >= Y
+    uint32_t ex = hi32(X) >> 20, ey = hi32(Y) >> 20;
+    uint32_t d = ex - ey;
+    bool far = (ey == 0) | (d >= 54);          // y = 0, or y < ulp(x) / 2: RN(x + y) = x
+    uint32_t dd = far ? 0 : d;
+    uint64_t mx = ((X & MANT) | HID) << 10, my = ((Y & MANT) | HID) << 10;
+    uint64_t lost = dd ? my << (64 - dd) : 0;  // the bits shifted out (sticky)
+    uint64_t s = mx + ((my >> dd) | (uint64_t)(lost != 0));
+    uint32_t carry = (uint32_t)(s >> 63);
+    s = carry ? ((s >> 1) | (s & 1)) : s;      // top bit at 62, sticky kept in bit 0
+    uint32_t g = (uint32_t)s & 0x7FF;          // bit 10: result lsb, bits 9..0: rounding bits
+    uint64_t m = (s >> 10) + (uint64_t)(((g & 0x3FF) > 0x200) | (((g & 0x3FF) == 0x200) & (g >> 10)));
+    uint64_t r = ((uint64_t)(ex + carry - 1) << 52) + m;
+    return from(far ? X : r);
+}
+
 // Max(|t|, m) on bit patterns: for non-negative doubles the IEEE order is the
 // unsigned integer order.  A NaN t leaves m unchanged, as (t > m ? t : m) does.
 SF_HD uint64_t absmax_bits(double t, uint64_t m) {

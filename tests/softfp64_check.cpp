@@ -51,3 +51,45 @@ extern "C" void softfp64_check(long n, uint64_t seed, long bad[4]) {
         bad[3] += !same(sf::div3p2(a, 1), a / six);
     }
 }
+
+// add_pos over pos_ok operands: exponent gaps 0..60 (beyond the far limit),
+// zeros, half-way patterns, carries into the next binade, values near 2^1022.
+static void posPair(uint64_t seed, uint64_t i, double &a, double &b) {
+    uint64_t r0 = mix(seed + 4 * i + 1), r1 = mix(seed + 4 * i + 2), r2 = mix(seed + 4 * i + 3);
+    uint64_t ea = 1 + (r2 & 0x3FF) % 0x7FC, gap = (r2 >> 12) % 61;
+    uint64_t eb = ea > gap ? ea - gap : 1;
+    uint64_t A = (ea << 52) | (r0 & sf::MANT), B = (eb << 52) | (r1 & sf::MANT);
+    switch ((r2 >> 20) & 7) {
+        case 0: B = 0; break;                                            // x + 0
+        case 1: B = (eb << 52) | (r1 & 0x000FFFFFFFF00000ull); break;   // few low bits: exact or tie
+        case 2: A |= 0x000FFFFFFFFFFFF0ull; break;                       // carry out of the significand
+        case 3: B = (eb << 52) | (1ull << ((r2 >> 24) % 52)); break;     // single bit: half-way cases
+        case 4: A = (0x7FDull << 52) | (r0 & sf::MANT); B = (0x7FDull << 52) | (r1 & sf::MANT); break;
+        case 5: A = sf::bits((double)(r0 >> 11) * (1.0 / 9007199254740992.0)); B = sf::bits((double)(r1 >> 11) * (1.0 / 9007199254740992.0)); break;
+        default: break;
+    }
+    a = sf::from(A);
+    b = sf::from(B);
+    if ((r2 >> 40) & 1) { double t = a; a = b; b = t; }
+}
+
+extern "C" long softfp64_check_pos(long n, uint64_t seed) {
+    long bad = 0;
+    for (long i = 0; i < n; i++) {
+        double a, b;
+        posPair(seed, (uint64_t)i, a, b);
+        if (!sf::pos_ok(a) || !sf::pos_ok(b)) { bad++; continue; }
+        bad += !same(sf::add_pos(a, b), a + b);
+    }
+    // chains of additions of [0,1) values: the stencil's use
+    for (long i = 0; i < n / 16; i++) {
+        double s = 0.0, t = 0.0;
+        for (int q = 0; q < 6; q++) {
+            double v = (double)(mix(seed ^ (uint64_t)(i * 8 + q)) >> 11) * (1.0 / 9007199254740992.0);
+            s = sf::add_pos(s, v);
+            t = t + v;
+        }
+        bad += !same(s, t);
+    }
+    return bad;
+}

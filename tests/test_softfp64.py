@@ -27,6 +27,14 @@ def test_softfp64_matches_host_fpu(hostlib, seed):
     assert list(bad) == [0, 0, 0, 0], "mismatches add/sub/mul/div6: %s" % list(bad)
 
 
+@pytest.mark.parametrize("seed", [3, 20261204])
+def test_add_pos_matches_host_fpu(hostlib, seed):
+    """The non-negative-operand addition of the stencil kernels, on its whole domain."""
+    hostlib.softfp64_check_pos.restype = ctypes.c_long
+    hostlib.softfp64_check_pos.argtypes = [ctypes.c_long, ctypes.c_uint64]
+    assert hostlib.softfp64_check_pos(4_000_000, seed) == 0
+
+
 @pytest.mark.gpu
 def test_softfp64_matches_gb300_fp64_unit():
     import __graft_entry__ as ge
