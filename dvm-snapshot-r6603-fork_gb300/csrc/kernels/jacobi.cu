@@ -154,9 +154,6 @@ UpdGeom updGeom(long ni, long nj, long lo2, long hi2) {
 
 constexpr int TX = 32;  // lanes: element pairs along k (64 elements)
 constexpr int TY = 8;   // warps: rows along j
-// rows per thread: 2 for the stencil loop, 1 for the fused loops (register budget)
-constexpr int JT_PLAIN = 2, JT_FUSED = 1;
-constexpr int SW = 66;  // shared row: k = kb-1 .. kb+64
 
 struct Box3 {
     long s0, s1;
@@ -211,154 +208,226 @@ __device__ __forceinline__ double stencil5(double a, double b, double c, double 
     return sf::scale_down_fast(t, 2, spc);
 }
 
-template <bool FUSED, int NATIVE, int JT>
-__global__ void __launch_bounds__(TX *TY, (JT > 1 && FUSED) ? 2 : 3) kStencil3(double *A, const double *B, double *Out, Box3 b, long p0,
-                                                     int ichunk, double *items) {
+// (((((a + b) + c) + d) + e) + f) / 6.0 for a tile whose inputs were all
+// checked pos_ok: the first 5 - N additions on the integer pipe (sf::add_pos),
+// the others on the FP64 unit, the division on the integer pipe.
+template <int N>
+__device__ __forceinline__ double stencil7pos(double a, double b, double c, double d, double e, double f, bool &spc) {
+    double t = N > 4 ? sf::nadd(a, b) : sf::add_pos(a, b);
+    t = N > 3 ? sf::nadd(t, c) : sf::add_pos(t, c);
+    t = N > 2 ? sf::nadd(t, d) : sf::add_pos(t, d);
+    t = N > 1 ? sf::nadd(t, e) : sf::add_pos(t, e);
+    t = N > 0 ? sf::nadd(t, f) : sf::add_pos(t, f);
+    return sf::div3p2_fast(t, 1, spc);
+}
+
+// The 3-D stencil loop (FUSED = false: Out = (6 neighbours of A) / 6) or the
+// update and stencil loops fused (FUSED = true: eps = Max(|B - A|, eps); A = B
+// over the box, then Out = (6 neighbours of A_new) / 6, A_new = B inside the
+// box and A outside it).
+//
+// A CTA of TY warps covers 64 elements of k (lane l owns the pair k = kb + 2l,
+// k + 1) and TJ = TY * JT rows of j (warp ty owns rows ty*JT .. ty*JT + JT-1),
+// and streams the planes i of its chunk.  Per thread, the own pairs of planes
+// i-1, i, i+1 are in registers and plane i+2 is in flight; plane i's rows are
+// also in shared memory (two buffers, one barrier per plane) for the j
+// neighbours owned by the next / previous warp; k neighbours come by shuffles,
+// the chunk's edge columns kb-1 / kb+64 are loaded by lanes 0 / 31.  Every
+// source element is read from HBM once.
+//
+// FP64 work per cell: the five additions (5 - NATIVE of them on the integer
+// pipe once the CTA has seen only pos_ok inputs).  The division by 6 and, in
+// the fused loop, the MAX of |B - A| run on the integer pipe: |B - A| of two
+// values in [2^-12, 1) is exact as 64-bit fixed point (value * 2^64), its
+// maximum is rounded once at the end -- RN is monotone and odd, so
+// RN(max |b - a|) = max |RN(b - a)|.  Values outside that range take the FP64
+// unit (a warp-uniform branch).
+template <bool FUSED, int NATIVE, int JT, int MINB>
+__global__ void __launch_bounds__(TX *TY, MINB) kStencil3(double *A, const double *B, double *Out, Box3 b,
+                                                                   long p0, int ichunk, double *items) {
     constexpr int TJ = TY * JT;
-    __shared__ double sm[TJ + 2][SW];
-    __shared__ double shr[TX * TY / 32];
+    __shared__ double2 sm[2][TJ + 2][TX];
+    __shared__ double shr[TY];
     const int lane = threadIdx.x, ty = threadIdx.y;
     const long kb = 2 * (p0 + (long)blockIdx.x * TX);
     const long jb = b.lo1 + (long)blockIdx.y * TJ;
     const long ib = b.lo0 + (long)blockIdx.z * ichunk;
-    long ie = ib + ichunk - 1;
-    if (ie > b.hi0) ie = b.hi0;
+    const long ie = ib + ichunk - 1 < b.hi0 ? ib + ichunk - 1 : b.hi0;
     const long k = kb + 2 * lane;
-    const double *Src = FUSED ? B : A;
 
-    // source value of a pair: in the fused loop, cells outside the box keep A
-    auto srcPair = [&](long i, long j, long kk) -> double2 {
-        if (!FUSED) return ldPair(A, b, i, j, kk);
-        double2 v = ldPair(B, b, i, j, kk);
-        bool x0 = inBox3(b, i, j, kk), x1 = inBox3(b, i, j, kk + 1);
-        if (!(x0 && x1)) {
-            double2 a = ldPair(A, b, i, j, kk);
-            if (!x0) v.x = a.x;
-            if (!x1) v.y = a.y;
-        }
-        return v;
-    };
-    auto srcOne = [&](long i, long j, long kk) -> double {
-        if (!FUSED) return ldOne(A, b, i, j, kk);
-        return inBox3(b, i, j, kk) ? ldOne(B, b, i, j, kk) : ldOne(A, b, i, j, kk);
-    };
-    (void)Src;
-
-    double2 am[JT], ac[JT], ap[JT];
-    double hcc[JT], hcn[JT];
-    double2 hrc = make_double2(0.0, 0.0), hrn = hrc;
-    const long hrow = (ty == 0) ? jb - 1 : jb + TJ;  // halo row this thread may own
-    const bool ownsRowHalo = (ty == 0) || (ty == TY - 1);
-    const long hcol = (lane == 0) ? kb - 1 : kb + 2 * TX;
-    const bool ownsColHalo = (lane == 0) || (lane == TX - 1);
-
+    // per-thread constants: the lane's columns, its rows, its edge column and halo row
+    const bool kA = k < b.e2, kA1 = k + 1 < b.e2;  // k >= 0 always
+    const bool kI0 = k >= b.lo2 && k <= b.hi2, kI1 = k + 1 >= b.lo2 && k + 1 <= b.hi2;
+    const bool edgeLane = lane == 0 || lane == TX - 1;
+    const long hc = lane == 0 ? kb - 1 : kb + 2 * TX;
+    const bool hcA = edgeLane && hc >= 0 && hc < b.e2, hcI = hc >= b.lo2 && hc <= b.hi2;
+    long jo[JT];
+    bool jA[JT], jI[JT];
 #pragma unroll
     for (int r = 0; r < JT; r++) {
-        long j = jb + ty + TY * r;
-        am[r] = srcPair(ib - 1, j, k);
-        ac[r] = srcPair(ib, j, k);
-        hcc[r] = ownsColHalo ? srcOne(ib, j, hcol) : 0.0;
+        const long j = jb + ty * JT + r;
+        jo[r] = j * b.s1;
+        jA[r] = j < b.e1;
+        jI[r] = j <= b.hi1;
     }
-    if (ownsRowHalo) hrc = srcPair(ib, hrow, k);
+    const bool haloWarp = ty == 0 || ty == TY - 1;
+    const long hr = ty == 0 ? jb - 1 : jb + TJ;
+    const bool hrA = haloWarp && hr >= 0 && hr < b.e1, hrI = hr >= b.lo1 && hr <= b.hi1;
+    const long hro = hr * b.s1;
+    const int hrIdx = ty == 0 ? 0 : TJ + 1;
 
-    uint64_t mb = 0;
-    bool seen = false;
-    for (long i = ib; i <= ie; i++) {
-        // prefetch plane i+1 and, in the fused loop, A_old of own cells in plane i
-        double2 aold[JT];
-#pragma unroll
-        for (int r = 0; r < JT; r++) {
-            long j = jb + ty + TY * r;
-            ap[r] = srcPair(i + 1, j, k);
-            hcn[r] = ownsColHalo ? srcOne(i + 1, j, hcol) : 0.0;
-            if (FUSED) aold[r] = ldPair(A, b, i, j, k);
-        }
-        if (ownsRowHalo) hrn = srcPair(i + 1, hrow, k);
-
-        // stage plane i
-#pragma unroll
-        for (int r = 0; r < JT; r++) {
-            sm[1 + ty + TY * r][1 + 2 * lane] = ac[r].x;
-            sm[1 + ty + TY * r][2 + 2 * lane] = ac[r].y;
-            if (ownsColHalo) sm[1 + ty + TY * r][lane == 0 ? 0 : SW - 1] = hcc[r];
-        }
-        if (ty == 0) {
-            sm[0][1 + 2 * lane] = hrc.x;
-            sm[0][2 + 2 * lane] = hrc.y;
-        } else if (ty == TY - 1) {
-            sm[TJ + 1][1 + 2 * lane] = hrc.x;
-            sm[TJ + 1][2 + 2 * lane] = hrc.y;
-        }
-        __syncthreads();
-
-        // all cells of this thread first (fast paths), then one warp-uniform
-        // native recompute for lanes that met a special operand or result
-        double v[JT][2], dif[JT][2];
-        bool spc = false;
-#pragma unroll
-        for (int r = 0; r < JT; r++) {
-            const int row = 1 + ty + TY * r;
-#pragma unroll
-            for (int e = 0; e < 2; e++) {
-                const int c = 1 + 2 * lane + e;
-                double ame = e ? am[r].y : am[r].x, ape = e ? ap[r].y : ap[r].x;
-                v[r][e] = stencil7<FUSED ? NATIVE - 1 : NATIVE>(ame, sm[row - 1][c], sm[row][c - 1], sm[row][c + 1],
-                                                                sm[row + 1][c], ape, spc);
-                if (FUSED) {
-                    double bo = e ? ac[r].y : ac[r].x, ao = e ? aold[r].y : aold[r].x;
-                    dif[r][e] = NATIVE > 0 ? sf::nadd(bo, -ao) : sf::sub_fast(bo, ao, spc);
-                }
-            }
-        }
-        if (__any_sync(0xffffffffu, spc)) {
-            if (spc) {
-#pragma unroll
-                for (int r = 0; r < JT; r++) {
-                    const int row = 1 + ty + TY * r;
-#pragma unroll
-                    for (int e = 0; e < 2; e++) {
-                        const int c = 1 + 2 * lane + e;
-                        double ame = e ? am[r].y : am[r].x, ape = e ? ap[r].y : ap[r].x;
-                        v[r][e] = sf::ndiv(sf::nadd(sf::nadd(sf::nadd(sf::nadd(sf::nadd(ame, sm[row - 1][c]),
-                                                                           sm[row][c - 1]), sm[row][c + 1]),
-                                                             sm[row + 1][c]), ape), 6.0);
-                        if (FUSED) dif[r][e] = sf::nadd(e ? ac[r].y : ac[r].x, -(e ? aold[r].y : aold[r].x));
+    bool bad = false;  // this thread loaded a value outside pos_ok
+    auto chk = [&](double x) {
+        if (NATIVE < 5) bad |= !sf::pos_ok(x);
+    };
+    // the loop's source value at (ii, row, pair k)
+    auto srcPair = [&](long ii, long joff, bool ja, bool ji) -> double2 {
+        double2 v = make_double2(0.0, 0.0);
+        if (ja && kA && ii >= 0 && ii < b.e0) {
+            const long off = ii * b.s0 + joff + k;
+            if (!FUSED) {
+                v = ld2(A + off);
+            } else {
+                const bool iin = ii >= b.lo0 && ii <= b.hi0;
+                const bool in0 = iin && ji && kI0, in1 = iin && ji && kI1;
+                if (in0 && in1) {
+                    v = ld2(B + off);
+                } else {
+                    v = ld2(A + off);
+                    if (in0 || in1) {
+                        const double2 w = ld2(B + off);
+                        if (in0) v.x = w.x;
+                        if (in1) v.y = w.y;
                     }
                 }
             }
+            if (!kA1) v.y = 0.0;
         }
+        chk(v.x);
+        chk(v.y);
+        return v;
+    };
+    auto srcEdge = [&](long ii, long joff, bool ja, bool ji) -> double {
+        double v = 0.0;
+        if (ja && hcA && ii >= 0 && ii < b.e0) {
+            const long off = ii * b.s0 + joff + hc;
+            v = (FUSED && ii >= b.lo0 && ii <= b.hi0 && ji && hcI) ? B[off] : A[off];
+        }
+        chk(v);
+        return v;
+    };
+
+    double2 pm[JT], pc[JT], pp[JT], pq[JT], ao[JT], aon[JT];
+    double ec[JT], ep[JT], eq[JT];
+    double2 hp = make_double2(0.0, 0.0), hq = hp;
+#pragma unroll
+    for (int r = 0; r < JT; r++) {
+        pm[r] = srcPair(ib - 1, jo[r], jA[r], jI[r]);
+        pc[r] = srcPair(ib, jo[r], jA[r], jI[r]);
+        pp[r] = srcPair(ib + 1, jo[r], jA[r], jI[r]);
+        ec[r] = srcEdge(ib, jo[r], jA[r], jI[r]);
+        ep[r] = srcEdge(ib + 1, jo[r], jA[r], jI[r]);
+        if (FUSED) ao[r] = (jA[r] && kA) ? ld2(A + ib * b.s0 + jo[r] + k) : make_double2(0.0, 0.0);
+    }
+    double2 hc0 = haloWarp ? srcPair(ib, hro, hrA, hrI) : make_double2(0.0, 0.0);
+    if (haloWarp) hp = srcPair(ib + 1, hro, hrA, hrI);
+#pragma unroll
+    for (int r = 0; r < JT; r++) sm[0][1 + ty * JT + r][lane] = pc[r];
+    if (haloWarp) sm[0][hrIdx][lane] = hc0;
+    bool ctaBad = __syncthreads_or(bad) != 0;
+
+    uint64_t mb = 0, qmax = 0;  // eps: FP64-unit part (bit pattern), fixed-point part
+    bool seen = false;
+    int cur = 0;
+    for (long i = ib; i <= ie; i++) {
+        // plane i+2 in flight, and A_old of plane i+1 for the update
 #pragma unroll
         for (int r = 0; r < JT; r++) {
-            const long j = jb + ty + TY * r;
-            if (j > b.hi1) continue;
-            bool in[2];
+            pq[r] = srcPair(i + 2, jo[r], jA[r], jI[r]);
+            eq[r] = srcEdge(i + 2, jo[r], jA[r], jI[r]);
+            if (FUSED)
+                aon[r] = (i + 1 <= ie && jA[r] && kA) ? ld2(A + (i + 1) * b.s0 + jo[r] + k) : make_double2(0.0, 0.0);
+        }
+        if (haloWarp) hq = srcPair(i + 2, hro, hrA, hrI);
+
+        // plane i
+        double v[JT][2];
+        bool spc = false;
 #pragma unroll
-            for (int e = 0; e < 2; e++) in[e] = (k + e) >= b.lo2 && (k + e) <= b.hi2;
-            const long off = i * b.s0 + j * b.s1 + k;
-            if (FUSED) {
-                // update loop on own cells: eps = Max(|B-A|, eps); A = B
-                if (in[0]) mb = sf::absmax_bits(dif[r][0], mb);
-                if (in[1]) mb = sf::absmax_bits(dif[r][1], mb);
-                seen = seen || in[0] || in[1];
-                if (in[0] && in[1]) st2cs(A + off, ac[r]);
-                else if (in[0]) A[off] = ac[r].x;
-                else if (in[1]) A[off + 1] = ac[r].y;
+        for (int r = 0; r < JT; r++) {
+            const double2 up = r > 0 ? pc[r - 1] : sm[cur][ty * JT + r][lane];
+            const double2 dn = r < JT - 1 ? pc[r + 1] : sm[cur][ty * JT + r + 2][lane];
+            double left = __shfl_up_sync(0xffffffffu, pc[r].y, 1), right = __shfl_down_sync(0xffffffffu, pc[r].x, 1);
+            if (lane == 0) left = ec[r];
+            if (lane == TX - 1) right = ec[r];
+            if (NATIVE < 5 && !ctaBad) {
+                v[r][0] = stencil7pos<NATIVE>(pm[r].x, up.x, left, pc[r].y, dn.x, pp[r].x, spc);
+                v[r][1] = stencil7pos<NATIVE>(pm[r].y, up.y, pc[r].x, right, dn.y, pp[r].y, spc);
+            } else {
+                v[r][0] = stencil7<5>(pm[r].x, up.x, left, pc[r].y, dn.x, pp[r].x, spc);
+                v[r][1] = stencil7<5>(pm[r].y, up.y, pc[r].x, right, dn.y, pp[r].y, spc);
             }
-            if (in[0] && in[1]) st2cs(Out + off, make_double2(v[r][0], v[r][1]));
-            else if (in[0]) Out[off] = v[r][0];
-            else if (in[1]) Out[off + 1] = v[r][1];
+            if (__any_sync(0xffffffffu, spc)) {  // rare: an operand or result the fast division does not cover
+                if (spc) {
+                    v[r][0] = sf::ndiv(sf::nadd(sf::nadd(sf::nadd(sf::nadd(sf::nadd(pm[r].x, up.x), left), pc[r].y),
+                                                         dn.x), pp[r].x), 6.0);
+                    v[r][1] = sf::ndiv(sf::nadd(sf::nadd(sf::nadd(sf::nadd(sf::nadd(pm[r].y, up.y), pc[r].x), right),
+                                                         dn.y), pp[r].y), 6.0);
+                }
+                spc = false;
+            }
         }
-        __syncthreads();
 #pragma unroll
         for (int r = 0; r < JT; r++) {
-            am[r] = ac[r];
-            ac[r] = ap[r];
-            hcc[r] = hcn[r];
+            if (!jI[r]) continue;
+            const long off = i * b.s0 + jo[r] + k;
+            if (FUSED) {
+                // update loop on own cells: eps = Max(|B - A|, eps); A = B
+                bool ok = true;
+                const uint64_t b0 = sf::q64(pc[r].x, ok), a0 = sf::q64(ao[r].x, ok);
+                const uint64_t b1 = sf::q64(pc[r].y, ok), a1 = sf::q64(ao[r].y, ok);
+                const uint64_t d0 = b0 > a0 ? b0 - a0 : a0 - b0, d1 = b1 > a1 ? b1 - a1 : a1 - b1;
+                if (kI0 && d0 > qmax) qmax = d0;
+                if (kI1 && d1 > qmax) qmax = d1;
+                if (__any_sync(0xffffffffu, !ok) && !ok) {
+                    if (kI0) mb = sf::absmax_bits(sf::nadd(pc[r].x, -ao[r].x), mb);
+                    if (kI1) mb = sf::absmax_bits(sf::nadd(pc[r].y, -ao[r].y), mb);
+                }
+                seen = seen || kI0 || kI1;
+                if (kI0 && kI1) st2cs(A + off, pc[r]);
+                else if (kI0) A[off] = pc[r].x;
+                else if (kI1) A[off + 1] = pc[r].y;
+            }
+            if (kI0 && kI1) st2cs(Out + off, make_double2(v[r][0], v[r][1]));
+            else if (kI0) Out[off] = v[r][0];
+            else if (kI1) Out[off + 1] = v[r][1];
         }
-        hrc = hrn;
+        // stage plane i+1, then rotate
+#pragma unroll
+        for (int r = 0; r < JT; r++) sm[cur ^ 1][1 + ty * JT + r][lane] = pp[r];
+        if (haloWarp) sm[cur ^ 1][hrIdx][lane] = hp;
+        ctaBad = (__syncthreads_or(bad) != 0) || ctaBad;
+        cur ^= 1;
+#pragma unroll
+        for (int r = 0; r < JT; r++) {
+            pm[r] = pc[r];
+            pc[r] = pp[r];
+            pp[r] = pq[r];
+            ec[r] = ep[r];
+            ep[r] = eq[r];
+            if (FUSED) ao[r] = aon[r];
+        }
+        hp = hq;
     }
     if (FUSED) {
-        double m = ctaMax(seen ? sf::from(mb) : -__builtin_huge_val(), shr);
+        // RN(max |b - a|) from the fixed-point part, then the MAX with the FP64-unit part
+        double m = -__builtin_huge_val();
+        if (seen) {
+            const double q = __ull2double_rn(qmax) * 0x1p-64;
+            const double f = sf::from(mb);
+            m = q > f ? q : f;
+        }
+        m = ctaMax(m, shr);
         if (ty == 0 && lane == 0)
             items[blockIdx.x + gridDim.x * ((long)blockIdx.y + (long)gridDim.y * blockIdx.z)] = m;
     }
@@ -396,6 +465,7 @@ St3Geom st3Geom(const long lo[3], const long hi[3], int TJ) {
 // ---------------------------------------------------------------- 2-D stencil / fused (1.5-D blocking)
 
 constexpr int T2Y = 8;  // independent column strips per CTA (one per warp)
+constexpr int SW = 66;  // shared row: k = kb-1 .. kb+64
 
 struct Box2 {
     long s0;
@@ -581,25 +651,24 @@ __global__ void kCopyOutside(const double *__restrict__ src, double *__restrict_
     }
 }
 
-// native = FP64 operations per cell on the FP64 unit (clamped to the kernel's count)
-// fused variant 7: all six operations native, two rows per thread
-constexpr int FUSED_JT2 = 7;
+// 3-D variants (stencil and fused alike): v < 12: v = 6 * (JT - 1) + N, N =
+// additions of a cell on the FP64 unit (0..5, the others on the integer pipe),
+// JT = rows per thread, two CTAs per SM; v = 12, 13: all additions native, one
+// row per thread, registers capped for three / four CTAs per SM
+constexpr int V3 = 14;
+int jtOf3(int v) { return (v >= 6 && v < 12) ? 2 : 1; }
 
 template <bool FUSED>
-void launch3(int native, const St3Geom &g, double *A, const double *B, double *Out, const Box3 &b, double *items,
+void launch3(int variant, const St3Geom &g, double *A, const double *B, double *Out, const Box3 &b, double *items,
              cudaStream_t s) {
-    const int n = FUSED ? 6 : 5;
     dim3 blk(TX, TY);
-    if (FUSED && native == FUSED_JT2) {
-        kStencil3<true, 6, 2><<<g.grid, blk, 0, s>>>(A, B, Out, b, g.p0, g.ichunk, items);
-        return;
-    }
-    native = native < 0 ? 0 : (native > n ? n : native);
-    switch (native) {
-#define C3(N)                                                                                   \
-    case N: kStencil3<FUSED, (FUSED ? N : (N > 5 ? 5 : N)), (FUSED ? JT_FUSED : JT_PLAIN)><<<g.grid, blk, 0, s>>>(A, B, Out, b, g.p0, g.ichunk, items); break;
-        C3(0) C3(1) C3(2) C3(3) C3(4) C3(5) C3(6)
+    switch (variant) {
+#define C3(V)                                                                                       \
+    case V: kStencil3<FUSED, (V) % 6, 1 + (V) / 6, 2><<<g.grid, blk, 0, s>>>(A, B, Out, b, g.p0, g.ichunk, items); break;
+        C3(0) C3(1) C3(2) C3(3) C3(4) C3(5) C3(6) C3(7) C3(8) C3(9) C3(10) C3(11)
 #undef C3
+    case 12: kStencil3<FUSED, 5, 1, 3><<<g.grid, blk, 0, s>>>(A, B, Out, b, g.p0, g.ichunk, items); break;
+    case 13: kStencil3<FUSED, 5, 1, 4><<<g.grid, blk, 0, s>>>(A, B, Out, b, g.p0, g.ichunk, items); break;
     }
 }
 
@@ -638,7 +707,8 @@ int dvmhgb_jac3d_update(double *A, const double *B, const long st[3], const long
 
 int dvmhgb_jac3d_stencil(const double *A, double *B, const long st[3], const long ext[3], const long lo[3],
                          const long hi[3], int native, void *stream) {
-    St3Geom g = st3Geom(lo, hi, TY * JT_PLAIN);
+    if (native < 0 || native >= V3) return -1;
+    St3Geom g = st3Geom(lo, hi, TY * jtOf3(native));
     if (!g.ok || !A || !B || !rows16(st, 3) || !aligned16(A) || !aligned16(B)) return -1;
     Box3 b{st[0], st[1], ext[0], ext[1], ext[2], lo[0], lo[1], lo[2], hi[0], hi[1], hi[2]};
     launch3<false>(native, g, (double *)A, nullptr, B, b, nullptr, (cudaStream_t)stream);
@@ -647,13 +717,15 @@ int dvmhgb_jac3d_stencil(const double *A, double *B, const long st[3], const lon
 }
 
 long dvmhgb_jac3d_fused_items(const long lo[3], const long hi[3], int native) {
-    St3Geom g = st3Geom(lo, hi, TY * (native == FUSED_JT2 ? 2 : JT_FUSED));
+    if (native < 0 || native >= V3) return -1;
+    St3Geom g = st3Geom(lo, hi, TY * jtOf3(native));
     return (long)g.grid.x * g.grid.y * g.grid.z;
 }
 
 int dvmhgb_jac3d_fused(double *A, const double *B, double *Bnew, const long st[3], const long ext[3],
                        const long lo[3], const long hi[3], double *items, int native, void *stream) {
-    St3Geom g = st3Geom(lo, hi, TY * (native == FUSED_JT2 ? 2 : JT_FUSED));
+    if (native < 0 || native >= V3) return -1;
+    St3Geom g = st3Geom(lo, hi, TY * jtOf3(native));
     if (!g.ok || !A || !B || !Bnew || !items || !rows16(st, 3) || !aligned16(A) || !aligned16(B) || !aligned16(Bnew))
         return -1;
     Box3 b{st[0], st[1], ext[0], ext[1], ext[2], lo[0], lo[1], lo[2], hi[0], hi[1], hi[2]};

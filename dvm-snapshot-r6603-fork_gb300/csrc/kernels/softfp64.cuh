@@ -340,6 +340,34 @@ SF_HD double add_pos(double a, double b) {
     return from(far ? X : r);
 }
 
+// pos_small: +0 or a positive normal below 2^1009 -- sums of up to 2^13 such
+// values stay below 2^1022, so chains of add_pos over them stay exact.
+SF_HD bool pos_small(double x) {
+    uint32_t h = hi32(bits(x));
+    return (h >> 20) - 1 < 0x7EFu || bits(x) == 0;  // exponent field 1..0x7EF: below 2^1009
+}
+
+// x * 2^k exactly for x = +-0 or a normal x whose exponent field is at most
+// 0x7FE - k (scale_up_ok); the exponent field is incremented by k.
+SF_HD bool scale_up_ok(double x, int k) {
+    uint32_t e = (hi32(bits(x)) >> 20) & 0x7FF;
+    return (e - 1 < (uint32_t)(0x7FE - k)) || (bits(x) & ~SIGN) == 0;
+}
+SF_HD double scale_up(double x, int k) {
+    uint64_t X = bits(x);
+    return (X & ~SIGN) == 0 ? x : from(X + ((uint64_t)k << 52));
+}
+
+// x * 2^64 as an exact 64-bit integer for x = +0 or 2^-12 <= x < 1 (such x are
+// multiples of 2^-64 below 1); ok is cleared for any other x (result 0).
+SF_HD uint64_t q64(double x, bool &ok) {
+    uint64_t X = bits(x);
+    uint32_t e = hi32(X) >> 20;  // the sign bit makes a negative x out of range
+    bool in = e - 1011u <= 11u;
+    ok &= in | (X == 0);
+    return in ? ((X & MANT) | HID) << (e - 1011u) : 0;
+}
+
 // Max(|t|, m) on bit patterns: for non-negative doubles the IEEE order is the
 // unsigned integer order.  A NaN t leaves m unchanged, as (t > m ? t : m) does.
 SF_HD uint64_t absmax_bits(double t, uint64_t m) {

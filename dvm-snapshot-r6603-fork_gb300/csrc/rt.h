@@ -66,8 +66,25 @@ struct Settings {
     int tuneMode = 0;           // 0 off, 1 exhaustive, 2 model-guided (DVMH_OPT_PARAMS)
     int graphCacheMax = 64;
     bool fuse = true;
+    bool hostProf = false;      // DVMH_GB_HOSTPROF: time the ABI entry points on the host
 };
 extern Settings settings;
+
+// ---------------------------------------------------------------- host profile
+//
+// With DVMH_GB_HOSTPROF=1 every profiled entry point accumulates its calls and
+// inclusive wall time (steady clock); the table is printed to stderr at exit
+// or by dvmhgb_hostprof_dump().  Off, a scope costs one branch.
+int profId(const char *name);
+struct ProfScope {
+    int id;
+    long long t0;
+    explicit ProfScope(int i);
+    ~ProfScope();
+};
+#define GB_PROF(name)                                                \
+    static const int gbProfId_ = ::dvmhgb::profId(name);             \
+    ::dvmhgb::ProfScope gbProfScope_(gbProfId_)
 
 // ---------------------------------------------------------------- objects
 
@@ -106,6 +123,8 @@ struct Array : Obj {
     bool hostActual = true, devActual = false;
     DvmType *desc = nullptr;
     std::string name;
+    const void *regMark = nullptr;  // the region this array was last registered in
+    size_t regIdx = 0;              // and its entry there
     size_t hostBytes() const { return helems * esize; }
     size_t devBytes() const { return delems * esize; }
 };

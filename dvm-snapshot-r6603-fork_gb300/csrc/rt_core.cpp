@@ -18,6 +18,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <ctime>
+#include <unordered_map>
 #include <unordered_set>
 
 #include "rt.h"
@@ -56,6 +57,44 @@ void logmsg(int level, const char *fmt, ...) {
     va_end(ap);
 }
 
+// ---------------------------------------------------------------- host profile
+
+namespace {
+struct ProfEntry {
+    const char *name;
+    long calls;
+    long long ns;
+};
+ProfEntry profTable[128];
+int profCount = 0;
+long long nowNs() {
+    struct timespec ts;
+    clock_gettime(CLOCK_MONOTONIC, &ts);
+    return (long long)ts.tv_sec * 1000000000LL + ts.tv_nsec;
+}
+void profAtExit() {
+    if (settings.hostProf) dvmhgb_hostprof_dump();
+}
+}  // namespace
+
+int profId(const char *name) {
+    if (profCount == 0) atexit(profAtExit);
+    if (profCount >= 128) return -1;
+    profTable[profCount] = {name, 0, 0};
+    return profCount++;
+}
+
+ProfScope::ProfScope(int i) : id(settings.hostProf ? i : -1), t0(0) {
+    if (id >= 0) t0 = nowNs();
+}
+
+ProfScope::~ProfScope() {
+    if (id >= 0) {
+        profTable[id].calls++;
+        profTable[id].ns += nowNs() - t0;
+    }
+}
+
 size_t typeSize(int vtype) {
     switch (vtype) {
         case rt_CHAR: case rt_UCHAR: return 1;
@@ -80,6 +119,7 @@ static void loadSettings() {
     if (const char *l = getenv("DVMH_LOGLEVEL")) settings.logLevel = atoi(l);
     if (const char *s = getenv("DVMH_SYNC_CUDA")) settings.syncEachLoop = atoi(s) != 0;
     if (const char *t = getenv("DVMH_OPT_PARAMS")) settings.tuneMode = atoi(t);
+    if (const char *h = getenv("DVMH_GB_HOSTPROF")) settings.hostProf = atoi(h) != 0;
     if (const char *f = getenv("DVMH_GB_FUSE")) settings.fuse = atoi(f) != 0;
 }
 
@@ -94,13 +134,12 @@ Array *arrayOf(const DvmType desc[], const char *what) {
     return (Array *)o;
 }
 
-bool isArrayDesc(const void *p) {
-    // handler parameters are checked against the registry before any dereference
-    for (Obj *o : liveObjs)
-        if (o->kind == K_ARRAY && ((Array *)o)->desc == (const DvmType *)p)
-            return true;
-    return false;
-}
+// descriptors of the live arrays: handler parameters are checked against this
+// registry before any dereference (one hash lookup per parameter)
+// (a count: a descriptor's storage may be reused by a new array before the old one is freed)
+static std::unordered_map<const void *, int> arrayDescs;
+
+bool isArrayDesc(const void *p) { return arrayDescs.count(p) != 0; }
 
 // ---------------------------------------------------------------- variables
 
@@ -325,6 +364,7 @@ void dvmh_array_create_C(DvmType dvmDesc[], DvmType rank, DvmType typeSize, ...)
     a->desc = dvmDesc;
     dvmDesc[0] = (DvmType)a;
     track(a);
+    arrayDescs[dvmDesc]++;
 }
 
 void dvmh_template_create_C(DvmType dvmDesc[], DvmType rank, ...) {
@@ -361,6 +401,7 @@ void dvmh_redistribute_C(DvmType dvmDesc[], DvmType rank, ...) {
 }
 
 DvmType dvmh_alignment_linear_C(DvmType axis, DvmType multiplier, DvmType summand) {
+    GB_PROF("dvmh_alignment_linear_C");
     AlignHelper *h = new AlignHelper{ALIGN_MAGIC, (long)axis, (long)multiplier, (long)summand};
     return (DvmType)h;
 }
@@ -396,6 +437,7 @@ void dvmh_array_free_C(DvmType dvmDesc[]) {
     if (a->devAlt) devFree(a->devAlt);
     if (a->host) hostFree(a->host);
     untrack(a);
+    if (--arrayDescs[a->desc] <= 0) arrayDescs.erase(a->desc);
     dvmDesc[0] = 0;
     delete a;
 }
@@ -478,6 +520,7 @@ void *dvmh_get_element_addr_C(const DvmType dvmDesc[], DvmType rank, ...) {
 // ---------------------------------------------------------------- actuality
 
 void dvmh_get_actual_variable2_(void *addr) {
+    GB_PROF("dvmh_get_actual_variable2_");
     if (!st.inited) return;
     auto it = st.vars.find((const char *)addr);
     if (it == st.vars.end()) return;  // unknown variables are always current on the host
@@ -489,6 +532,7 @@ void dvmh_get_actual_variable2_(void *addr) {
 }
 
 void dvmh_actual_variable2_(const void *addr) {
+    GB_PROF("dvmh_actual_variable2_");
     if (!st.inited) return;
     auto it = st.vars.find((const char *)addr);
     if (it == st.vars.end()) return;
@@ -498,11 +542,13 @@ void dvmh_actual_variable2_(const void *addr) {
 }
 
 void dvmh_get_actual_array2_(const DvmType dvmDesc[]) {
+    GB_PROF("dvmh_get_actual_array2_");
     Array *a = arrayOf(dvmDesc, "dvmh_get_actual_array");
     ensureHostActual(a);
 }
 
 void dvmh_actual_array2_(const DvmType dvmDesc[]) {
+    GB_PROF("dvmh_actual_array2_");
     Array *a = arrayOf(dvmDesc, "dvmh_actual_array");
     GB_CHECK(a->distributed, "array is not distributed");
     a->hostActual = true;
@@ -564,6 +610,7 @@ void dvmh_actual_all2_(void) {
 // ---------------------------------------------------------------- shadow renew
 
 void dvmh_shadow_renew_C(const DvmType dvmDesc[], DvmType cornerFlag, DvmType specifiedRank, ...) {
+    GB_PROF("dvmh_shadow_renew_C");
     (void)cornerFlag;
     Array *a = arrayOf(dvmDesc, "dvmh_shadow_renew");
     GB_CHECK(specifiedRank == 0 || specifiedRank == a->rank, "shadow renew rank mismatch");
@@ -582,6 +629,7 @@ void dvmh_shadow_renew_C(const DvmType dvmDesc[], DvmType cornerFlag, DvmType sp
 // ---------------------------------------------------------------- regions
 
 DvmType dvmh_region_create_C(DvmType regionFlags) {
+    GB_PROF("dvmh_region_create_C");
     GB_CHECK(st.inited, "LibDVMH is not initialized");
     GB_CHECK(!st.curRegion, "nested regions are not allowed");
     Region *r = new Region();
@@ -598,16 +646,18 @@ static Region *regionOf(DvmType ref, const char *what) {
 }
 
 void dvmh_region_register_array_C(DvmType curRegion, DvmType intent, const DvmType dvmDesc[], const char varName[]) {
+    GB_PROF("dvmh_region_register_array_C");
     Region *r = regionOf(curRegion, "dvmh_region_register_array");
     Obj *o = (Obj *)dvmDesc[0];
     if (isLive(o, K_TEMPLATE)) return;
     Array *a = arrayOf(dvmDesc, "dvmh_region_register_array");
     if (varName && a->name.empty()) a->name = varName;
-    for (auto &ra : r->arrays)
-        if (ra.arr == a) {
-            ra.intent |= (long)intent;
-            return;
-        }
+    if (a->regMark == r && a->regIdx < r->arrays.size() && r->arrays[a->regIdx].arr == a) {
+        r->arrays[a->regIdx].intent |= (long)intent;
+        return;
+    }
+    a->regMark = r;
+    a->regIdx = r->arrays.size();
     r->arrays.push_back({a, (long)intent});
 }
 
@@ -621,6 +671,7 @@ void dvmh_region_register_subarray_C(DvmType curRegion, DvmType intent, const Dv
 
 void dvmh_region_register_scalar_C(DvmType curRegion, DvmType intent, const void *addr, DvmType typeSize,
                                    const char varName[]) {
+    GB_PROF("dvmh_region_register_scalar_C");
     Region *r = regionOf(curRegion, "dvmh_region_register_scalar");
     GB_CHECK(addr && typeSize > 0, "invalid scalar registration");
     Var *v = varGet(addr, (size_t)typeSize);
@@ -634,6 +685,7 @@ void dvmh_region_register_scalar_C(DvmType curRegion, DvmType intent, const void
 }
 
 void dvmh_region_execute_on_targets_C(DvmType curRegion, DvmType deviceTypes) {
+    GB_PROF("dvmh_region_execute_on_targets_C");
     Region *r = regionOf(curRegion, "dvmh_region_execute_on_targets");
     GB_CHECK(deviceTypes & DEVICE_TYPE_CUDA,
              "region targets exclude CUDA: this runtime executes parallel loops on the GPU only");
@@ -653,6 +705,7 @@ void dvmh_region_execute_on_targets_C(DvmType curRegion, DvmType deviceTypes) {
 }
 
 void dvmh_region_end_C(DvmType curRegion) {
+    GB_PROF("dvmh_region_end_C");
     Region *r = regionOf(curRegion, "dvmh_region_end");
     GB_CHECK(!st.curLoop, "region ends inside a parallel loop");
     // everything queued inside the region is launched by its end: handler
@@ -677,6 +730,18 @@ void dvmhgb_get_stats(dvmhgb_stats_t *out) {
 }
 
 void dvmhgb_reset_stats(void) { memset(&stats, 0, sizeof stats); }
+
+void dvmhgb_hostprof_dump(void) {
+    fprintf(stderr, "[dvmh_gb host profile] %-40s %10s %12s %10s\n", "entry point", "calls", "total ms", "us/call");
+    for (int i = 0; i < profCount; i++)
+        if (profTable[i].calls)
+            fprintf(stderr, "[dvmh_gb host profile] %-40s %10ld %12.3f %10.3f\n", profTable[i].name, profTable[i].calls,
+                    profTable[i].ns * 1e-6, profTable[i].ns * 1e-3 / profTable[i].calls);
+}
+
+void dvmhgb_hostprof_reset(void) {
+    for (int i = 0; i < profCount; i++) profTable[i].calls = 0, profTable[i].ns = 0;
+}
 
 void dvmhgb_count_launches(long n) { stats.kernel_launches += n; }
 

@@ -108,6 +108,7 @@ void deviceFinish() {
 
 void collectTimings();
 void streamSync() {
+    GB_PROF("streamSync");
     GB_CUDA(cudaStreamSynchronize(gpu.stream));
     collectTimings();
     int code = *(volatile int *)gpu.statusHost;
@@ -211,6 +212,7 @@ Staging &stageFor(const Var *v) {
 }  // namespace
 
 void varH2D(Var *v) {
+    GB_PROF("varH2D");
     ensureVarDev(v);
     queueFlush();
     Staging &s = stageFor(v);
@@ -222,6 +224,7 @@ void varH2D(Var *v) {
 }
 
 void varD2H(Var *v) {
+    GB_PROF("varD2H");
     GB_INTERNAL(v->dev, "variable without a device copy");
     queueFlush();
     Staging &s = stageFor(v);

@@ -221,6 +221,7 @@ static void timeEnd(TimedExec &t) {
 // a launch of a cached graph, timed as a whole when timing is on; the time
 // goes to its handler when it ran exactly one
 static void launchGraph(CachedGraph &g) {
+    GB_PROF("launchGraph");
     bool timed = timingOn && !g.times.empty();
     if (timed) {
         if (!g.e0) {
@@ -410,6 +411,7 @@ static void dropGraph(CachedGraph &g) {
 }
 
 void queueFlush() {
+    GB_PROF("queueFlush");
     if (queue.empty() || ctx.capturing) return;
     std::vector<Loop *> q;
     q.swap(queue);
@@ -493,6 +495,7 @@ extern "C" {
 // ---------------------------------------------------------------- loop construction
 
 DvmType dvmh_loop_create_C(DvmType curRegion, DvmType rank, ...) {
+    GB_PROF("dvmh_loop_create_C");
     GB_CHECK(st.inited, "LibDVMH is not initialized");
     GB_CHECK(!st.curLoop, "nested parallel loops are not allowed");
     GB_CHECK(rank >= 0 && rank <= MAXR, "loop rank must be in 0..%d", MAXR);
@@ -522,6 +525,7 @@ DvmType dvmh_loop_create_C(DvmType curRegion, DvmType rank, ...) {
 }
 
 void dvmh_loop_map_C(DvmType curLoop, const DvmType templDesc[], DvmType templRank, ...) {
+    GB_PROF("dvmh_loop_map_C");
     Loop *l = loopOf(curLoop, "dvmh_loop_map");
     Obj *o = (Obj *)templDesc[0];
     if (isLive(o, K_ARRAY)) l->mapArr = (Array *)o;
@@ -540,6 +544,7 @@ void dvmh_loop_map_C(DvmType curLoop, const DvmType templDesc[], DvmType templRa
 }
 
 void dvmh_loop_set_cuda_block_C(DvmType curLoop, DvmType xSize, DvmType ySize, DvmType zSize) {
+    GB_PROF("dvmh_loop_set_cuda_block_C");
     Loop *l = loopOf(curLoop, "dvmh_loop_set_cuda_block");
     GB_CHECK(xSize >= 1 && ySize >= 1 && zSize >= 1 && xSize * ySize * zSize <= 1024, "invalid CUDA block");
     l->cudaBlock[0] = (int)xSize;
@@ -552,6 +557,7 @@ void dvmh_loop_set_stage_C(DvmType curLoop, DvmType stage) { loopOf(curLoop, "dv
 
 void dvmh_loop_reduction_C(DvmType curLoop, DvmType redType, void *arrayAddr, DvmType varType, DvmType arrayLength,
                            void *locAddr, DvmType locSize) {
+    GB_PROF("dvmh_loop_reduction_C");
     Loop *l = loopOf(curLoop, "dvmh_loop_reduction");
     GB_CHECK(arrayAddr, "NULL reduction variable");
     GB_CHECK(redType >= rf_SUM && redType <= rf_MINLOC, "unknown reduction function %ld", (long)redType);
@@ -605,6 +611,7 @@ void dvmh_loop_reduction_C(DvmType curLoop, DvmType redType, void *arrayAddr, Dv
 }
 
 void dvmh_loop_across_C(DvmType curLoop, DvmType isOut, const DvmType dvmDesc[], DvmType rank, ...) {
+    GB_PROF("dvmh_loop_across_C");
     Loop *l = loopOf(curLoop, "dvmh_loop_across");
     Array *a = arrayOf(dvmDesc, "dvmh_loop_across");
     GB_CHECK(rank == a->rank, "rank in across directive must be the rank of the array");
@@ -630,6 +637,7 @@ void dvmh_loop_shadow_compute_C(DvmType curLoop, const DvmType templDesc[], DvmT
 }
 
 DvmType dvmh_handler_func_C(DvmHandlerFunc handlerFunc, DvmType customParamCount, ...) {
+    GB_PROF("dvmh_handler_func_C");
     GB_CHECK(handlerFunc, "NULL handler function");
     GB_CHECK(customParamCount >= 0 && customParamCount <= 40, "handler with %ld parameters (at most 40)",
              (long)customParamCount);
@@ -644,6 +652,7 @@ DvmType dvmh_handler_func_C(DvmHandlerFunc handlerFunc, DvmType customParamCount
 }
 
 void dvmh_loop_register_handler_C(DvmType curLoop, DvmType deviceType, DvmType handlerType, DvmType handlerHelper) {
+    GB_PROF("dvmh_loop_register_handler_C");
     (void)handlerType;
     Loop *l = loopOf(curLoop, "dvmh_loop_register_handler");
     HandlerRef *h = (HandlerRef *)handlerHelper;
@@ -661,6 +670,7 @@ void dvmh_loop_register_handler_C(DvmType curLoop, DvmType deviceType, DvmType h
 }
 
 void dvmh_loop_perform_C(DvmType curLoop) {
+    GB_PROF("dvmh_loop_perform_C");
     Loop *l = loopOf(curLoop, "dvmh_loop_perform");
     if (settings.tuneMode) timingOn = true;  // the tuner learns from recorded timings
     stats.loops_performed++;

@@ -71,13 +71,15 @@ extern "C" void loop_heat_batch_cuda(DvmType *refs, DvmType count) {
     dvmhgb_heat_desc *table =
         (dvmhgb_heat_desc *)dvmhgb_loop_host_scratch(refs[0], (DvmType)(sizeof(dvmhgb_heat_desc) * count));
     cudaStream_t stream = 0;
-    long total = 0;
+    long total = 0, units = 0;
     for (DvmType q = 0; q < count; q++) {
         DvmType ref = refs[q];
         prepare(ref, (DvmType *)dvmhgb_loop_param(ref, 0), (DvmType *)dvmhgb_loop_param(ref, 1),
                 (double *)dvmhgb_loop_param(ref, 5), &table[q], &stream);
-        table[q].unitBase = total;
-        total += table[q].units;
+        table[q].unitBase = units;
+        table[q].stripBase = total;
+        units += table[q].units;
+        total += table[q].strips;
     }
     dvmhgb_heat_desc *dev =
         (dvmhgb_heat_desc *)dvmhgb_loop_scratch(refs[0], (DvmType)(sizeof(dvmhgb_heat_desc) * count));

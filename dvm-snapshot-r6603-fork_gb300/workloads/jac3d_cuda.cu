@@ -17,10 +17,9 @@
 #include "dvmh_gb_kernels.h"
 
 #define R 3
-// FP64 additions per cell of the stencil loop; default count on the FP64 unit
-#define NOPS_STN 5
-#define DEF_STN 5
-#define DEF_FUSED 6
+// default kernel variants (v = 6 * (rows per thread - 1) + additions on the FP64 unit)
+#define DEF_STN 13   // all additions on the FP64 unit, one row a thread, four CTAs per SM
+#define DEF_FUSED 12 // the same, three CTAs per SM
 
 namespace {
 
@@ -88,7 +87,7 @@ extern "C" void loop_jac3d_stn_cuda(DvmType *pLoopRef, DvmType A_hdr[], DvmType 
     dim3 threads(0, 0, 0);
     cudaStream_t stream;
     dvmh_loop_cuda_get_config_C(loop_ref, 0, 0, &threads, &stream, 0);
-    check(dvmhgb_jac3d_stencil(A.base, B.base, A.st, A.ext, lo, hi, dvmhgb_loop_variant(loop_ref, NOPS_STN + 1, DEF_STN), stream), "loop_jac3d_stn_cuda");
+    check(dvmhgb_jac3d_stencil(A.base, B.base, A.st, A.ext, lo, hi, dvmhgb_loop_variant(loop_ref, DVMHGB_JAC3D_VARIANTS, DEF_STN), stream), "loop_jac3d_stn_cuda");
 }
 
 // refs[0]: the update loop (A_hdr, B_hdr, eps_ptr), refs[1]: the stencil loop (A2_hdr, B2_hdr)
@@ -111,7 +110,7 @@ extern "C" void loop_jac3d_fused_cuda(DvmType refs[2], DvmType A_hdr[], DvmType 
     cudaStream_t stream;
     dvmh_loop_cuda_get_config_C(upd, 0, 0, &threads, &stream, 0);
     dvmh_loop_cuda_get_config_C(stn, 0, 0, &threads, &stream, 0);
-    const int variant = dvmhgb_loop_variant(upd, NOPS_STN + 3, DEF_FUSED);
+    const int variant = dvmhgb_loop_variant(upd, DVMHGB_JAC3D_VARIANTS, DEF_FUSED);
     double eps, *eps_grid = 0;
     dvmh_loop_cuda_register_red_C(upd, 1, (void **)&eps_grid, 0);
     dvmh_loop_red_init_C(upd, 1, &eps, 0);

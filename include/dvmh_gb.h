@@ -99,6 +99,11 @@ void dvmhgb_reset_stats(void);
  * kernels inside captured graphs, once per replay). */
 void dvmhgb_count_launches(long n);
 
+/* Host profile of the ABI entry points (DVMH_GB_HOSTPROF=1): calls and
+ * inclusive wall time per entry point, printed to stderr at exit or now. */
+void dvmhgb_hostprof_dump(void);
+void dvmhgb_hostprof_reset(void);
+
 /* Stream the runtime launches on (a cudaStream_t). */
 void *dvmhgb_stream(void);
 

@@ -29,13 +29,18 @@ extern "C" {
 long dvmhgb_jac3d_update_items(const long lo[3], const long hi[3]);
 int dvmhgb_jac3d_update(double *A, const double *B, const long st[3], const long lo[3], const long hi[3],
                         double *items, int native, void *stream);
-/* loop 2: B = (A[i-1]+A[j-1]+A[k-1]+A[k+1]+A[j+1]+A[i+1]) / 6 over the box */
+/* loop 2: B = (A[i-1]+A[j-1]+A[k-1]+A[k+1]+A[j+1]+A[i+1]) / 6 over the box.
+ * Variants (stencil and fused alike): v = 0..11: v = 6 * (rows per thread - 1)
+ * + N, N = 0..5 additions of a cell on the FP64 unit (the others on the integer
+ * pipe when the CTA's inputs are all +0 or positive normal, else all native);
+ * v = 12, 13: all native, one row per thread, registers capped for 3 / 4 CTAs
+ * per SM; -1 for v outside 0..DVMHGB_JAC3D_VARIANTS-1 */
+#define DVMHGB_JAC3D_VARIANTS 14
 int dvmhgb_jac3d_stencil(const double *A, double *B, const long st[3], const long ext[3], const long lo[3],
                          const long hi[3], int native, void *stream);
 /* loops 1+2 fused (same box): reads A, B; writes A = B and Bnew = stencil(A_new)
  * into Bnew (a second buffer of B's layout), B's values outside the box copied
- * into Bnew; MAX partials, one per CTA (count depends on the variant: native
- * 0..6 = FP64 operations on the FP64 unit, 7 = all native, two rows a thread) */
+ * into Bnew; MAX partials, one per CTA (the count depends on the variant) */
 long dvmhgb_jac3d_fused_items(const long lo[3], const long hi[3], int native);
 int dvmhgb_jac3d_fused(double *A, const double *B, double *Bnew, const long st[3], const long ext[3],
                        const long lo[3], const long hi[3], double *items, int native, void *stream);
@@ -64,7 +69,10 @@ int dvmhgb_sor3d_sweep(double *A, const long st[3], const long ext[3], const lon
 
 /* ---- explicit 2-D heat step, FP64 (workloads/heat.c), with SUM and MINLOC:
  * per (row, 64-wide chunk) unit one SUM item (canonical pairwise tree), one
- * MINLOC value item and its location {i, j} (two ints) ---- */
+ * MINLOC value item and its location {i, j} (two ints).  The kernels walk
+ * strips of sr rows of one chunk; dvmhgb_heat (one loop) shortens the strips
+ * until they fill the GPU ---- */
+#define DVMHGB_HEAT_STRIP 64
 typedef struct {
     const double *src;
     double *dst;
@@ -72,14 +80,17 @@ typedef struct {
     long lo0, hi0, lo1, hi1; /* loop box */
     const double *coef;      /* device address of c */
     long c0, nck, units, unitBase;
+    long sr;                 /* rows per strip (dvmhgb_heat_desc_fill: DVMHGB_HEAT_STRIP) */
+    long strips, stripBase;  /* strips of this loop; prefix over a table (dvmhgb_heat_many) */
     double *sumItems, *minItems;
     int *locItems;
 } dvmhgb_heat_desc;
 int dvmhgb_heat_desc_fill(dvmhgb_heat_desc *d, const double *src, double *dst, long rowStride, const long lo[2],
                           const long hi[2], const double *coefDev);
 int dvmhgb_heat(const dvmhgb_heat_desc *d, void *stream);
-/* dDev: device array of n descriptors with unitBase = prefix sums of units */
-int dvmhgb_heat_many(const dvmhgb_heat_desc *dDev, int n, long totalUnits, void *stream);
+/* dDev: device array of n descriptors with unitBase / stripBase = prefix sums of
+ * units / strips; totalStrips = the sum of strips */
+int dvmhgb_heat_many(const dvmhgb_heat_desc *dDev, int n, long totalStrips, void *stream);
 
 /* ---- no counterpart in the reference: the Jacobi-3D update loop for callers
  * that cannot allocate device memory (inside a stream capture in global mode,

@@ -93,3 +93,26 @@ extern "C" long softfp64_check_pos(long n, uint64_t seed) {
     }
     return bad;
 }
+
+// scale_up(x, 2) == x * 4.0 wherever scale_up_ok(x, 2); pos_small implies pos_ok
+extern "C" long softfp64_check_scale(long n, uint64_t seed) {
+    long bad = 0;
+    for (long i = 0; i < n; i++) {
+        uint64_t r = mix(seed + 2 * i + 1), q = mix(seed + 2 * i + 2);
+        uint64_t X = r;
+        switch (q & 7) {
+            case 0: X &= sf::SIGN; break;                                          // +-0
+            case 1: X = (X & 0x800FFFFFFFFFFFFFull); break;                         // subnormal
+            case 2: X = (X & 0x800FFFFFFFFFFFFFull) | (0x7FCull << 52); break;      // largest that scales
+            case 3: X = (X & 0x800FFFFFFFFFFFFFull) | (0x7FDull << 52); break;      // would overflow
+            case 4: X |= 0x7FF0000000000000ull; break;                              // inf / nan
+            default: break;
+        }
+        double x = sf::from(X);
+        if (sf::scale_up_ok(x, 2)) bad += !same(sf::scale_up(x, 2), x * 4.0);
+        if ((q & 7) == 1 && (X & ~sf::SIGN) != 0) bad += sf::scale_up_ok(x, 2);  // subnormals must be refused
+        if ((q & 7) == 3) bad += sf::scale_up_ok(x, 2);
+        if (sf::pos_small(x)) bad += !sf::pos_ok(x) || x < 0.0 || x >= 0x1p1009;
+    }
+    return bad;
+}

@@ -102,3 +102,77 @@ def test_plain_mode_no_fusion(g):
     j.close()
     g.set_mode("batched")
     assert s["fused_pairs"] == 0 and s["graphs_captured"] == 0 and s["handler_calls"] == 6
+
+
+@pytest.mark.parametrize("variant", list(range(14)))
+def test_jacobi3d_variants_vs_oracle(g, variant):
+    """Every kernel variant of the 3-D loops (rows per thread x additions on the
+    FP64 unit, the rest on the integer pipe) through the program, plain
+    (separate update and stencil loops) and batched (the fused loop)."""
+    try:
+        g.force_variant(variant)
+        for n, iters in ((19, 4), (66, 3), (131, 2)):
+            e_ref, A_ref, B_ref = orc.jacobi_run(3, n, iters, 900 + n)
+            for mode in ("plain", "batched"):
+                g.set_mode(mode)
+                j = g.Jacobi(3, n, 900 + n)
+                eps = j.run(iters)
+                A, B = j.fetch()
+                j.close()
+                assert np.array_equal(eps, e_ref), (variant, n, mode)
+                assert np.array_equal(A, A_ref) and np.array_equal(B, B_ref), (variant, n, mode)
+    finally:
+        g.force_variant(-1)
+
+
+def _stencil_ref(A):
+    """(A[i-1]+A[j-1]+A[k-1]+A[k+1]+A[j+1]+A[i+1]) / 6 over the interior, float64
+    on the CPU, one IEEE operation at a time in the source order."""
+    c = A[1:-1, 1:-1, 1:-1]
+    t = A[:-2, 1:-1, 1:-1] + A[1:-1, :-2, 1:-1]
+    t = t + A[1:-1, 1:-1, :-2]
+    t = t + A[1:-1, 1:-1, 2:]
+    t = t + A[1:-1, 2:, 1:-1]
+    t = t + A[2:, 1:-1, 1:-1]
+    return t / 6.0, c
+
+
+@pytest.mark.parametrize("variant", list(range(14)))
+def test_jacobi3d_kernels_signs_and_tiny_values(g, variant):
+    """The kernels directly through the C ABI on values that take every path:
+    negative values (no integer-pipe additions for that CTA), values below
+    2^-12 and zeros (the FP64-unit fallback of the fixed-point MAX), and
+    ordinary [0, 1) values; A, Bnew and eps bit-exact against float64 on the CPU."""
+    import ctypes
+    import torch
+    L = g.runtime()
+    L.dvmhgb_jac3d_fused_items.restype = ctypes.c_long
+    n0, n1, n2 = 23, 37, 150  # row pitch 150: 16-byte aligned rows
+    LA = ctypes.c_long * 3
+    st, ext, lo, hi = LA(n1 * n2, n2, 1), LA(n0, n1, n2), LA(1, 1, 1), LA(n0 - 2, n1 - 2, n2 - 2)
+    gen = torch.Generator().manual_seed(variant)
+    A = torch.rand(n0, n1, n2, dtype=torch.float64, generator=gen)
+    B = torch.rand(n0, n1, n2, dtype=torch.float64, generator=gen)
+    B[3:9, :, :40] -= 0.5  # negative values in some tiles
+    B[12:, 20:, 64:90] *= 2.0 ** -20  # tiny values
+    A[12:, 20:, 64:70] = 0.0
+    Ad, Bd = A.cuda(), B.cuda()
+    Bnew = torch.full_like(Bd, 7.0)
+    vp = lambda t: ctypes.c_void_p(t.data_ptr())
+    items = torch.empty(L.dvmhgb_jac3d_fused_items(lo, hi, variant), dtype=torch.float64, device="cuda")
+    sp = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    assert L.dvmhgb_jac3d_fused(vp(Ad), vp(Bd), vp(Bnew), st, ext, lo, hi, vp(items), variant, sp) == 0
+    Bs = torch.full_like(Bd, 7.0)
+    assert L.dvmhgb_jac3d_stencil(vp(Bd), vp(Bs), st, ext, lo, hi, variant, sp) == 0
+    torch.cuda.synchronize()
+    # reference: update on the interior, then the stencil of the updated A
+    An = A.clone()
+    An[1:-1, 1:-1, 1:-1] = B[1:-1, 1:-1, 1:-1]
+    eps_ref = (B[1:-1, 1:-1, 1:-1] - A[1:-1, 1:-1, 1:-1]).abs().max().item()
+    s_ref, _ = _stencil_ref(An)
+    assert items.max().item() == eps_ref, variant
+    assert torch.equal(Ad.cpu(), An), variant
+    assert torch.equal(Bnew.cpu()[1:-1, 1:-1, 1:-1], s_ref), variant
+    assert torch.equal(Bnew.cpu()[0], B[0]), variant  # outside the box: B's values
+    s2, _ = _stencil_ref(B)
+    assert torch.equal(Bs.cpu()[1:-1, 1:-1, 1:-1], s2), variant

@@ -35,6 +35,13 @@ def test_add_pos_matches_host_fpu(hostlib, seed):
     assert hostlib.softfp64_check_pos(4_000_000, seed) == 0
 
 
+def test_scale_up_and_pos_small(hostlib):
+    """The exact x * 4.0 of the heat kernel and the range test of its integer SUM tree."""
+    hostlib.softfp64_check_scale.restype = ctypes.c_long
+    hostlib.softfp64_check_scale.argtypes = [ctypes.c_long, ctypes.c_uint64]
+    assert hostlib.softfp64_check_scale(2_000_000, 11) == 0
+
+
 @pytest.mark.gpu
 def test_softfp64_matches_gb300_fp64_unit():
     import __graft_entry__ as ge
