@@ -18,6 +18,9 @@ Printed as one JSON line:
              bytes 32 per cell x 510^3 cells per launch / its average duration
              from the runtime's event timing over the timed region, against the
              measured HBM copy bandwidth
+  roofline_fp64  the same kernel's 5 FP64 additions per cell against the
+             measured FP64 addition rate of the GPU (the bound of these loops:
+             2 FP64 thread-operations per clock per SM)
   cpu_baseline  the CPU port of the same loops (oracle/restate.c, OpenMP,
              static schedule over the outermost loop like the reference host
              handlers) on this machine's host cores, bounded sample
@@ -44,6 +47,7 @@ sys.path.insert(0, ROOT)
 N_DEFAULT = 512
 SEED = 20261203
 BYTES_PER_CELL = 32  # A and B each read once and written once per step
+FP64_ADDS_PER_CELL = 5  # the stencil's additions; division, MAX and |B-A| run on the integer pipe
 
 
 def peaks():
@@ -208,6 +212,10 @@ def main():
     peak, peak_kind = peaks()
     achieved = BYTES_PER_CELL * cells / (kern_ms * 1e-3) / 1e9
     value = cells / (ms * 1e-3)
+    # the stencil's five FP64 additions per cell against the measured FP64 addition rate
+    rate = ctypes.c_double(0.0)
+    fp64_peak = rate.value if rt.dvmhgb_fp64_add_rate(ctypes.byref(rate)) == 0 else None
+    fp64_achieved = FP64_ADDS_PER_CELL * cells / (kern_ms * 1e-3)
 
     # e2e: host arrays in, host arrays out, through the C ABI
     e2e_runs = 2
@@ -241,6 +249,10 @@ def main():
                          "traffic": None, "kernel": "loop_jac3d_fused_cuda (fused update+stencil, incl. its fold)",
                          "bytes_per_launch": BYTES_PER_CELL * cells, "launch_ms": kern_ms,
                          "hbm_frac_of_step": BYTES_PER_CELL * cells / (ms * 1e-3) / 1e9 / peak},
+            "roofline_fp64": {"bound": "fp64", "achieved": fp64_achieved, "peak": fp64_peak, "unit": "FP64 add/s",
+                              "frac": fp64_achieved / fp64_peak if fp64_peak else None,
+                              "ops_per_cell": FP64_ADDS_PER_CELL,
+                              "peak_kind": "measured (dvmhgb_fp64_add_rate: independent DADD chains on every SM)"},
             "clocks": ck, "e2e": e2e, "gpu_launches": st["kernel_launches"]}
     traffic = os.path.join(ROOT, "profiles", "traffic.json")
     if os.path.exists(traffic):
@@ -285,6 +297,9 @@ def extra_configs(g, stream):
         ms = e0.elapsed_time(e1) / sweeps
         s.close()
         res[mode] = {"value": (n - 2) ** 3 / (ms * 1e-3), "ms_per_sweep": ms}
+    peak, _ = peaks()
+    for r in res.values():
+        r["hbm_frac"] = r["value"] * 16 / 1e9 / peak
     out["sor3d_across_384"] = {"unit": "cell-updates/s", "bytes_per_cell": 16, **res}
     # batched uneven heat: 256 arrays, sides log-uniform in [64, 2048], 200 steps
     res = {}
@@ -306,6 +321,8 @@ def extra_configs(g, stream):
         ms = e0.elapsed_time(e1) / steps
         h.close()
         res[mode] = {"value": cells / (ms * 1e-3), "ms_per_step": ms, "wall_ms_per_step": 1000 * wall, "steps": steps}
+    for m in ("batched", "plain"):
+        res[m]["hbm_frac"] = res[m]["value"] * 16 / 1e9 / peak
     res["batched_over_plain"] = res["batched"]["value"] / res["plain"]["value"]
     out["heat_batched_256"] = {"unit": "cell-updates/s", "bytes_per_cell": 16, "cells": cells, **res}
     g.set_mode("batched")

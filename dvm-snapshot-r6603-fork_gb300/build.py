@@ -7,7 +7,7 @@
 
 Device code: nvcc -gencode arch=compute_103a,code=sm_103a -O3 -lineinfo
 -fmad=false (no FMA contraction: each cell's arithmetic is the source
-program's).  Host code of the programs: gcc -O2 -ffp-contract=off.
+program's).  Host code of the programs: gcc -O2 -ffp-contract=off -fopenmp.
 Translation units compile in parallel; nothing is rebuilt when up to date.
 """
 import concurrent.futures as cf
@@ -27,7 +27,8 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVFLAGS = ARCH + ["-O3", "-lineinfo", "-fmad=false", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-Wall",
                   "-I" + INC, "--expt-relaxed-constexpr", "-Xptxas", "-warn-spills"]
 CXXFLAGS = ["-O2", "-std=c++17", "-fPIC", "-Wall", "-I" + INC, "-I" + os.path.join(CUDA, "include")]
-CFLAGS = ["-O2", "-ffp-contract=off", "-fno-fast-math", "-fPIC", "-Wall", "-Wno-unused-variable", "-I" + INC]
+CFLAGS = ["-O2", "-ffp-contract=off", "-fno-fast-math", "-fopenmp", "-fPIC", "-Wall", "-Wno-unused-variable",
+          "-I" + INC]
 
 RUNTIME = "libdvmh_gb.so"
 WORKLOADS = "libdvmhgb_workloads.so"
@@ -82,7 +83,7 @@ def build(verbose=False):
     wl = os.path.join(LIB, WORKLOADS)
     if _newer(wl_obj + [rt], wl):
         subprocess.check_call([NVCC] + ARCH + ["-shared", "-o", wl + ".tmp"] + wl_obj +
-                              ["-L" + LIB, "-ldvmh_gb", "-lcudart", "-Xlinker", "-rpath=$ORIGIN"])
+                              ["-L" + LIB, "-ldvmh_gb", "-lcudart", "-lgomp", "-Xlinker", "-rpath=$ORIGIN"])
         os.replace(wl + ".tmp", wl)
     if verbose:
         print(rt)

@@ -657,6 +657,9 @@ __global__ void kCopyOutside(const double *__restrict__ src, double *__restrict_
 // row per thread, registers capped for three / four CTAs per SM
 constexpr int V3 = 14;
 int jtOf3(int v) { return (v >= 6 && v < 12) ? 2 : 1; }
+// the fused entry point's extra variant: the two loops as two kernels (the
+// update, then the stencil with variant UNFUSED_STN into the second buffer)
+constexpr int V3_UNFUSED = V3, UNFUSED_STN = 13;
 
 template <bool FUSED>
 void launch3(int variant, const St3Geom &g, double *A, const double *B, double *Out, const Box3 &b, double *items,
@@ -717,6 +720,7 @@ int dvmhgb_jac3d_stencil(const double *A, double *B, const long st[3], const lon
 }
 
 long dvmhgb_jac3d_fused_items(const long lo[3], const long hi[3], int native) {
+    if (native == V3_UNFUSED) return dvmhgb_jac3d_update_items(lo, hi);
     if (native < 0 || native >= V3) return -1;
     St3Geom g = st3Geom(lo, hi, TY * jtOf3(native));
     return (long)g.grid.x * g.grid.y * g.grid.z;
@@ -724,6 +728,12 @@ long dvmhgb_jac3d_fused_items(const long lo[3], const long hi[3], int native) {
 
 int dvmhgb_jac3d_fused(double *A, const double *B, double *Bnew, const long st[3], const long ext[3],
                        const long lo[3], const long hi[3], double *items, int native, void *stream) {
+    if (native == V3_UNFUSED) {
+        if (dvmhgb_jac3d_update(A, B, st, lo, hi, items, 1, stream) != 0 ||
+            dvmhgb_jac3d_stencil(A, Bnew, st, ext, lo, hi, UNFUSED_STN, stream) != 0)
+            return -1;
+        return dvmhgb_copy_outside_box(3, B, Bnew, st, ext, lo, hi, stream);
+    }
     if (native < 0 || native >= V3) return -1;
     St3Geom g = st3Geom(lo, hi, TY * jtOf3(native));
     if (!g.ok || !A || !B || !Bnew || !items || !rows16(st, 3) || !aligned16(A) || !aligned16(B) || !aligned16(Bnew))

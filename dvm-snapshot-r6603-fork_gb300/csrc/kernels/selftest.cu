@@ -70,7 +70,57 @@ __global__ void kSelftest(long n, uint64_t seed, unsigned long long *bad) {
         if (c[k]) atomicAdd(bad + k, c[k]);
 }
 
+// FP64 addition throughput: every thread runs 8 independent chains of native
+// additions (enough independent work to keep the FP64 unit busy on every SM)
+__global__ void __launch_bounds__(256) kFp64Rate(double *out, int iters) {
+    double x[8], c[8];
+    const unsigned t = blockIdx.x * blockDim.x + threadIdx.x;
+#pragma unroll
+    for (int q = 0; q < 8; q++) {
+        x[q] = 0.25 + 1e-3 * ((t * 7 + q * 13) % 97);
+        c[q] = 1e-4 * (1 + (t + q) % 31);
+    }
+    for (int it = 0; it < iters; it++) {
+#pragma unroll
+        for (int q = 0; q < 8; q++) x[q] = sf::nadd(x[q], c[q]);
+    }
+    double s = 0.0;
+#pragma unroll
+    for (int q = 0; q < 8; q++) s += x[q];
+    out[t] = s;
+}
+
 }  // namespace
+
+// Measured FP64 addition rate of this GPU (additions per second): 8 CTAs of
+// 256 threads per SM, 8 independent chains per thread, timed with CUDA events
+// after a warm-up launch.  The denominator of the FP64 roofline of the stencils.
+extern "C" int dvmhgb_fp64_add_rate(double *addsPerSecond) {
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (sms <= 0 || !addsPerSecond) return -1;
+    const int grid = sms * 8, iters = 4000;
+    double *out = nullptr;
+    if (cudaMalloc(&out, sizeof(double) * grid * 256) != cudaSuccess) return -1;
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    kFp64Rate<<<grid, 256>>>(out, 100);
+    cudaEventRecord(e0);
+    kFp64Rate<<<grid, 256>>>(out, iters);
+    cudaEventRecord(e1);
+    cudaEventSynchronize(e1);
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaError_t err = cudaGetLastError();
+    cudaFree(out);
+    if (err != cudaSuccess || ms <= 0.f) return -1;
+    *addsPerSecond = (double)grid * 256 * 8 * iters / (ms * 1e-3);
+    return 0;
+}
 
 extern "C" int dvmhgb_selftest_softfp64(long n, unsigned long long seed, long mismatches[4]) {
     unsigned long long *d = nullptr;

@@ -126,7 +126,10 @@ void copyH2D(Array *a) {
     long rows = (long)(a->helems / a->ext[a->rank - 1]);
     size_t w = a->ext[a->rank - 1] * a->esize;
     size_t dp = (a->rank == 1 ? a->ext[0] : a->dstride[a->rank - 2]) * a->esize;
-    GB_CUDA(cudaMemcpy2DAsync(a->dev, dp, a->host, w, w, rows, cudaMemcpyHostToDevice, gpu.stream));
+    if (dp == w)  // unpadded rows: one linear copy
+        GB_CUDA(cudaMemcpyAsync(a->dev, a->host, w * rows, cudaMemcpyHostToDevice, gpu.stream));
+    else
+        GB_CUDA(cudaMemcpy2DAsync(a->dev, dp, a->host, w, w, rows, cudaMemcpyHostToDevice, gpu.stream));
     stats.h2d_bytes += (long)(w * rows);
 }
 
@@ -134,7 +137,10 @@ void copyD2H(Array *a) {
     long rows = (long)(a->helems / a->ext[a->rank - 1]);
     size_t w = a->ext[a->rank - 1] * a->esize;
     size_t dp = (a->rank == 1 ? a->ext[0] : a->dstride[a->rank - 2]) * a->esize;
-    GB_CUDA(cudaMemcpy2DAsync(a->host, w, a->dev, dp, w, rows, cudaMemcpyDeviceToHost, gpu.stream));
+    if (dp == w)
+        GB_CUDA(cudaMemcpyAsync(a->host, a->dev, w * rows, cudaMemcpyDeviceToHost, gpu.stream));
+    else
+        GB_CUDA(cudaMemcpy2DAsync(a->host, w, a->dev, dp, w, rows, cudaMemcpyDeviceToHost, gpu.stream));
     stats.d2h_bytes += (long)(w * rows);
     streamSync();
 }

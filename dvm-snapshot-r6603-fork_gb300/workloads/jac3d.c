@@ -185,6 +185,7 @@ static void jac3d_xfer(DvmType *D, double *dense, int dir) {
     long n = P.n, i, j, st[3];
     double *h = (double *)dvmh_get_natural_base_C(0, D);
     wl_strides(D, 3, st);
+#pragma omp parallel for private(j) schedule(static)
     for (i = 0; i < n; i++)
         for (j = 0; j < n; j++) {
             double *row = h + i * st[0] + j * st[1], *drow = dense + (i * n + j) * n;
@@ -208,15 +209,15 @@ int wl_jac3d_fetch(double *a_out, double *b_out) {
     return 0;
 }
 
-/* Replaces A and B with caller data (NULL keeps an array) and marks the host copies actual. */
+/* Replaces A and B with caller data (NULL keeps an array) and marks the host
+ * copies actual: every element is overwritten, so the old contents are not
+ * fetched first. */
 int wl_jac3d_load(const double *a_in, const double *b_in) {
     if (a_in) {
-        dvmh_get_actual_array2_(A);
         jac3d_xfer(A, (double *)a_in, 1);
         dvmh_actual_array2_(A);
     }
     if (b_in) {
-        dvmh_get_actual_array2_(B);
         jac3d_xfer(B, (double *)b_in, 1);
         dvmh_actual_array2_(B);
     }

@@ -110,7 +110,7 @@ extern "C" void loop_jac3d_fused_cuda(DvmType refs[2], DvmType A_hdr[], DvmType 
     cudaStream_t stream;
     dvmh_loop_cuda_get_config_C(upd, 0, 0, &threads, &stream, 0);
     dvmh_loop_cuda_get_config_C(stn, 0, 0, &threads, &stream, 0);
-    const int variant = dvmhgb_loop_variant(upd, DVMHGB_JAC3D_VARIANTS, DEF_FUSED);
+    const int variant = dvmhgb_loop_variant(upd, DVMHGB_JAC3D_VARIANTS + 1, DEF_FUSED);  // + the unfused pair
     double eps, *eps_grid = 0;
     dvmh_loop_cuda_register_red_C(upd, 1, (void **)&eps_grid, 0);
     dvmh_loop_red_init_C(upd, 1, &eps, 0);

@@ -71,6 +71,9 @@ void dvmhgb_force_variant(int v);
 /* Self-test of the integer-pipe FP64 operations against the FP64 unit on n
  * random operand pairs: mismatches[0..3] = add, sub, mul, division by 6. */
 int dvmhgb_selftest_softfp64(long n, unsigned long long seed, long mismatches[4]);
+/* Measured FP64 addition throughput of the current GPU (additions/s): the
+ * FP64 roofline's denominator.  0 on success. */
+int dvmhgb_fp64_add_rate(double *addsPerSecond);
 
 /* ---- handler timing (the runtime's timing database) -----------------------
  * On: every handler execution is bracketed by CUDA events on the runtime

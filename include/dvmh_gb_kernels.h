@@ -40,7 +40,10 @@ int dvmhgb_jac3d_stencil(const double *A, double *B, const long st[3], const lon
                          const long hi[3], int native, void *stream);
 /* loops 1+2 fused (same box): reads A, B; writes A = B and Bnew = stencil(A_new)
  * into Bnew (a second buffer of B's layout), B's values outside the box copied
- * into Bnew; MAX partials, one per CTA (the count depends on the variant) */
+ * into Bnew; MAX partials, one per CTA (the count depends on the variant).
+ * Variants 0..DVMHGB_JAC3D_VARIANTS-1 as above, and DVMHGB_JAC3D_UNFUSED: the
+ * update and the stencil kernels one after the other */
+#define DVMHGB_JAC3D_UNFUSED DVMHGB_JAC3D_VARIANTS
 long dvmhgb_jac3d_fused_items(const long lo[3], const long hi[3], int native);
 int dvmhgb_jac3d_fused(double *A, const double *B, double *Bnew, const long st[3], const long ext[3],
                        const long lo[3], const long hi[3], double *items, int native, void *stream);
