@@ -156,6 +156,12 @@ def main():
     ap.add_argument("--impl", default="gb300")
     ap.add_argument("--grid", type=int, default=N_DEFAULT)
     ap.add_argument("--quick", action="store_true", help="headline only (no extra modes/configs/cpu leg)")
+    ap.add_argument("--only", choices=["jacobi3d", "sor", "heat"], default=None,
+                    help="time one workload alone (small cases for profiling): --grid is its size "
+                         "(heat: the largest side), --steps its steps or sweeps")
+    ap.add_argument("--mode", choices=["batched", "async", "plain"], default="batched", help="with --only")
+    ap.add_argument("--arrays", type=int, default=256, help="heat arrays, with --only heat")
+    ap.add_argument("--variant", type=int, default=-1, help="force a kernel variant, with --only")
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", "0"))
     if args.impl == "reference":
@@ -173,6 +179,9 @@ def main():
     g.init()
     rt = g.runtime()
     stream = torch.cuda.ExternalStream(rt.dvmhgb_stream())
+    if args.only:
+        run_only(args, g, stream)
+        return
     wl = g.workloads()
     n = args.grid
     cells = (n - 2) ** 3
@@ -275,6 +284,36 @@ def main():
                                 "sample": "%d Jacobi-3D steps at %d^3 on the host cores" % (it, n)}
     if rank == 0:
         print(json.dumps(line), flush=True)
+
+
+def run_only(args, g, stream):
+    """One workload alone, device-timed: the small cases the profiles are taken on."""
+    import torch
+    g.force_variant(args.variant)
+    g.set_mode(args.mode)
+    if args.only == "jacobi3d":
+        w = g.Jacobi(3, args.grid, SEED)
+        cells, unit = (args.grid - 2) ** 3, "step"
+    elif args.only == "sor":
+        w = g.Sor(args.grid, 1.5, SEED + 2)
+        cells, unit = (args.grid - 2) ** 3, "sweep"
+    else:
+        w = g.Heat(args.arrays, 64, args.grid, 0.2, SEED + 3)
+        cells, unit = w.cells(), "step"
+    w.run(args.warmup)
+    g.sync()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    w.run(args.steps)
+    e1.record(stream)
+    g.sync()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / args.steps
+    w.close()
+    g.force_variant(-1)
+    print(json.dumps({"workload": args.only, "grid": args.grid, "mode": args.mode, "variant": args.variant,
+                      "steps": args.steps, "ms_per_" + unit: ms, "cell-updates/s": cells / (ms * 1e-3)}), flush=True)
 
 
 def extra_configs(g, stream):

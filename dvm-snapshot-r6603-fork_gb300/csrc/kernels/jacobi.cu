@@ -804,7 +804,7 @@ int dvmhgb_jac2d_fused(double *A, const double *B, double *Bnew, const long st[2
 namespace {
 
 constexpr long NOALLOC_PARTIALS = 4096;  // maximum CTAs of one call
-__device__ __align__(256) double noallocPartials[NOALLOC_PARTIALS];
+static __device__ __align__(256) double noallocPartials[NOALLOC_PARTIALS];
 
 // eps = the largest partial (MAX is order-independent)
 __global__ void __launch_bounds__(256) kMaxPartials(const double *partials, long n, double *eps) {
