@@ -250,12 +250,14 @@ def main():
             "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic: splitmix64-seeded uniform[0,1) interior, zero boundary",
             "config": {"workload": "jacobi3d-7pt fp64 %d^3 (%d^3 interior), update+MAX, renew, stencil per step"
-                                   % (n, n - 2), "grid": n, "mode": "batched (captured graph, fused loops)",
+                                   % (n, n - 2), "grid": n, "mode": "batched (one captured graph per step, loop pair through the fusion rule)",
                        "l2": "no flush: inputs 2 x %.2f GB > 129 MB L2" % (8 * n ** 3 / 1e9),
                        "parallelism": "replicas" if args.gpus > 1 else "single GPU"},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "peak_kind": peak_kind,
-                         "traffic": None, "kernel": "loop_jac3d_fused_cuda (fused update+stencil, incl. its fold)",
+                         "traffic": None,
+                         "kernel": "loop_jac3d_fused_cuda: the update+stencil pair of the fusion rule (kUpdate with "
+                                   "fixed-point MAX, then kStencil3) in the step's captured graph",
                          "bytes_per_launch": BYTES_PER_CELL * cells, "launch_ms": kern_ms,
                          "hbm_frac_of_step": BYTES_PER_CELL * cells / (ms * 1e-3) / 1e9 / peak},
             "roofline_fp64": {"bound": "fp64", "achieved": fp64_achieved, "peak": fp64_peak, "unit": "FP64 add/s",
@@ -267,7 +269,7 @@ def main():
     if os.path.exists(traffic):
         try:
             tj = json.load(open(traffic))
-            line["roofline"]["traffic"] = tj.get("jac3d_fused_bytes_per_launch_512")
+            line["roofline"]["traffic"] = tj.get("jac3d_step_bytes_per_launch_512") if n == 512 else None
         except Exception:
             pass
 

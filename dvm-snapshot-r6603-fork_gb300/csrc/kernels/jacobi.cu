@@ -78,7 +78,7 @@ __global__ void __launch_bounds__(UPD_THREADS) kUpdate(double *A, const double *
                                                        double *items, int native) {
     __shared__ double sh[UPD_THREADS / 32];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    uint64_t mb = 0;
+    uint64_t mb = 0, qmax = 0;  // FP64-unit / integer-pipe MAX parts (native == 2: the latter)
     bool seen = false;
     const unsigned wstride = gridDim.x * (UPD_THREADS / 32);
     // UNITS units per trip: all their loads are issued before any is used
@@ -105,15 +105,30 @@ __global__ void __launch_bounds__(UPD_THREADS) kUpdate(double *A, const double *
         for (int q = 0; q < UNITS; q++) {
             if (!live[q]) continue;
             bool in0 = k0[q] >= lo2 && k0[q] <= hi2, in1 = k0[q] + 1 >= lo2 && k0[q] + 1 <= hi2;
-            if (in0) mb = sf::absmax_bits(native ? sf::nadd(b[q].x, -a[q].x) : sf::sub(b[q].x, a[q].x), mb);
-            if (in1) mb = sf::absmax_bits(native ? sf::nadd(b[q].y, -a[q].y) : sf::sub(b[q].y, a[q].y), mb);
+            bool ok = native == 2;
+            if (ok) {
+                // |B - A| exact as 64-bit fixed point for values in [2^-12, 1) (see kStencil3)
+                const uint64_t b0 = sf::q64(b[q].x, ok), a0 = sf::q64(a[q].x, ok);
+                const uint64_t b1 = sf::q64(b[q].y, ok), a1 = sf::q64(a[q].y, ok);
+                const uint64_t d0 = b0 > a0 ? b0 - a0 : a0 - b0, d1 = b1 > a1 ? b1 - a1 : a1 - b1;
+                if (ok && in0 && d0 > qmax) qmax = d0;  // only exact differences enter the maximum
+                if (ok && in1 && d1 > qmax) qmax = d1;
+            }
+            if (!ok) {  // native 0 / 1, or a value outside the fixed-point range (rare)
+                if (in0) mb = sf::absmax_bits(native ? sf::nadd(b[q].x, -a[q].x) : sf::sub(b[q].x, a[q].x), mb);
+                if (in1) mb = sf::absmax_bits(native ? sf::nadd(b[q].y, -a[q].y) : sf::sub(b[q].y, a[q].y), mb);
+            }
             seen = seen || in0 || in1;
             if (in0 && in1) st2cs(A + off[q], b[q]);
             else if (in0) A[off[q]] = b[q].x;
             else if (in1) A[off[q] + 1] = b[q].y;
         }
     }
-    double m = seen ? sf::from(mb) : -__builtin_huge_val();
+    double m = -__builtin_huge_val();
+    if (seen) {
+        const double qd = __ull2double_rn(qmax) * 0x1p-64, f = sf::from(mb);  // RN(max |b - a|), then MAX
+        m = qd > f ? qd : f;
+    }
     m = ctaMax(m, sh);
     if (threadIdx.x == 0) items[blockIdx.x] = m;
 }
@@ -387,8 +402,8 @@ __global__ void __launch_bounds__(TX *TY, MINB) kStencil3(double *A, const doubl
                 const uint64_t b0 = sf::q64(pc[r].x, ok), a0 = sf::q64(ao[r].x, ok);
                 const uint64_t b1 = sf::q64(pc[r].y, ok), a1 = sf::q64(ao[r].y, ok);
                 const uint64_t d0 = b0 > a0 ? b0 - a0 : a0 - b0, d1 = b1 > a1 ? b1 - a1 : a1 - b1;
-                if (kI0 && d0 > qmax) qmax = d0;
-                if (kI1 && d1 > qmax) qmax = d1;
+                if (ok && kI0 && d0 > qmax) qmax = d0;  // only exact differences enter the maximum
+                if (ok && kI1 && d1 > qmax) qmax = d1;
                 if (__any_sync(0xffffffffu, !ok) && !ok) {
                     if (kI0) mb = sf::absmax_bits(sf::nadd(pc[r].x, -ao[r].x), mb);
                     if (kI1) mb = sf::absmax_bits(sf::nadd(pc[r].y, -ao[r].y), mb);
@@ -729,11 +744,13 @@ long dvmhgb_jac3d_fused_items(const long lo[3], const long hi[3], int native) {
 int dvmhgb_jac3d_fused(double *A, const double *B, double *Bnew, const long st[3], const long ext[3],
                        const long lo[3], const long hi[3], double *items, int native, void *stream) {
     if (native == V3_UNFUSED) {
-        if (dvmhgb_jac3d_update(A, B, st, lo, hi, items, 1, stream) != 0 ||
+        if (dvmhgb_jac3d_update(A, B, st, lo, hi, items, 2, stream) != 0 ||
             dvmhgb_jac3d_stencil(A, Bnew, st, ext, lo, hi, UNFUSED_STN, stream) != 0)
             return -1;
-        return dvmhgb_copy_outside_box(3, B, Bnew, st, ext, lo, hi, stream);
+        // Bnew == B: the stencil wrote B in place of the second buffer (it reads only A)
+        return Bnew == B ? 0 : dvmhgb_copy_outside_box(3, B, Bnew, st, ext, lo, hi, stream);
     }
+    if (Bnew == B) return -1;  // the fused kernel reads B while it writes the next B
     if (native < 0 || native >= V3) return -1;
     St3Geom g = st3Geom(lo, hi, TY * jtOf3(native));
     if (!g.ok || !A || !B || !Bnew || !items || !rows16(st, 3) || !aligned16(A) || !aligned16(B) || !aligned16(Bnew))

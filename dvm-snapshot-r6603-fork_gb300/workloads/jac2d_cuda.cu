@@ -75,7 +75,7 @@ extern "C" void loop_jac2d_upd_cuda(DvmType *pLoopRef, DvmType A_hdr[], DvmType 
     dvmh_loop_cuda_register_red_C(loop_ref, 1, (void **)&eps_grid, 0);
     dvmh_loop_red_init_C(loop_ref, 1, &eps, 0);
     dvmh_loop_cuda_red_prepare_C(loop_ref, 1, dvmhgb_jac2d_update_items(lo, hi), 0);
-    check(dvmhgb_jac2d_update(A.base, B.base, A.st, lo, hi, eps_grid, dvmhgb_loop_variant(loop_ref, 2, 1), stream), "loop_jac2d_upd_cuda");
+    check(dvmhgb_jac2d_update(A.base, B.base, A.st, lo, hi, eps_grid, dvmhgb_loop_variant(loop_ref, 3, 2), stream), "loop_jac2d_upd_cuda");
     dvmh_loop_cuda_red_finish_C(loop_ref, 1);
 }
 

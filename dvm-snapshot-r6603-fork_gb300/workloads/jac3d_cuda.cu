@@ -19,7 +19,9 @@
 #define R 3
 // default kernel variants (v = 6 * (rows per thread - 1) + additions on the FP64 unit)
 #define DEF_STN 13   // all additions on the FP64 unit, one row a thread, four CTAs per SM
-#define DEF_FUSED 12 // the same, three CTAs per SM
+// the fused pair: the update and the stencil kernels back to back in one graph (on GB300 the loops are
+// FP64-issue bound, and the one-pass fused kernel, variant 12, is 6% slower despite its 32 vs 40 B/cell)
+#define DEF_FUSED DVMHGB_JAC3D_UNFUSED
 
 namespace {
 
@@ -74,7 +76,7 @@ extern "C" void loop_jac3d_upd_cuda(DvmType *pLoopRef, DvmType A_hdr[], DvmType 
     dvmh_loop_cuda_register_red_C(loop_ref, 1, (void **)&eps_grid, 0);
     dvmh_loop_red_init_C(loop_ref, 1, &eps, 0);
     dvmh_loop_cuda_red_prepare_C(loop_ref, 1, dvmhgb_jac3d_update_items(lo, hi), 0);
-    check(dvmhgb_jac3d_update(A.base, B.base, A.st, lo, hi, eps_grid, dvmhgb_loop_variant(loop_ref, 2, 1), stream), "loop_jac3d_upd_cuda");
+    check(dvmhgb_jac3d_update(A.base, B.base, A.st, lo, hi, eps_grid, dvmhgb_loop_variant(loop_ref, 3, 2), stream), "loop_jac3d_upd_cuda");
     dvmh_loop_cuda_red_finish_C(loop_ref, 1);
 }
 
@@ -115,7 +117,8 @@ extern "C" void loop_jac3d_fused_cuda(DvmType refs[2], DvmType A_hdr[], DvmType 
     dvmh_loop_cuda_register_red_C(upd, 1, (void **)&eps_grid, 0);
     dvmh_loop_red_init_C(upd, 1, &eps, 0);
     dvmh_loop_cuda_red_prepare_C(upd, 1, dvmhgb_jac3d_fused_items(lo, hi, variant), 0);
-    double *Bnew = (double *)dvmhgb_loop_alt_buffer(stn, B_hdr);
+    // the fused kernel writes the next B into a second buffer; the unfused pair writes B itself
+    double *Bnew = variant == DVMHGB_JAC3D_UNFUSED ? B.base : (double *)dvmhgb_loop_alt_buffer(stn, B_hdr);
     check(dvmhgb_jac3d_fused(A.base, B.base, Bnew, A.st, A.ext, lo, hi, eps_grid, variant, stream),
           "loop_jac3d_fused_cuda");
     dvmh_loop_cuda_red_finish_C(upd, 1);

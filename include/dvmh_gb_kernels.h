@@ -25,7 +25,9 @@ extern "C" {
 #endif
 
 /* ---- Jacobi 3-D (examples/Performance/jac3d_perf.c:56-73, FP64) ---- */
-/* loop 1: eps = max |B-A|, A = B over the box; MAX partials, one per CTA */
+/* loop 1: eps = max |B-A|, A = B over the box; MAX partials, one per CTA.
+ * native: 0 = |B-A| on the integer pipe (general), 1 = on the FP64 unit, 2 =
+ * exact 64-bit fixed point for values in [2^-12, 1) (FP64 unit otherwise) */
 long dvmhgb_jac3d_update_items(const long lo[3], const long hi[3]);
 int dvmhgb_jac3d_update(double *A, const double *B, const long st[3], const long lo[3], const long hi[3],
                         double *items, int native, void *stream);
@@ -42,7 +44,8 @@ int dvmhgb_jac3d_stencil(const double *A, double *B, const long st[3], const lon
  * into Bnew (a second buffer of B's layout), B's values outside the box copied
  * into Bnew; MAX partials, one per CTA (the count depends on the variant).
  * Variants 0..DVMHGB_JAC3D_VARIANTS-1 as above, and DVMHGB_JAC3D_UNFUSED: the
- * update and the stencil kernels one after the other */
+ * update and the stencil kernels one after the other (Bnew may then be B
+ * itself: the stencil reads only A; the fused variants reject Bnew == B) */
 #define DVMHGB_JAC3D_UNFUSED DVMHGB_JAC3D_VARIANTS
 long dvmhgb_jac3d_fused_items(const long lo[3], const long hi[3], int native);
 int dvmhgb_jac3d_fused(double *A, const double *B, double *Bnew, const long st[3], const long ext[3],

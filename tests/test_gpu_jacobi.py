@@ -156,6 +156,7 @@ def test_jacobi3d_kernels_signs_and_tiny_values(g, variant):
     B[3:9, :, :40] -= 0.5  # negative values in some tiles
     B[12:, 20:, 64:90] *= 2.0 ** -20  # tiny values
     A[12:, 20:, 64:70] = 0.0
+    B[5, 5, 100], A[5, 5, 100] = 0.999, 2.0 ** -40  # the largest |B - A|: A below the fixed-point range
     Ad, Bd = A.cuda(), B.cuda()
     Bnew = torch.full_like(Bd, 7.0)
     vp = lambda t: ctypes.c_void_p(t.data_ptr())
@@ -176,3 +177,38 @@ def test_jacobi3d_kernels_signs_and_tiny_values(g, variant):
     assert torch.equal(Bnew.cpu()[0], B[0]), variant  # outside the box: B's values
     s2, _ = _stencil_ref(B)
     assert torch.equal(Bs.cpu()[1:-1, 1:-1, 1:-1], s2), variant
+
+
+@pytest.mark.parametrize("native", [0, 1, 2])
+def test_jacobi3d_update_kernel_all_paths(g, native):
+    """The update loop through the C ABI: |B - A| on the integer pipe (0), the
+    FP64 unit (1) and as exact fixed point with its FP64 fallback (2), on
+    values that take every path; A and eps bit-exact against float64 on the CPU."""
+    import ctypes
+    import torch
+    L = g.runtime()
+    L.dvmhgb_jac3d_update_items.restype = ctypes.c_long
+    n0, n1, n2 = 21, 33, 140
+    LA = ctypes.c_long * 3
+    st, lo, hi = LA(n1 * n2, n2, 1), LA(1, 1, 1), LA(n0 - 2, n1 - 2, n2 - 2)
+    gen = torch.Generator().manual_seed(40 + native)
+    A = torch.rand(n0, n1, n2, dtype=torch.float64, generator=gen)
+    B = torch.rand(n0, n1, n2, dtype=torch.float64, generator=gen)
+    B[2:5, :, :30] -= 0.7   # negative values
+    A[10:, 5:9, 40:70] *= 2.0 ** -30  # below the fixed-point range
+    B[6, 7, 8] = 0.0
+    B[12, 20, 50], A[12, 20, 50] = 0.9999, 2.0 ** -40  # the largest |B - A|, A out of the fixed-point range
+    for case in range(2):
+        if case == 1:  # the largest difference among ordinary values only
+            A, B = A.abs() % 1.0, B.abs() % 1.0
+        Ad, Bd = A.cuda(), B.cuda()
+        items = torch.empty(L.dvmhgb_jac3d_update_items(lo, hi), dtype=torch.float64, device="cuda")
+        vp = lambda t: ctypes.c_void_p(t.data_ptr())
+        sp = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+        assert L.dvmhgb_jac3d_update(vp(Ad), vp(Bd), st, lo, hi, vp(items), native, sp) == 0
+        torch.cuda.synchronize()
+        eps_ref = (B[1:-1, 1:-1, 1:-1] - A[1:-1, 1:-1, 1:-1]).abs().max().item()
+        An = A.clone()
+        An[1:-1, 1:-1, 1:-1] = B[1:-1, 1:-1, 1:-1]
+        assert items.max().item() == eps_ref, (native, case)
+        assert torch.equal(Ad.cpu(), An), (native, case)
