@@ -107,6 +107,35 @@ class Clocks:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
+class Replicas:
+    """One process per GPU running an independent replica of the workload (the
+    path does not shard).  A gloo group carries only timing: every timed region
+    is bracketed by barriers and its time is the maximum over the ranks; the
+    whole-job value is the units of all ranks divided by that time."""
+
+    def __init__(self):
+        self.world = int(os.environ.get("WORLD_SIZE", "1"))
+        self.rank = int(os.environ.get("RANK", "0"))
+        if self.world > 1:
+            import torch.distributed as dist
+            if not dist.is_initialized():
+                dist.init_process_group("gloo", init_method="env://", rank=self.rank, world_size=self.world)
+
+    def barrier(self):
+        if self.world > 1:
+            import torch.distributed as dist
+            dist.barrier()
+
+    def max(self, x):
+        if self.world == 1:
+            return x
+        import torch
+        import torch.distributed as dist
+        t = torch.tensor([float(x)], dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        return float(t.item())
+
+
 def cpu_port_rate(n, seconds=10.0, max_iters=40, threads=None):
     """Jacobi-3D steps of the CPU port on the host cores: (cell-updates/s, iters, threads)."""
     from oracle import orc
@@ -163,7 +192,7 @@ def main():
     ap.add_argument("--arrays", type=int, default=256, help="heat arrays, with --only heat")
     ap.add_argument("--variant", type=int, default=-1, help="force a kernel variant, with --only")
     args = ap.parse_args()
-    rank = int(os.environ.get("RANK", "0"))
+    rank = int(os.environ.get("RANK", "0"))  # under torchrun; --impl reference runs on rank 0 only
     if args.impl == "reference":
         if rank == 0:
             run_reference(args)
@@ -185,6 +214,7 @@ def main():
     wl = g.workloads()
     n = args.grid
     cells = (n - 2) ** 3
+    reps = Replicas()
 
     def timed_run(mode, steps, warmup, clocks=None):
         g.set_mode(mode)
@@ -197,13 +227,15 @@ def main():
         if clocks:
             clocks.start()
         torch.cuda.synchronize()
+        reps.barrier()
         e0.record(stream)
         j.run(steps)
         e1.record(stream)
         g.sync()
         torch.cuda.synchronize()
+        reps.barrier()
         ck = clocks.stop() if clocks else None
-        ms = e0.elapsed_time(e1) / steps
+        ms = reps.max(e0.elapsed_time(e1) / steps)  # the slowest replica
         st = g.stats()
         j.close()
         return ms, st, ck
@@ -220,7 +252,7 @@ def main():
     kern_ms = tot.value / max(cnt.value, 1)
     peak, peak_kind = peaks()
     achieved = BYTES_PER_CELL * cells / (kern_ms * 1e-3) / 1e9
-    value = cells / (ms * 1e-3)
+    value = reps.world * cells / (ms * 1e-3)  # whole job: every replica's cells
     # the stencil's five FP64 additions per cell against the measured FP64 addition rate
     rate = ctypes.c_double(0.0)
     fp64_peak = rate.value if rt.dvmhgb_fp64_add_rate(ctypes.byref(rate)) == 0 else None
@@ -233,14 +265,16 @@ def main():
     A0, B0 = j.fetch()
     j.run(3)  # graphs captured
     g.sync()
+    torch.cuda.synchronize()
+    reps.barrier()
     t0 = time.time()
     for _ in range(e2e_runs):
         j.load(A0, B0)
         j.run(args.steps)
         A, B = j.fetch()
-    dt = time.time() - t0
+    dt = reps.max(time.time() - t0)
     j.close()
-    e2e = {"value": cells * args.steps * e2e_runs / dt, "unit": "cell-updates/s",
+    e2e = {"value": reps.world * cells * args.steps * e2e_runs / dt, "unit": "cell-updates/s",
            "h2d_bytes_per_step": int((2 * 8 * n ** 3 + 8 * args.steps) / args.steps),
            "d2h_bytes_per_step": int((2 * 8 * n ** 3 + 8 * args.steps) / args.steps),
            "note": "per run: load A,B from pinned host memory, %d steps, read A,B back" % args.steps}
@@ -273,13 +307,16 @@ def main():
         except Exception:
             pass
 
-    if not args.quick and rank == 0:
+    if not args.quick:
+        # the other modes on every replica (collective timing, whole-job values)
         modes = {}
         for mode in ("plain", "async"):
             mms, _, _ = timed_run(mode, min(args.steps, 20), 2)
-            modes[mode] = {"value": cells / (mms * 1e-3), "ms_per_step": mms}
+            modes[mode] = {"value": reps.world * cells / (mms * 1e-3), "ms_per_step": mms}
         modes["batched"] = {"value": value, "ms_per_step": ms}
         line["modes"] = modes
+    if not args.quick and rank == 0:
+        # secondary workloads and the CPU baseline: rank 0 alone, no collective
         line["configs"] = extra_configs(g, stream)
         v, it, thr = cpu_port_rate(n)
         line["cpu_baseline"] = {"value": v, "unit": "cell-updates/s", "cores": thr, "kind": "port",
