@@ -291,7 +291,8 @@ def main():
                          "frac": achieved / peak, "peak_kind": peak_kind,
                          "traffic": None,
                          "kernel": "loop_jac3d_fused_cuda: the update+stencil pair of the fusion rule (kUpdate with "
-                                   "fixed-point MAX, then kStencil3) in the step's captured graph",
+                                   "fixed-point MAX, kStencil3) overlapped in 8 chunks of planes on two streams, "
+                                   "in the step's captured graph",
                          "bytes_per_launch": BYTES_PER_CELL * cells, "launch_ms": kern_ms,
                          "hbm_frac_of_step": BYTES_PER_CELL * cells / (ms * 1e-3) / 1e9 / peak},
             "roofline_fp64": {"bound": "fp64", "achieved": fp64_achieved, "peak": fp64_peak, "unit": "FP64 add/s",

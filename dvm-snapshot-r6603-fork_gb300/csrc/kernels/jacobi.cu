@@ -675,6 +675,12 @@ int jtOf3(int v) { return (v >= 6 && v < 12) ? 2 : 1; }
 // the fused entry point's extra variant: the two loops as two kernels (the
 // update, then the stencil with variant UNFUSED_STN into the second buffer)
 constexpr int V3_UNFUSED = V3, UNFUSED_STN = 13;
+// ... and the pair overlapped (V3_OVERLAP): the HBM-bound update and the
+// FP64-bound stencil in OVL_CHUNKS chunks of planes, the updates on the caller's
+// stream, the stencils on a second stream of the library; stencil chunk q waits
+// for update chunk q+1 (it reads A up to the first plane of the next chunk),
+// and nothing an update reads is written by a stencil running beside it
+constexpr int V3_OVERLAP = V3 + 1, OVL_CHUNKS = 8;
 
 template <bool FUSED>
 void launch3(int variant, const St3Geom &g, double *A, const double *B, double *Out, const Box3 &b, double *items,
@@ -734,8 +740,71 @@ int dvmhgb_jac3d_stencil(const double *A, double *B, const long st[3], const lon
     return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }
 
+// plane range of chunk q of K over [lo0, hi0]
+void ovlChunk(const long lo[3], const long hi[3], int q, int K, long clo[3], long chi[3]) {
+    const long n = hi[0] - lo[0] + 1;
+    for (int d = 0; d < 3; d++) clo[d] = lo[d], chi[d] = hi[d];
+    clo[0] = lo[0] + n * q / K;
+    chi[0] = lo[0] + n * (q + 1) / K - 1;
+}
+
+int ovlCount(const long lo[3], const long hi[3]) {
+    const long n = hi[0] - lo[0] + 1;
+    return (int)(n < OVL_CHUNKS ? n : OVL_CHUNKS);
+}
+
+long ovlItems(const long lo[3], const long hi[3]) {
+    const int K = ovlCount(lo, hi);
+    long total = 0;
+    for (int q = 0; q < K; q++) {
+        long clo[3], chi[3];
+        ovlChunk(lo, hi, q, K, clo, chi);
+        total += dvmhgb_jac3d_update_items(clo, chi);
+    }
+    return total;
+}
+
+// the second stream and the events of the overlapped pair, per device (created
+// on the first use on that device)
+constexpr int OVL_DEVICES = 64;
+struct Ovl {
+    bool ready = false;
+    cudaStream_t s2 = nullptr;
+    cudaEvent_t ev[OVL_CHUNKS + 1] = {};
+};
+Ovl ovlState[OVL_DEVICES];
+
+int runOverlap(double *A, const double *B, const long st[3], const long ext[3], const long lo[3], const long hi[3],
+               double *items, cudaStream_t s1) {
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= OVL_DEVICES) return -1;
+    Ovl &o = ovlState[dev];
+    if (!o.ready) {
+        if (cudaStreamCreateWithFlags(&o.s2, cudaStreamNonBlocking) != cudaSuccess) return -1;
+        for (auto &e : o.ev)
+            if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) return -1;
+        o.ready = true;
+    }
+    const int K = ovlCount(lo, hi);
+    long clo[OVL_CHUNKS][3], chi[OVL_CHUNKS][3];
+    for (int q = 0; q < K; q++) ovlChunk(lo, hi, q, K, clo[q], chi[q]);
+    double *it = items;
+    for (int q = 0; q < K; q++) {  // the updates, in order, on the caller's stream
+        if (dvmhgb_jac3d_update(A, B, st, clo[q], chi[q], it, 2, s1) != 0) return -1;
+        it += dvmhgb_jac3d_update_items(clo[q], chi[q]);
+        if (cudaEventRecord(o.ev[q], s1) != cudaSuccess) return -1;
+    }
+    for (int q = 0; q < K; q++) {  // the stencils on the second stream, each after the update it reads
+        if (cudaStreamWaitEvent(o.s2, o.ev[q + 1 < K ? q + 1 : K - 1], 0) != cudaSuccess) return -1;
+        if (dvmhgb_jac3d_stencil(A, (double *)B, st, ext, clo[q], chi[q], UNFUSED_STN, o.s2) != 0) return -1;
+    }
+    if (cudaEventRecord(o.ev[OVL_CHUNKS], o.s2) != cudaSuccess) return -1;
+    return cudaStreamWaitEvent(s1, o.ev[OVL_CHUNKS], 0) == cudaSuccess ? 0 : -1;  // join
+}
+
 long dvmhgb_jac3d_fused_items(const long lo[3], const long hi[3], int native) {
     if (native == V3_UNFUSED) return dvmhgb_jac3d_update_items(lo, hi);
+    if (native == V3_OVERLAP) return ovlItems(lo, hi);
     if (native < 0 || native >= V3) return -1;
     St3Geom g = st3Geom(lo, hi, TY * jtOf3(native));
     return (long)g.grid.x * g.grid.y * g.grid.z;
@@ -749,6 +818,10 @@ int dvmhgb_jac3d_fused(double *A, const double *B, double *Bnew, const long st[3
             return -1;
         // Bnew == B: the stencil wrote B in place of the second buffer (it reads only A)
         return Bnew == B ? 0 : dvmhgb_copy_outside_box(3, B, Bnew, st, ext, lo, hi, stream);
+    }
+    if (native == V3_OVERLAP) {
+        if (Bnew != B || !A || !B || !items || !rows16(st, 3) || !aligned16(A) || !aligned16(B)) return -1;
+        return runOverlap(A, B, st, ext, lo, hi, items, (cudaStream_t)stream);
     }
     if (Bnew == B) return -1;  // the fused kernel reads B while it writes the next B
     if (native < 0 || native >= V3) return -1;

@@ -19,9 +19,10 @@
 #define R 3
 // default kernel variants (v = 6 * (rows per thread - 1) + additions on the FP64 unit)
 #define DEF_STN 13   // all additions on the FP64 unit, one row a thread, four CTAs per SM
-// the fused pair: the update and the stencil kernels back to back in one graph (on GB300 the loops are
-// FP64-issue bound, and the one-pass fused kernel, variant 12, is 6% slower despite its 32 vs 40 B/cell)
-#define DEF_FUSED DVMHGB_JAC3D_UNFUSED
+// the fused pair: the update and the stencil kernels overlapped in chunks of planes (on GB300 the stencil is
+// FP64-issue bound and the update HBM bound; the one-pass fused kernel, variant 12, is 11% slower despite its
+// 32 vs 40 B/cell, the two kernels back to back 5%)
+#define DEF_FUSED DVMHGB_JAC3D_OVERLAP
 
 namespace {
 
@@ -112,13 +113,13 @@ extern "C" void loop_jac3d_fused_cuda(DvmType refs[2], DvmType A_hdr[], DvmType 
     cudaStream_t stream;
     dvmh_loop_cuda_get_config_C(upd, 0, 0, &threads, &stream, 0);
     dvmh_loop_cuda_get_config_C(stn, 0, 0, &threads, &stream, 0);
-    const int variant = dvmhgb_loop_variant(upd, DVMHGB_JAC3D_VARIANTS + 1, DEF_FUSED);  // + the unfused pair
+    const int variant = dvmhgb_loop_variant(upd, DVMHGB_JAC3D_VARIANTS + 2, DEF_FUSED);  // + the pair, unfused or overlapped
     double eps, *eps_grid = 0;
     dvmh_loop_cuda_register_red_C(upd, 1, (void **)&eps_grid, 0);
     dvmh_loop_red_init_C(upd, 1, &eps, 0);
     dvmh_loop_cuda_red_prepare_C(upd, 1, dvmhgb_jac3d_fused_items(lo, hi, variant), 0);
     // the fused kernel writes the next B into a second buffer; the unfused pair writes B itself
-    double *Bnew = variant == DVMHGB_JAC3D_UNFUSED ? B.base : (double *)dvmhgb_loop_alt_buffer(stn, B_hdr);
+    double *Bnew = variant >= DVMHGB_JAC3D_UNFUSED ? B.base : (double *)dvmhgb_loop_alt_buffer(stn, B_hdr);
     check(dvmhgb_jac3d_fused(A.base, B.base, Bnew, A.st, A.ext, lo, hi, eps_grid, variant, stream),
           "loop_jac3d_fused_cuda");
     dvmh_loop_cuda_red_finish_C(upd, 1);

@@ -47,6 +47,11 @@ int dvmhgb_jac3d_stencil(const double *A, double *B, const long st[3], const lon
  * update and the stencil kernels one after the other (Bnew may then be B
  * itself: the stencil reads only A; the fused variants reject Bnew == B) */
 #define DVMHGB_JAC3D_UNFUSED DVMHGB_JAC3D_VARIANTS
+/* DVMHGB_JAC3D_OVERLAP: the pair in 8 chunks of planes, the updates on
+ * `stream`, the stencils on a second stream of the library (stencil chunk k
+ * after update chunk k+1), joined back into `stream`, so that the HBM-bound
+ * update runs beside the FP64-bound stencil; Bnew must be B */
+#define DVMHGB_JAC3D_OVERLAP (DVMHGB_JAC3D_VARIANTS + 1)
 long dvmhgb_jac3d_fused_items(const long lo[3], const long hi[3], int native);
 int dvmhgb_jac3d_fused(double *A, const double *B, double *Bnew, const long st[3], const long ext[3],
                        const long lo[3], const long hi[3], double *items, int native, void *stream);

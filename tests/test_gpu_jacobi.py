@@ -104,7 +104,7 @@ def test_plain_mode_no_fusion(g):
     assert s["fused_pairs"] == 0 and s["graphs_captured"] == 0 and s["handler_calls"] == 6
 
 
-@pytest.mark.parametrize("variant", list(range(15)))
+@pytest.mark.parametrize("variant", list(range(16)))
 def test_jacobi3d_variants_vs_oracle(g, variant):
     """Every kernel variant of the 3-D loops (rows per thread x additions on the
     FP64 unit, the rest on the integer pipe) through the program, plain
