@@ -475,86 +475,88 @@ void launchRedFold(int op, int vtype, long count, long elemCount, const void *it
 // tree (as kFold does), block results are kept in shared memory and folded by
 // the pairwise tree again -- the same tree as the multi-pass fold, so the
 // result is identical -- then combined with the initial value.
-__global__ void __launch_bounds__(FOLD_THREADS) kFoldSeg(const FoldJob *jobs) {
-    __shared__ double sv[FOLD_SPAN];
-    __shared__ long si[FOLD_SPAN];
-    __shared__ double bv[FOLD_SPAN];
-    __shared__ long bi[FOLD_SPAN];
-    const FoldJob &J = jobs[blockIdx.x];
-    const int op = J.op;
-    const bool loc = (op == rf_MINLOC || op == rf_MAXLOC);
-    const double ident = identityOf<double>(op);
-    const double *items = (const double *)J.items;
-    const long nblk = (J.count + FOLD_SPAN - 1) / FOLD_SPAN;
-    for (long blk = 0; blk < nblk; blk++) {
-        for (int h = 0; h < 2; h++) {
-            long i = blk * FOLD_SPAN + h * FOLD_THREADS + threadIdx.x;
-            bool in = i < J.count;
-            sv[h * FOLD_THREADS + threadIdx.x] = in ? items[i] : ident;
-            si[h * FOLD_THREADS + threadIdx.x] = in ? i : -1;
-        }
-        __syncthreads();
-        for (int w = 1; w < FOLD_SPAN; w <<= 1) {
-            int pairs = FOLD_SPAN / (2 * w);
-            for (int p = threadIdx.x; p < pairs; p += FOLD_THREADS) {
-                int a = p * 2 * w, b = a + w;
-                double d = sv[a];
-                if (loc) {
-                    bool take = (si[a] < 0 && si[b] >= 0) || (si[b] >= 0 && combine<double>(op, d, sv[b]));
-                    if (take) {
-                        sv[a] = sv[b];
-                        si[a] = si[b];
-                    }
-                } else {
-                    combine<double>(op, d, sv[b]);
-                    sv[a] = d;
-                }
-            }
-            __syncthreads();
-        }
-        if (threadIdx.x == 0) {
-            bv[blk] = sv[0];
-            bi[blk] = si[0];
-        }
-        __syncthreads();
-    }
-    // tree over the block results (padded with the identity)
-    for (int h = 0; h < 2; h++) {
-        int q = h * FOLD_THREADS + threadIdx.x;
-        if (q >= nblk) {
-            bv[q] = ident;
-            bi[q] = -1;
-        }
-    }
-    __syncthreads();
+// pairwise tree over v[0..FOLD_SPAN) (and the item indices vi for LOC ops) in
+// shared memory; the result is left in v[0], vi[0]
+__device__ void foldSpan(int op, bool loc, double *v, long *vi) {
     for (int w = 1; w < FOLD_SPAN; w <<= 1) {
         int pairs = FOLD_SPAN / (2 * w);
         for (int p = threadIdx.x; p < pairs; p += FOLD_THREADS) {
             int a = p * 2 * w, b = a + w;
-            double d = bv[a];
+            double d = v[a];
             if (loc) {
-                bool take = (bi[a] < 0 && bi[b] >= 0) || (bi[b] >= 0 && combine<double>(op, d, bv[b]));
+                bool take = (vi[a] < 0 && vi[b] >= 0) || (vi[b] >= 0 && combine<double>(op, d, v[b]));
                 if (take) {
-                    bv[a] = bv[b];
-                    bi[a] = bi[b];
+                    v[a] = v[b];
+                    vi[a] = vi[b];
                 }
             } else {
-                combine<double>(op, d, bv[b]);
-                bv[a] = d;
+                combine<double>(op, d, v[b]);
+                v[a] = d;
             }
         }
         __syncthreads();
     }
+}
+
+// pass 1: one CTA per 1024-item block of every job (CTAs of all jobs at once)
+__global__ void __launch_bounds__(FOLD_THREADS) kFoldSegBlocks(const FoldJob *jobs, int njobs, double *bv, long *bi) {
+    __shared__ double sv[FOLD_SPAN];
+    __shared__ long si[FOLD_SPAN];
+    const long gb = blockIdx.x;
+    int lo = 0, hi = njobs - 1;  // the job whose blocks hold gb: last blockBase <= gb
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (jobs[mid].blockBase <= gb) lo = mid;
+        else hi = mid - 1;
+    }
+    const FoldJob &J = jobs[lo];
+    const int op = J.op;
+    const bool loc = (op == rf_MINLOC || op == rf_MAXLOC);
+    const double ident = identityOf<double>(op);
+    const double *items = (const double *)J.items;
+    const long blk = gb - J.blockBase;
+    for (int h = 0; h < 2; h++) {
+        long i = blk * FOLD_SPAN + h * FOLD_THREADS + threadIdx.x;
+        bool in = i < J.count;
+        sv[h * FOLD_THREADS + threadIdx.x] = in ? items[i] : ident;
+        si[h * FOLD_THREADS + threadIdx.x] = in ? i : -1;
+    }
+    __syncthreads();
+    foldSpan(op, loc, sv, si);
+    if (threadIdx.x == 0) {
+        bv[gb] = sv[0];
+        bi[gb] = si[0];
+    }
+}
+
+// pass 2: one CTA per job, the pairwise tree over its block results (padded
+// with the identity) -- with pass 1 the same tree as the multi-pass fold --
+// then the combination with the initial value
+__global__ void __launch_bounds__(FOLD_THREADS) kFoldSegFinal(const FoldJob *jobs, const double *bv, const long *bi) {
+    __shared__ double sv[FOLD_SPAN];
+    __shared__ long si[FOLD_SPAN];
+    const FoldJob &J = jobs[blockIdx.x];
+    const int op = J.op;
+    const bool loc = (op == rf_MINLOC || op == rf_MAXLOC);
+    const double ident = identityOf<double>(op);
+    const long nblk = (J.count + FOLD_SPAN - 1) / FOLD_SPAN;
+    for (int h = 0; h < 2; h++) {
+        const int q = h * FOLD_THREADS + threadIdx.x;
+        sv[q] = q < nblk ? bv[J.blockBase + q] : ident;
+        si[q] = q < nblk ? bi[J.blockBase + q] : -1;
+    }
+    __syncthreads();
+    foldSpan(op, loc, sv, si);
     if (threadIdx.x == 0) {
         double *dst = (double *)J.dst;
         double init = dst[0];
         double r = (op == rf_SUM) ? 0.0 : (op == rf_PROD ? 1.0 : init);
-        long ri = bi[0];
+        long ri = si[0];
         bool fromLoop = false;
         if (loc) {
-            if (ri >= 0) fromLoop = combine<double>(op, r, bv[0]);
+            if (ri >= 0) fromLoop = combine<double>(op, r, sv[0]);
         } else {
-            combine<double>(op, r, bv[0]);
+            combine<double>(op, r, sv[0]);
             combine<double>(op, r, init);
         }
         dst[0] = r;
@@ -575,11 +577,22 @@ void launchRedFoldBatch(const std::vector<FoldJob> &jobs, cudaStream_t s, std::v
     FoldJob *h = (FoldJob *)hostAlloc(bytes);
     hostScratch.push_back(h);
     memcpy(h, jobs.data(), bytes);
+    long blocks = 0;  // 1024-item blocks of all jobs
+    for (size_t q = 0; q < jobs.size(); q++) {
+        h[q].blockBase = blocks;
+        blocks += (h[q].count + FOLD_SPAN - 1) / FOLD_SPAN;
+    }
+    GB_INTERNAL(blocks < (1L << 31), "reduction batch too large");
     FoldJob *d = (FoldJob *)devAlloc(bytes);
     devScratch.push_back(d);
+    double *bv = (double *)devAlloc(sizeof(double) * (blocks > 0 ? blocks : 1));
+    long *bi = (long *)devAlloc(sizeof(long) * (blocks > 0 ? blocks : 1));
+    devScratch.push_back(bv);
+    devScratch.push_back(bi);
     GB_CUDA(cudaMemcpyAsync(d, h, bytes, cudaMemcpyHostToDevice, s));
-    kFoldSeg<<<(unsigned)jobs.size(), FOLD_THREADS, 0, s>>>(d);
-    dvmhgb_count_launches(1);
+    if (blocks > 0) kFoldSegBlocks<<<(unsigned)blocks, FOLD_THREADS, 0, s>>>(d, (int)jobs.size(), bv, bi);
+    kFoldSegFinal<<<(unsigned)jobs.size(), FOLD_THREADS, 0, s>>>(d, bv, bi);
+    dvmhgb_count_launches(2);
     GB_CUDA(cudaGetLastError());
 }
 
