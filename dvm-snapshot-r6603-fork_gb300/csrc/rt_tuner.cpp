@@ -20,6 +20,7 @@
 #include <cstring>
 #include <map>
 #include <unordered_map>
+#include <vector>
 
 #include "rt.h"
 #include "../../include/dvmh_gb_kernels.h"
@@ -96,21 +97,47 @@ static const int BLOCKS[][3] = {{32, 1, 1},  {64, 1, 1},  {128, 1, 1}, {256, 1, 
                                 {32, 4, 2},  {32, 8, 2},  {32, 2, 4},  {16, 8, 2},  {64, 2, 2},  {32, 4, 4},
                                 {16, 4, 4},  {8, 8, 4},   {64, 4, 2},  {128, 2, 2}};
 
+// The reference's default block for a loop of this rank (loop.cpp:1464-1485).
+static void defaultFor(int rank, int b[3]) {
+    b[0] = rank == 1 ? 256 : 32;
+    b[1] = rank == 1 ? 1 : (rank == 2 ? 8 : 4);
+    b[2] = rank >= 3 ? 2 : 1;
+}
+
+// Every launchable (block, elements per thread, axis on x) of the loop; when
+// there are more than maxOut, an evenly spread subset of them (so that every
+// kind of block stays represented), always with the reference's default block.
 static int candidates(const dvmhgb_synth_loop *L, dvmhgb_synth_cand *out, int maxOut) {
-    int n = 0;
+    std::vector<dvmhgb_synth_cand> all;
+    int dflt = -1, db[3];
+    defaultFor(L->rank, db);
     for (const auto &b : BLOCKS) {
         if (b[1] > 1 && L->rank < 2) continue;
         if (b[2] > 1 && L->rank < 3 && !L->across) continue;
-        for (int ept = 1; ept <= 2; ept++)
+        // elements per thread 1, 2 (and 4 for rank-1 loops, whose block has one axis: 16+ candidates each)
+        for (int ept = 1; ept <= (L->rank == 1 ? 4 : 2); ept *= 2)
             for (int xin = 1; xin >= 0; xin--) {
                 if (!xin && (L->rank == 1 || L->across)) continue;
                 dvmhgb_synth_cand c{b[0], b[1], b[2], xin, ept};
                 if (dvmhgb_synth_items(L, &c) < 0) continue;
-                if (n < maxOut) out[n] = c;
-                n++;
+                if (b[0] == db[0] && b[1] == db[1] && b[2] == db[2] && xin == 1 && ept == 1) dflt = (int)all.size();
+                all.push_back(c);
             }
     }
-    return std::min(n, maxOut);
+    const int n = (int)all.size();
+    if (maxOut <= 0) return 0;
+    if (n <= maxOut) {
+        for (int q = 0; q < n; q++) out[q] = all[q];
+        return n;
+    }
+    bool hasDflt = false;
+    for (int q = 0; q < maxOut; q++) {
+        const int src = (int)((long)q * n / maxOut);
+        out[q] = all[src];
+        hasDflt = hasDflt || src == dflt;
+    }
+    if (dflt >= 0 && !hasDflt) out[(int)((long)dflt * maxOut / n)] = all[dflt];  // in its own neighbourhood
+    return maxOut;
 }
 
 static float lg(double v) { return (float)std::log2(v > 1 ? v : 1); }
