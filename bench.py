@@ -11,9 +11,11 @@ configuration's 50 iterations.
 Printed as one JSON line:
   value      cell-updates/s, device-timed (CUDA events on the runtime's stream),
              arrays resident in HBM (2 x 1.07 GB, larger than L2: no flush needed)
-  e2e        the same metric through the C ABI from host arrays: every run loads
-             A and B from pinned host memory (H2D), runs the steps, reads A and B
-             back (D2H); bytes per step = those copies / steps
+  e2e        the same metric through the C ABI from host arrays: every run
+             declares the program's pinned host copies of A and B current
+             (dvmh_actual_array2_: uploaded by the first step), runs the steps,
+             reads A and B back (dvmh_get_actual_array2_); bytes per step =
+             those copies / steps
   roofline   dominant kernel (the fused update+stencil handler): algorithmic
              bytes 32 per cell x 510^3 cells per launch / its average duration
              from the runtime's event timing over the timed region, against the
@@ -262,22 +264,23 @@ def main():
     e2e_runs = 2
     g.set_mode("batched")
     j = g.Jacobi(3, n, SEED)
-    A0, B0 = j.fetch()
     j.run(3)  # graphs captured
+    j.pull()
     g.sync()
     torch.cuda.synchronize()
     reps.barrier()
     t0 = time.time()
     for _ in range(e2e_runs):
-        j.load(A0, B0)
+        j.push()  # the program's pinned host arrays are the input: uploaded by the first step
         j.run(args.steps)
-        A, B = j.fetch()
+        j.pull()  # and the output: get_actual of A and B
     dt = reps.max(time.time() - t0)
     j.close()
     e2e = {"value": reps.world * cells * args.steps * e2e_runs / dt, "unit": "cell-updates/s",
            "h2d_bytes_per_step": int((2 * 8 * n ** 3 + 8 * args.steps) / args.steps),
            "d2h_bytes_per_step": int((2 * 8 * n ** 3 + 8 * args.steps) / args.steps),
-           "note": "per run: load A,B from pinned host memory, %d steps, read A,B back" % args.steps}
+           "note": "per run: A,B uploaded from the program's pinned host arrays (actual), %d steps, "
+                   "A,B read back (get_actual)" % args.steps}
 
     line = {"metric": "cell-updates/s", "value": value, "unit": "cell-updates/s", "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,

@@ -157,6 +157,14 @@ class Jacobi:
         assert self.rank == 3
         self.w.wl_jac3d_load(P(A) if A is not None else None, P(B) if B is not None else None)
 
+    def push(self):
+        """Host copies of A and B declared current: the next step uploads them (3-D only)."""
+        self.w.wl_jac3d_push()
+
+    def pull(self):
+        """A and B made current on the host again (get_actual, 3-D only)."""
+        self.w.wl_jac3d_pull()
+
     def close(self):
         getattr(self.w, "wl_%s_teardown" % self.p)()
 

@@ -224,6 +224,19 @@ int wl_jac3d_load(const double *a_in, const double *b_in) {
     return 0;
 }
 
+/* The program's own host arrays as the data source and sink: declares the host
+ * copies of A and B current (the next region uploads them) ... */
+void wl_jac3d_push(void) {
+    dvmh_actual_array2_(A);
+    dvmh_actual_array2_(B);
+}
+
+/* ... and makes them current again from the device (get_actual). */
+void wl_jac3d_pull(void) {
+    dvmh_get_actual_array2_(A);
+    dvmh_get_actual_array2_(B);
+}
+
 void wl_jac3d_teardown(void) {
     dvmh_array_free_C(B);
     dvmh_array_free_C(A);
