@@ -122,6 +122,8 @@ extern dvmhgb_stats_t stats;
 
 // Dense host layout <-> device layout whose innermost rows are padded: one 2-D
 // copy (rows = product of the outer extents).
+// Uploads read the program's own (pinned) host array: they complete before
+// returning, so that the program may write the host data again right after.
 void copyH2D(Array *a) {
     long rows = (long)(a->helems / a->ext[a->rank - 1]);
     size_t w = a->ext[a->rank - 1] * a->esize;
@@ -131,6 +133,7 @@ void copyH2D(Array *a) {
     else
         GB_CUDA(cudaMemcpy2DAsync(a->dev, dp, a->host, w, w, rows, cudaMemcpyHostToDevice, gpu.stream));
     stats.h2d_bytes += (long)(w * rows);
+    streamSync();
 }
 
 void copyD2H(Array *a) {
@@ -187,7 +190,10 @@ static void copyBox(Array *a, const long lo[], const long hi[], bool toDev) {
     else stats.d2h_bytes += cells * (long)a->esize;
 }
 
-void copyBoxH2D(Array *a, const long lo[], const long hi[]) { copyBox(a, lo, hi, true); }
+void copyBoxH2D(Array *a, const long lo[], const long hi[]) {
+    copyBox(a, lo, hi, true);
+    streamSync();  // the box is read from the program's host array: done before the program may change it
+}
 void copyBoxD2H(Array *a, const long lo[], const long hi[]) {
     copyBox(a, lo, hi, false);
     streamSync();

@@ -237,6 +237,35 @@ void wl_jac3d_pull(void) {
     dvmh_get_actual_array2_(B);
 }
 
+/* Box [lo, hi] of A (which = 0) or B (which = 1) and its dense copy box_io
+ * (row-major, innermost last).  get: makes the box current on the host
+ * (dvmh_get_actual_subarray_C) and copies it out; put: writes box_io into the
+ * host array and declares the box current there (dvmh_actual_subarray_C). */
+static DvmType *pick(int which) { return which ? B : A; }
+
+int wl_jac3d_box(int which, int put, const long lo[3], const long hi[3], double *box_io) {
+    DvmType *D = pick(which);
+    double *h = (double *)dvmh_get_natural_base_C(0, D);
+    long st[3], i, j, w = hi[2] - lo[2] + 1, q = 0;
+    wl_strides(D, 3, st);
+    if (!put) dvmh_get_actual_subarray_C(D, 3, (DvmType)lo[0], (DvmType)hi[0], (DvmType)lo[1], (DvmType)hi[1],
+                                         (DvmType)lo[2], (DvmType)hi[2]);
+    for (i = lo[0]; i <= hi[0]; i++)
+        for (j = lo[1]; j <= hi[1]; j++, q += w) {
+            double *row = h + i * st[0] + j * st[1] + lo[2];
+            if (put)
+                memcpy(row, box_io + q, sizeof(double) * w);
+            else
+                memcpy(box_io + q, row, sizeof(double) * w);
+        }
+    if (put) dvmh_actual_subarray_C(D, 3, (DvmType)lo[0], (DvmType)hi[0], (DvmType)lo[1], (DvmType)hi[1],
+                                    (DvmType)lo[2], (DvmType)hi[2]);
+    return 0;
+}
+
+/* The host copy of A or B as it is (dense n^3), without making it current. */
+void wl_jac3d_host_peek(int which, double *out) { jac3d_xfer(pick(which), out, 0); }
+
 void wl_jac3d_teardown(void) {
     dvmh_array_free_C(B);
     dvmh_array_free_C(A);

@@ -212,3 +212,45 @@ def test_jacobi3d_update_kernel_all_paths(g, native):
         An[1:-1, 1:-1, 1:-1] = B[1:-1, 1:-1, 1:-1]
         assert items.max().item() == eps_ref, (native, case)
         assert torch.equal(Ad.cpu(), An), (native, case)
+
+
+@pytest.mark.parametrize("mode", ["plain", "batched"])
+def test_subarray_actuality(g, mode):
+    """dvmh_get_actual_subarray_C brings exactly its box to the host (the rest of
+    the host copy stays as it was); dvmh_actual_subarray_C sends a host box to the
+    device, whose copy stays whole and current; the program continues from the
+    mixed state exactly as the oracle does."""
+    import ctypes
+    g.set_mode(mode)
+    w = g.workloads()
+    LA = ctypes.c_long * 3
+    n, seed = 20, 4242
+    A, B = orc.jacobi_init(3, n, seed)
+    A0 = A.copy()
+    j = g.Jacobi(3, n, seed)
+    j.run(1)
+    orc.lib().orc_jacobi_step(3, n, orc.P(A), orc.P(B), 1)
+    lo, hi = (2, 3, 4), (9, 7, 15)
+    sl = tuple(slice(a, b + 1) for a, b in zip(lo, hi))
+    box = np.zeros(int(np.prod([b - a + 1 for a, b in zip(lo, hi)])))
+    assert w.wl_jac3d_box(0, 0, LA(*lo), LA(*hi), orc.P(box)) == 0
+    A3, A03 = A.reshape(n, n, n), A0.reshape(n, n, n)
+    assert np.array_equal(box.reshape(A3[sl].shape), A3[sl])
+    peek = np.zeros(n ** 3)
+    w.wl_jac3d_host_peek(0, orc.P(peek))
+    peek = peek.reshape(n, n, n)
+    inside = np.zeros((n, n, n), dtype=bool)
+    inside[sl] = True
+    assert np.array_equal(peek[inside], A3[inside]) and np.array_equal(peek[~inside], A03[~inside])
+    # a host box of B, declared current, then one more step from the mixed state
+    lo2, hi2 = (5, 1, 0), (12, 18, 19)
+    sl2 = tuple(slice(a, b + 1) for a, b in zip(lo2, hi2))
+    vals = np.random.default_rng(7).random(B.reshape(n, n, n)[sl2].shape)
+    assert w.wl_jac3d_box(1, 1, LA(*lo2), LA(*hi2), orc.P(np.ascontiguousarray(vals).ravel())) == 0
+    B.reshape(n, n, n)[sl2] = vals
+    eps = j.run(1)
+    e_ref = orc.lib().orc_jacobi_step(3, n, orc.P(A), orc.P(B), 1)
+    Ag, Bg = j.fetch()
+    j.close()
+    assert np.array_equal(Ag, A) and np.array_equal(Bg, B), mode
+    assert eps[0] == e_ref, mode
