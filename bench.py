@@ -73,7 +73,10 @@ class Clocks:
              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
              "clocks_event_reasons.sw_power_cap")
         try:
-            self.p = subprocess.Popen(["nvidia-smi", "-i", os.environ.get("CUDA_VISIBLE_DEVICES", "0").split(",")[0],
+            visible = os.environ.get("CUDA_VISIBLE_DEVICES", "").split(",")
+            local = int(os.environ.get("LOCAL_RANK", "0"))
+            gpu = visible[local] if local < len(visible) and visible[local] else str(local)  # this rank's GPU
+            self.p = subprocess.Popen(["nvidia-smi", "-i", gpu,
                                        "--query-gpu=" + q, "--format=csv,noheader,nounits", "-lms", "200"],
                                       stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
@@ -204,6 +207,8 @@ def main():
         os.environ.setdefault("DVMH_GB_DEVICE", os.environ.get("LOCAL_RANK", "0"))
 
     import torch
+    if args.gpus > 1:
+        torch.cuda.set_device(int(os.environ["DVMH_GB_DEVICE"]))  # events on the runtime's device
     import __graft_entry__ as ge
     ge.build()
     _, g = ge.package()
