@@ -67,6 +67,7 @@ struct Settings {
     int graphCacheMax = 64;
     bool fuse = true;
     bool hostProf = false;      // DVMH_GB_HOSTPROF: time the ABI entry points on the host
+    bool autoTfm = true;        // DVMH_GB_AUTOTFM: honour dvmh_loop_autotransform_C (else keep natural layouts)
 };
 extern Settings settings;
 
@@ -103,6 +104,16 @@ struct Obj {
     virtual ~Obj() { kind = 0; }
 };
 
+// How the axes of an array, a template or a loop's mapping correspond to the
+// axes of the distribution root they are (transitively) aligned with: root
+// axis r holds own axis ax[r] (1-based, 0 = none), in direction sign[r].
+struct AlignMap {
+    const Obj *root = nullptr;
+    int rank = 0;  // root rank
+    int ax[MAXR] = {};
+    int sign[MAXR] = {};
+};
+
 struct Array : Obj {
     Array() : Obj(K_ARRAY) {}
     int rank = 0;
@@ -119,7 +130,13 @@ struct Array : Obj {
     long dstride[MAXR] = {};
     size_t delems = 0;
     char *dev = nullptr;
-    char *devAlt = nullptr;  // second buffer for double-buffered (fused) loops
+    char *devAlt = nullptr;  // second buffer for double-buffered (fused) loops and relayouts
+    // device layout: natural (tperm all zero) or transformed (rt_layout.h):
+    // stored position k holds axis tperm[k] (1-based); tdiag 1 / 2 = the last
+    // two stored axes diagonalised (2: slash orientation)
+    int tperm[MAXR] = {};
+    int tdiag = 0;
+    AlignMap align;  // set by dvmh_distribute_C / dvmh_align_C
     bool hostActual = true, devActual = false;
     DvmType *desc = nullptr;
     std::string name;
@@ -133,6 +150,7 @@ struct Templ : Obj {
     Templ() : Obj(K_TEMPLATE) {}
     int rank = 0;
     long ext[MAXR] = {};
+    AlignMap align;  // itself, identity
 };
 
 // A regular (non-distributed) variable known to the runtime: scalars and
@@ -184,6 +202,7 @@ struct Loop : Obj {
     bool empty = false;
     Array *mapArr = nullptr;
     int arrAxisToLoop[MAXR] = {};  // array axis -> loop axis (1-based), 0 = none
+    AlignMap map;                  // distribution root axis -> loop axis (dvmh_loop_map_C)
     std::vector<Reduction> reds;
     std::vector<Across> across;
     long depMask = 0;
@@ -238,6 +257,10 @@ struct SpecLoop : Obj {
 };
 
 // ---------------------------------------------------------------- device layer (rt_device.cu)
+
+struct LayoutDesc;
+void launchRelayout(const char *src, const LayoutDesc &from, char *dst, const LayoutDesc &to, size_t esize,
+                    cudaStream_t s);
 
 struct Device {
     int ordinal = -1;
@@ -309,6 +332,25 @@ void fillDesc(Array *a);
 void queueFlush();  // run or replay everything queued (batched mode)
 bool queueBusy();
 void loopsAtExit();
+void noteSwap(Array *a);          // a device buffer swap, recorded when a graph is being captured
+void noteLayout(Array *a);        // a layout change, likewise
+bool inHandlerCall();             // a handler is running
+bool transformedInCall(const Array *a);  // autotransformed by the handler running now
+
+// ---------------------------------------------------------------- device layouts (rt_layout.cpp)
+
+bool layoutNatural(const Array *a);
+// make the device copy natural again (before copies and hand-written kernels)
+void makeNatural(Array *a);
+// the reference's choice of layout for an ACROSS loop's array; returns the
+// state dvmh_fill_header_C reports (0 natural, 1 permuted, 2 diagonalised)
+int autotransform(const Loop *l, Array *a);
+int layoutState(const Array *a);
+// header coefficients and diagonal parameters of the current device layout
+void layoutHeader(const Array *a, long coef[], long ext7[7]);
+void alignIdentity(AlignMap &m, const Obj *self, int rank);
+const AlignMap *alignOf(const DvmType desc[]);  // of an array or template descriptor (rt_core.cpp)
+void alignCompose(AlignMap &out, const AlignMap &target, const int axis[], const int sign[], int targetRank);
 
 // ---------------------------------------------------------------- tuner (rt_tuner.cpp)
 

@@ -121,6 +121,7 @@ static void loadSettings() {
     if (const char *t = getenv("DVMH_OPT_PARAMS")) settings.tuneMode = atoi(t);
     if (const char *h = getenv("DVMH_GB_HOSTPROF")) settings.hostProf = atoi(h) != 0;
     if (const char *f = getenv("DVMH_GB_FUSE")) settings.fuse = atoi(f) != 0;
+    if (const char *t = getenv("DVMH_GB_AUTOTFM")) settings.autoTfm = atoi(t) != 0;
 }
 
 static void track(Obj *o) { liveObjs.insert(o); }
@@ -287,6 +288,15 @@ static bool boxFromVa(Array *a, long rank, va_list &ap, long lo[], long hi[]) {
     return true;
 }
 
+// The alignment target's axes, or null for an unknown or undistributed target.
+const AlignMap *alignOf(const DvmType desc[]) {
+    if (!desc) return nullptr;
+    Obj *o = (Obj *)desc[0];
+    if (isLive(o, K_ARRAY)) return ((Array *)o)->align.root ? &((Array *)o)->align : nullptr;
+    if (isLive(o, K_TEMPLATE)) return &((Templ *)o)->align;
+    return nullptr;
+}
+
 }  // namespace dvmhgb
 
 using namespace dvmhgb;
@@ -376,6 +386,7 @@ void dvmh_template_create_C(DvmType dvmDesc[], DvmType rank, ...) {
     va_start(ap, rank);
     for (int i = 0; i < t->rank; i++) t->ext[i] = (long)va_arg(ap, DvmType);
     va_end(ap);
+    alignIdentity(t->align, t, t->rank);
     dvmDesc[0] = (DvmType)t;
     track(t);
 }
@@ -392,6 +403,7 @@ void dvmh_distribute_C(DvmType dvmDesc[], DvmType rank, ...) {
     GB_CHECK(rank == a->rank, "distribution rank %ld differs from array rank %d", (long)rank, a->rank);
     // one process: BLOCK (and every other rule) maps the whole index space here
     allocateHost(a);
+    alignIdentity(a->align, a, a->rank);
 }
 
 void dvmh_redistribute_C(DvmType dvmDesc[], DvmType rank, ...) {
@@ -417,15 +429,19 @@ static AlignHelper takeAlign(DvmType v) {
 
 void dvmh_align_C(DvmType dvmDesc[], const DvmType templDesc[], DvmType templRank, ...) {
     Array *a = arrayOf(dvmDesc, "dvmh_align");
+    GB_CHECK(templRank >= 0 && templRank <= MAXR, "alignment target rank %ld out of range", (long)templRank);
+    int axis[MAXR] = {}, sign[MAXR] = {};
     va_list ap;
     va_start(ap, templRank);
     for (long i = 0; i < templRank; i++) {
         AlignHelper h = takeAlign(va_arg(ap, DvmType));
-        GB_CHECK(h.axis == -1 || (h.axis >= 1 && h.axis <= a->rank), "alignment axis %ld out of range", h.axis);
+        GB_CHECK(h.axis == -1 || (h.axis >= 0 && h.axis <= a->rank), "alignment axis %ld out of range", h.axis);
+        axis[i] = h.axis > 0 ? (int)h.axis : 0;
+        sign[i] = h.mult > 0 ? 1 : (h.mult < 0 ? -1 : 0);
     }
     va_end(ap);
-    (void)templDesc;
     allocateHost(a);
+    if (const AlignMap *t = alignOf(templDesc)) alignCompose(a->align, *t, axis, sign, (int)templRank);
 }
 
 void dvmh_array_free_C(DvmType dvmDesc[]) {
@@ -455,12 +471,21 @@ void dvmh_delete_object_(DvmType dvmDesc[]) {
 
 // ---------------------------------------------------------------- addresses and headers
 
+// A handler that did not ask for a transform of this array, and any caller
+// outside handlers, gets the natural device layout.
+static void deviceNatural(Array *a) {
+    if (layoutNatural(a) || transformedInCall(a)) return;
+    if (!inHandlerCall()) queueFlush();  // queued loops first, in their layouts
+    makeNatural(a);
+}
+
 void *dvmh_get_natural_base_C(DvmType deviceNum, const DvmType dvmDesc[]) {
     GB_CHECK(st.inited, "LibDVMH is not initialized");
     GB_CHECK(deviceNum == 0 || deviceNum == 1, "illegal device number %ld", (long)deviceNum);
     Array *a = arrayOf(dvmDesc, "dvmh_get_natural_base");
     if (deviceNum == 0)
         return a->host;
+    deviceNatural(a);
     return a->dev;
 }
 
@@ -474,21 +499,35 @@ void *dvmh_get_device_addr_C(DvmType deviceNum, const void *addr) {
     return v->dev + off;
 }
 
+// Header of the array as a handler sees it (rts/dvmh/dvmh2.cpp:2226-2258):
+// per-axis coefficients of the device layout (zero for the two diagonal
+// axes of a diagonalised copy), the offset from the given base, the base.
+// Returns 0 natural, 1 permuted, 2 diagonalised; for 2, extendedParams gets
+// x axis, x first index, x extent, y axis, y first index, y extent, slash.
 DvmType dvmh_fill_header_C(DvmType deviceNum, const void *baseAddr, const DvmType dvmDesc[], DvmType devHeader[],
                            DvmType extendedParams[]) {
-    (void)extendedParams;
     GB_CHECK(deviceNum == 0 || deviceNum == 1, "illegal device number %ld", (long)deviceNum);
     Array *a = arrayOf(dvmDesc, "dvmh_fill_header");
     GB_CHECK(devHeader, "NULL header passed to dvmh_fill_header");
-    const long *s = deviceNum == 0 ? a->hstride : a->dstride;
+    long coef[MAXR], ext7[7] = {};
+    int state = 0;
+    if (deviceNum == 0) {
+        for (int i = 0; i < a->rank; i++) coef[i] = a->hstride[i];
+    } else {
+        deviceNatural(a);
+        layoutHeader(a, coef, ext7);
+        state = layoutState(a);
+    }
     const char *buf = deviceNum == 0 ? a->host : a->dev;
     devHeader[0] = (DvmType)a;
-    for (int i = 0; i < a->rank; i++) devHeader[i + 1] = s[i];
+    for (int i = 0; i < a->rank; i++) devHeader[i + 1] = coef[i];
     GB_CHECK(((buf - (const char *)baseAddr) % (long)a->esize) == 0,
              "impossible to express the array relative to the given base");
     devHeader[a->rank + 1] = (DvmType)((buf - (const char *)baseAddr) / (long)a->esize);
     devHeader[a->rank + 2] = (DvmType)baseAddr;
-    return 0;  // natural layout, never transformed or diagonalised
+    if (extendedParams && state == 2)
+        for (int i = 0; i < 7; i++) extendedParams[i] = ext7[i];
+    return state;
 }
 
 DvmType dvmh_calc_linear_C(const DvmType dvmDesc[], DvmType rank, ...) {

@@ -18,6 +18,7 @@
 #include <map>
 
 #include "rt.h"
+#include "rt_layout.h"
 
 namespace dvmhgb {
 
@@ -125,6 +126,9 @@ extern dvmhgb_stats_t stats;
 // Uploads read the program's own (pinned) host array: they complete before
 // returning, so that the program may write the host data again right after.
 void copyH2D(Array *a) {
+    // the whole device copy is replaced: it is natural afterwards, whatever it was
+    for (int i = 0; i < MAXR; i++) a->tperm[i] = 0;
+    a->tdiag = 0;
     long rows = (long)(a->helems / a->ext[a->rank - 1]);
     size_t w = a->ext[a->rank - 1] * a->esize;
     size_t dp = (a->rank == 1 ? a->ext[0] : a->dstride[a->rank - 2]) * a->esize;
@@ -137,6 +141,7 @@ void copyH2D(Array *a) {
 }
 
 void copyD2H(Array *a) {
+    makeNatural(a);
     long rows = (long)(a->helems / a->ext[a->rank - 1]);
     size_t w = a->ext[a->rank - 1] * a->esize;
     size_t dp = (a->rank == 1 ? a->ext[0] : a->dstride[a->rank - 2]) * a->esize;
@@ -151,6 +156,7 @@ void copyD2H(Array *a) {
 // Box copies: the innermost axis is the row; rows are enumerated over the
 // outer axes (one 2-D copy per index of the second-innermost axis group).
 static void copyBox(Array *a, const long lo[], const long hi[], bool toDev) {
+    makeNatural(a);
     int r = a->rank;
     size_t w = (hi[r - 1] - lo[r - 1] + 1) * a->esize;
     if (r == 1) {
@@ -197,6 +203,63 @@ void copyBoxH2D(Array *a, const long lo[], const long hi[]) {
 void copyBoxD2H(Array *a, const long lo[], const long hi[]) {
     copyBox(a, lo, hi, false);
     streamSync();
+}
+
+// ---------------------------------------------------------------- relayout
+
+// One pass over every element in natural index order (last axis fastest):
+// read it where layout `from` keeps it, write it where `to` keeps it.  A
+// permutation or a diagonal renumbering is a bijection of the index space, so
+// every destination element is written exactly once.  One side of the copy
+// is strided; the pass runs once per layout change, not per loop.
+template <typename T>
+__global__ void kRelayout(const T *__restrict__ src, LayoutDesc from, T *__restrict__ dst, LayoutDesc to, long n) {
+    for (long t = blockIdx.x * (long)blockDim.x + threadIdx.x; t < n; t += (long)gridDim.x * blockDim.x) {
+        long idx[LAYOUT_MAXR], r = t;
+        for (int a = from.rank - 1; a >= 0; a--) {
+            idx[a] = r % from.ext[a];
+            r /= from.ext[a];
+        }
+        dst[layoutOffset(to, idx)] = src[layoutOffset(from, idx)];
+    }
+}
+
+struct Bytes16 {
+    uint4 v;
+};
+
+void launchRelayout(const char *src, const LayoutDesc &from, char *dst, const LayoutDesc &to, size_t esize,
+                    cudaStream_t s) {
+    long n = 1;
+    for (int a = 0; a < from.rank; a++) n *= from.ext[a];
+    if (n == 0) return;
+    long blocks = std::min<long>((n + 255) / 256, (long)gpu.smCount * 8);
+    switch (esize) {
+        case 1: kRelayout<uint8_t><<<(unsigned)blocks, 256, 0, s>>>((const uint8_t *)src, from, (uint8_t *)dst, to, n); break;
+        case 2: kRelayout<uint16_t><<<(unsigned)blocks, 256, 0, s>>>((const uint16_t *)src, from, (uint16_t *)dst, to, n); break;
+        case 4: kRelayout<uint32_t><<<(unsigned)blocks, 256, 0, s>>>((const uint32_t *)src, from, (uint32_t *)dst, to, n); break;
+        case 8: kRelayout<uint64_t><<<(unsigned)blocks, 256, 0, s>>>((const uint64_t *)src, from, (uint64_t *)dst, to, n); break;
+        case 16: kRelayout<Bytes16><<<(unsigned)blocks, 256, 0, s>>>((const Bytes16 *)src, from, (Bytes16 *)dst, to, n); break;
+        default: {
+            // other element sizes: the same pass over bytes, the element as the innermost axis
+            LayoutDesc f = from, g = to;
+            GB_CHECK(from.rank < LAYOUT_MAXR, "relayout of a rank-%d array of %zu-byte elements", from.rank, esize);
+            f.ext[f.rank] = g.ext[g.rank] = (long)esize;
+            for (int a = 0; a < f.rank; a++) {
+                f.coef[a] *= (long)esize;
+                g.coef[a] *= (long)esize;
+            }
+            f.coef[f.rank] = g.coef[g.rank] = 1;
+            f.diagUnit *= (long)esize;
+            g.diagUnit *= (long)esize;
+            f.rank++;
+            g.rank++;
+            kRelayout<uint8_t><<<(unsigned)std::min<long>((n * (long)esize + 255) / 256, (long)gpu.smCount * 8), 256,
+                                 0, s>>>((const uint8_t *)src, f, (uint8_t *)dst, g, n * (long)esize);
+        }
+    }
+    GB_CUDA(cudaGetLastError());
+    dvmhgb_count_launches(1);
 }
 
 // Variables: through a pinned staging copy so the transfer is asynchronous

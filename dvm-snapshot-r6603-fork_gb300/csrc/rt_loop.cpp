@@ -89,6 +89,20 @@ void collectTimings() {  // called after a stream synchronisation
 
 static char graphTimingKey;  // handler key for graphs that ran several handlers
 
+// an array's device layout, as recorded for graph replays
+struct LayoutState {
+    int perm[MAXR] = {};
+    int diag = 0;
+    LayoutState() = default;
+    explicit LayoutState(const Array *a) : diag(a->tdiag) {
+        for (int k = 0; k < MAXR; k++) perm[k] = a->tperm[k];
+    }
+    void applyTo(Array *a) const {
+        for (int k = 0; k < MAXR; k++) a->tperm[k] = perm[k];
+        a->tdiag = diag;
+    }
+};
+
 struct CachedGraph {
     uint64_t key;
     std::vector<uint64_t> sig;
@@ -98,6 +112,7 @@ struct CachedGraph {
     std::vector<void *> scratch;
     std::vector<void *> hostScratch;
     std::vector<Array *> swaps;
+    std::vector<std::pair<Array *, LayoutState>> layouts;  // layout changes, in order
     long launches = 0;
 };
 static std::list<CachedGraph> graphCache;  // most recently used first
@@ -150,8 +165,32 @@ struct ExecCtx {
     std::vector<void *> *keep = nullptr;      // scratch kept alive with a cached graph
     std::vector<void *> *keepHost = nullptr;  // pinned host scratch kept with it
     std::vector<Array *> *swaps = nullptr;    // swaps performed (recorded for replays)
+    std::vector<std::pair<Array *, LayoutState>> *layouts = nullptr;  // layout changes, likewise
 };
 static ExecCtx ctx;
+
+// the handler call in progress and the arrays it autotransformed
+static int callDepth = 0;
+static std::vector<const Array *> callTfm;
+bool inHandlerCall() { return callDepth > 0; }
+bool transformedInCall(const Array *a) {
+    return callDepth > 0 && std::find(callTfm.begin(), callTfm.end(), a) != callTfm.end();
+}
+struct CallScope {
+    CallScope() {
+        if (callDepth++ == 0) callTfm.clear();
+    }
+    ~CallScope() {
+        if (--callDepth == 0) callTfm.clear();
+    }
+};
+
+void noteSwap(Array *a) {
+    if (ctx.swaps) ctx.swaps->push_back(a);
+}
+void noteLayout(Array *a) {
+    if (ctx.layouts) ctx.layouts->push_back({a, LayoutState(a)});
+}
 // reduction folds deferred while a batched handler runs: one launch for all
 static bool deferFolds = false;
 static std::vector<FoldJob> deferred;
@@ -249,7 +288,10 @@ static void runSingle(Loop *l) {
     stats.handler_calls++;
     TimedExec t;
     if (timingOn) timeBegin(t, (void *)l->cuda.func);
-    callWithParams(l->cuda.func, &ref, l->cuda.nparams, l->cuda.params);
+    {
+        CallScope call;
+        callWithParams(l->cuda.func, &ref, l->cuda.nparams, l->cuda.params);
+    }
     if (timingOn) {
         memcpy(t.block, s->block, sizeof t.block);
         t.variant = s->variant;
@@ -270,7 +312,10 @@ static void runFused(DvmHandlerFunc fused, Loop *a, Loop *b) {
     stats.fused_pairs++;
     TimedExec t;
     if (timingOn) timeBegin(t, (void *)fused);
-    callWithParams(fused, refs, n, params);
+    {
+        CallScope call;
+        callWithParams(fused, refs, n, params);
+    }
     if (timingOn) timeEnd(t);
     finishSpec(sa);
     finishSpec(sb);
@@ -289,7 +334,10 @@ static void runBatch(DvmHandlerFunc batched, const std::vector<Loop *> &group) {
     deferred.clear();
     TimedExec t;
     if (timingOn) timeBegin(t, (void *)batched);
-    ((void (*)(DvmType *, DvmType))batched)(refs.data(), (DvmType)refs.size());
+    {
+        CallScope call;
+        ((void (*)(DvmType *, DvmType))batched)(refs.data(), (DvmType)refs.size());
+    }
     deferFolds = false;
     if (!deferred.empty()) launchRedFoldBatch(deferred, gpu.stream, specs[0]->scratch, specs[0]->hostScratch);
     deferred.clear();
@@ -362,6 +410,9 @@ static std::vector<uint64_t> signature(const std::vector<Loop *> &q) {
                 Array *a = (Array *)((const DvmType *)l->cuda.params[i])[0];
                 sigAdd(s, (uint64_t)a->dev);
                 sigAdd(s, (uint64_t)a->devAlt);
+                uint64_t lay = (uint64_t)a->tdiag;
+                for (int k = 0; k < MAXR; k++) lay = lay * 8 + (uint64_t)a->tperm[k];
+                sigAdd(s, lay);
             } else {
                 size_t off = 0;
                 Var *v = varAt(l->cuda.params[i], &off);
@@ -387,6 +438,7 @@ static std::vector<uint64_t> signature(const std::vector<Loop *> &q) {
     }
     sigAdd(s, (uint64_t)settings.fuse);
     sigAdd(s, (uint64_t)(int64_t)forcedVariant);  // a forced variant is captured anew
+    sigAdd(s, (uint64_t)settings.autoTfm);
     return s;
 }
 
@@ -422,6 +474,7 @@ void queueFlush() {
         if (it->key == key && it->sig == sig) {
             launchGraph(*it);
             for (Array *a : it->swaps) std::swap(a->dev, a->devAlt);
+            for (auto &pl : it->layouts) pl.second.applyTo(pl.first);
             stats.graph_replays++;
             stats.kernel_launches += it->launches;
             graphCache.splice(graphCache.begin(), graphCache, it);
@@ -439,6 +492,7 @@ void queueFlush() {
     ctx.keep = &g.scratch;
     ctx.keepHost = &g.hostScratch;
     ctx.swaps = &g.swaps;
+    ctx.layouts = &g.layouts;
     GB_CUDA(cudaStreamBeginCapture(gpu.stream, cudaStreamCaptureModeRelaxed));
     runQueued(q);
     cudaGraph_t graph = nullptr;
@@ -529,18 +583,23 @@ void dvmh_loop_map_C(DvmType curLoop, const DvmType templDesc[], DvmType templRa
     Loop *l = loopOf(curLoop, "dvmh_loop_map");
     Obj *o = (Obj *)templDesc[0];
     if (isLive(o, K_ARRAY)) l->mapArr = (Array *)o;
+    GB_CHECK(templRank >= 0 && templRank <= MAXR, "mapping target rank %ld out of range", (long)templRank);
+    int axis[MAXR] = {}, sign[MAXR] = {};
     va_list ap;
     va_start(ap, templRank);
-    for (long i = 0; i < templRank && i < MAXR; i++) {
+    for (long i = 0; i < templRank; i++) {
         DvmType hv = va_arg(ap, DvmType);
         struct H { uint32_t magic; long axis, mult, summand; } *h = (H *)hv;
         GB_CHECK(h && h->magic == 0x414c4e31u, "invalid alignment helper in dvmh_loop_map");
-        GB_CHECK(h->axis == -1 || (h->axis >= 1 && h->axis <= l->rank), "loop axis %ld out of range", h->axis);
+        GB_CHECK(h->axis == -1 || (h->axis >= 0 && h->axis <= l->rank), "loop axis %ld out of range", h->axis);
         l->arrAxisToLoop[i] = h->axis > 0 ? (int)h->axis : 0;
+        axis[i] = l->arrAxisToLoop[i];
+        sign[i] = h->mult > 0 ? 1 : (h->mult < 0 ? -1 : 0);
         h->magic = 0;
         delete h;
     }
     va_end(ap);
+    if (const AlignMap *t = alignOf(templDesc)) alignCompose(l->map, *t, axis, sign, (int)templRank);
 }
 
 void dvmh_loop_set_cuda_block_C(DvmType curLoop, DvmType xSize, DvmType ySize, DvmType zSize) {
@@ -716,10 +775,16 @@ DvmType dvmh_loop_get_dependency_mask_C(DvmType curLoop) {
     return specOf(curLoop, "dvmh_loop_get_dependency_mask")->loop->depMask;
 }
 
+// The handler asks for the layout the reference would choose for this loop
+// (rts/dvmh/dvmh2.cpp:4011-4026): the array may stay transformed for the
+// rest of this handler call; the header it fills next describes the layout.
 DvmType dvmh_loop_autotransform_C(DvmType curLoop, DvmType dvmDesc[]) {
-    (void)specOf(curLoop, "dvmh_loop_autotransform");
-    (void)arrayOf(dvmDesc, "dvmh_loop_autotransform");
-    return 0;  // natural layout kept: the wavefront kernels index it directly
+    SpecLoop *s = specOf(curLoop, "dvmh_loop_autotransform");
+    Array *a = arrayOf(dvmDesc, "dvmh_loop_autotransform");
+    ensureDevBuffer(a);
+    int state = autotransform(s->loop, a);
+    if (state != 0) callTfm.push_back(a);
+    return state;
 }
 
 void dvmh_loop_fill_bounds_C(DvmType curLoop, DvmType boundsLow[], DvmType boundsHigh[], DvmType loopSteps[]) {
@@ -935,6 +1000,13 @@ void dvmhgb_set_mode(int mode) {
 
 int dvmhgb_get_mode(void) { return settings.mode; }
 
+void dvmhgb_set_autotransform(int on) {
+    queueFlush();
+    settings.autoTfm = on != 0;
+}
+
+int dvmhgb_get_autotransform(void) { return settings.autoTfm ? 1 : 0; }
+
 void dvmhgb_flush(void) { queueFlush(); }
 
 void dvmhgb_sync(void) {
@@ -1019,10 +1091,7 @@ void *dvmhgb_loop_alt_buffer(DvmType loopRef, const DvmType dvmDesc[]) {
     SpecLoop *s = specOf(loopRef, "dvmhgb_loop_alt_buffer");
     Array *a = arrayOf(dvmDesc, "dvmhgb_loop_alt_buffer");
     GB_CHECK(a->dev, "array has no device copy");
-    if (!a->devAlt) {
-        GB_CHECK(!ctx.capturing || true, "");
-        a->devAlt = (char *)devAlloc(a->devBytes());
-    }
+    if (!a->devAlt) a->devAlt = (char *)devAlloc(a->devBytes());
     for (Array *x : s->swaps) GB_CHECK(x != a, "alternate buffer requested twice in one loop");
     s->swaps.push_back(a);
     return a->devAlt;

@@ -38,7 +38,7 @@ class HeatParams(ctypes.Structure):
 class Stats(ctypes.Structure):
     _fields_ = [(n, ctypes.c_long) for n in (
         "loops_performed", "handler_calls", "fused_pairs", "batched_groups", "graphs_captured", "graph_replays",
-        "flushes", "h2d_bytes", "d2h_bytes", "kernel_launches")]
+        "flushes", "h2d_bytes", "d2h_bytes", "kernel_launches", "relayouts")]
 
     def asdict(self):
         return {n: getattr(self, n) for n, _ in self._fields_}

@@ -68,6 +68,17 @@ int dvmhgb_loop_variant(DvmType loopRef, int nvariants, int dflt);
  * variant count); v < 0 restores tuning / defaults.  Overrides DVMH_GB_VARIANT. */
 void dvmhgb_force_variant(int v);
 
+/* Device layouts for ACROSS loops.  On (default; environment
+ * DVMH_GB_AUTOTFM=0 turns it off), dvmh_loop_autotransform_C stores a loop's
+ * array as the reference does: the array axis of the fastest independent loop
+ * axis innermost (one dependence), or the two fastest dependent axes
+ * numbered along the diagonal the loop sweeps (two or more).  Off, arrays
+ * stay natural and autotransform reports 0.  Either way a device copy is
+ * natural again before host copies and before any handler that did not ask
+ * for the transform.  The tuner may also choose per loop (dvmhgb_tuner_*). */
+void dvmhgb_set_autotransform(int on);
+int dvmhgb_get_autotransform(void);
+
 /* Self-test of the integer-pipe FP64 operations against the FP64 unit on n
  * random operand pairs: mismatches[0..3] = add, sub, mul, division by 6. */
 int dvmhgb_selftest_softfp64(long n, unsigned long long seed, long mismatches[4]);
@@ -95,6 +106,7 @@ typedef struct {
     long flushes;
     long h2d_bytes, d2h_bytes;
     long kernel_launches;   /* launches issued by this library's launchers */
+    long relayouts;         /* device copies moved between layouts (autotransform) */
 } dvmhgb_stats_t;
 void dvmhgb_get_stats(dvmhgb_stats_t *out);
 void dvmhgb_reset_stats(void);

@@ -36,6 +36,11 @@ def lib():
         L.orc_heat_init.argtypes = [ctypes.c_long, ctypes.c_uint64, ctypes.c_long, _dp, _dp]
         L.orc_heat_step.argtypes = [ctypes.c_long, ctypes.c_double, _dp, _dp, _dp, _dp, _dp,
                                     ctypes.POINTER(ctypes.c_int)]
+        L.orc_gsd2d_init.argtypes = [ctypes.c_long, ctypes.c_long, ctypes.c_uint64, _dp]
+        L.orc_gsd2d_sweep.restype = ctypes.c_double
+        L.orc_gsd2d_sweep.argtypes = [ctypes.c_long, ctypes.c_long, ctypes.c_int, ctypes.c_int, _dp]
+        L.orc_diag_index.restype = ctypes.c_long
+        L.orc_diag_index.argtypes = [ctypes.c_long, ctypes.c_long, ctypes.c_long, ctypes.c_long, ctypes.c_int]
         L.orc_max_threads.restype = ctypes.c_int
         _L = L
     return _L
@@ -94,3 +99,11 @@ def heat_run(count, lo, hi, steps, coef, seed):
             src, dst = dst, src
         out["finals"].append(src)
     return out
+
+
+def gsd2d_run(n0, n1, sweeps, seed, dir0=1, dir1=1):
+    A = np.zeros(n0 * n1)
+    L = lib()
+    L.orc_gsd2d_init(n0, n1, seed, P(A))
+    m = [L.orc_gsd2d_sweep(n0, n1, dir0, dir1, P(A)) for _ in range(sweeps)]
+    return np.array(m), A

@@ -285,6 +285,53 @@ void orc_heat_step(long n, double c, const double *src, double *dst, double *sum
     loc[1] = l1;
 }
 
+/*
+ * Gauss-Seidel over an n0 x n1 array with dependences on both axes
+ * (dvm-snapshot-r6603-fork_gb300/workloads/gsd2d.c): the sequential loop, each axis
+ * forward (dir > 0) or backward, interior only; returns MAX |new - old| of
+ * the sweep combined with the initial value 0 (the reduction's result).
+ */
+void orc_gsd2d_init(long n0, long n1, uint64_t seed, double *A) {
+    for (long i = 0; i < n0; i++)
+        for (long j = 0; j < n1; j++)
+            A[i * n1 + j] =
+                (i == 0 || j == 0 || i == n0 - 1 || j == n1 - 1) ? 0.0 : orc_u01(seed, 17, (uint64_t)(i * n1 + j));
+}
+
+double orc_gsd2d_sweep(long n0, long n1, int dir0, int dir1, double *A) {
+    double m = 0.0;  /* MAX identity of non-negative values; the initial value 0 is folded in last */
+    for (long a = 0; a < n0 - 2; a++) {
+        long i = dir0 > 0 ? 1 + a : n0 - 2 - a;
+        for (long b = 0; b < n1 - 2; b++) {
+            long j = dir1 > 0 ? 1 + b : n1 - 2 - b;
+            double old = A[i * n1 + j];
+            double v = (((A[(i - 1) * n1 + j] + A[(i + 1) * n1 + j]) + A[i * n1 + j - 1]) + A[i * n1 + j + 1]) * 0.25;
+            A[i * n1 + j] = v;
+            m = Max(m, fabs(v - old));
+        }
+    }
+    return Max(m, 0.0);
+}
+
+/* position of (x, y) in the diagonal numbering of an Rx x Ry plane
+ * (rts/dvmh/util.cpp:1009-1055), by walking the diagonals: cells ordered by
+ * d = x + y (slash: x + Ry - 1 - y), inside a diagonal along y when Rx < Ry
+ * or (Rx == Ry and d < Rx), else along x.  Counting, not a closed form, so it
+ * checks the runtime's closed form independently. */
+long orc_diag_index(long x, long y, long Rx, long Ry, int slash) {
+    long yy = slash ? Ry - 1 - y : y, d = x + yy, pos = 0;
+    for (long e = 0; e < d; e++)
+        for (long xx = 0; xx < Rx; xx++)
+            if (e - xx >= 0 && e - xx < Ry) pos++;
+    int alongY = Rx < Ry || (Rx == Ry && d < Rx);
+    for (long xx = 0; xx < Rx; xx++) {
+        long y2 = d - xx;
+        if (y2 < 0 || y2 >= Ry) continue;
+        if (alongY ? y2 < yy : xx < x) pos++;
+    }
+    return pos;
+}
+
 int orc_max_threads(void) {
 #ifdef _OPENMP
     return omp_get_max_threads();

@@ -1,0 +1,98 @@
+"""Transformed device layouts (the reference's autotransform) through a
+program whose ACROSS loop has two dependences and a handler in the shape cdvmh
+generates with automatic transforms (workloads/gsd2d*.c/cu): one launch per
+diagonal, the array indexed through the header the runtime fills.  With
+transforms on, the runtime stores the array diagonalised (slash orientation
+when the loop runs its two axes in opposite directions); a mirror loop whose
+handler does not ask for transforms reads the array in the natural layout in
+between.  Everything is checked bit for bit against the sequential loop."""
+import ctypes
+
+import numpy as np
+import pytest
+
+import __graft_entry__ as ge
+from oracle import orc
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def g():
+    ge.build()
+    _, g = ge.package()
+    g.init()
+    w = g.workloads()
+    w.wl_gsd2d_run.argtypes = [ctypes.c_long, ctypes.c_long, ctypes.c_long, ctypes.c_uint64, ctypes.c_int,
+                               ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.POINTER(ctypes.c_double),
+                               ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)]
+    yield g
+    g.set_mode("batched")
+    g.runtime().dvmhgb_set_autotransform(1)
+
+
+def run(g, n0, n1, sweeps, seed, dirs=(1, 1), read_each=1, mirror=0):
+    m = np.zeros(sweeps)
+    a = np.zeros(n0 * n1)
+    b = np.zeros(n0 * n1)
+    g.reset_stats()
+    assert g.workloads().wl_gsd2d_run(n0, n1, sweeps, seed, dirs[0], dirs[1], read_each, mirror, orc.P(m), orc.P(a),
+                                      orc.P(b)) == 0
+    return m, a, b, g.stats()
+
+
+def check(m, a, b, n0, n1, sweeps, seed, dirs, read_each, mirror):
+    m_ref, a_ref = orc.gsd2d_run(n0, n1, sweeps, seed, dirs[0], dirs[1])
+    assert np.array_equal(a, a_ref)
+    if read_each:
+        assert np.array_equal(m, m_ref)
+    else:
+        assert m[0] == m_ref[-1]
+    if mirror:
+        assert np.array_equal(b, a_ref * 2.0)
+
+
+@pytest.mark.parametrize("mode", ["plain", "async", "batched"])
+@pytest.mark.parametrize("tfm", [1, 0])
+def test_modes_and_switch(g, mode, tfm):
+    g.set_mode(mode)
+    g.runtime().dvmhgb_set_autotransform(tfm)
+    n0, n1, sweeps, seed = 40, 40, 3, 11
+    m, a, b, s = run(g, n0, n1, sweeps, seed, read_each=1, mirror=1)
+    check(m, a, b, n0, n1, sweeps, seed, (1, 1), 1, 1)
+    if tfm:
+        # every sweep diagonalises A, every mirror loop makes it natural again (counted when
+        # run or captured; a replayed graph repeats them without counting)
+        assert s["relayouts"] >= (2 * sweeps if mode != "batched" else 2), s
+    else:
+        assert s["relayouts"] == 0, s
+
+
+@pytest.mark.parametrize("dirs", [(1, 1), (-1, 1), (1, -1), (-1, -1)])
+@pytest.mark.parametrize("shape", [(23, 23), (17, 41), (41, 17)])
+def test_directions_and_shapes(g, dirs, shape):
+    g.set_mode("batched")
+    g.runtime().dvmhgb_set_autotransform(1)
+    n0, n1 = shape
+    m, a, b, s = run(g, n0, n1, 4, 5, dirs=dirs, read_each=0, mirror=0)
+    check(m, a, b, n0, n1, 4, 5, dirs, 0, 0)
+    # one relayout to the diagonal layout for the whole time loop, one back for get_actual
+    assert s["relayouts"] == 2, s
+
+
+def test_graph_replays_keep_layouts(g):
+    # the same queue replayed: captured relayouts and swaps are replayed with their layouts
+    g.set_mode("batched")
+    g.runtime().dvmhgb_set_autotransform(1)
+    n0, n1, sweeps, seed = 33, 26, 6, 3
+    m, a, b, s = run(g, n0, n1, sweeps, seed, dirs=(-1, 1), read_each=1, mirror=1)
+    check(m, a, b, n0, n1, sweeps, seed, (-1, 1), 1, 1)
+    assert s["graph_replays"] > 0, s
+
+
+def test_larger_grid_int_and_long_index(g):
+    g.set_mode("batched")
+    g.runtime().dvmhgb_set_autotransform(1)
+    n0, n1, sweeps, seed = 300, 257, 2, 8
+    m, a, b, s = run(g, n0, n1, sweeps, seed, dirs=(1, -1), read_each=1, mirror=0)
+    check(m, a, b, n0, n1, sweeps, seed, (1, -1), 1, 0)
