@@ -190,12 +190,14 @@ def main():
     ap.add_argument("--impl", default="gb300")
     ap.add_argument("--grid", type=int, default=N_DEFAULT)
     ap.add_argument("--quick", action="store_true", help="headline only (no extra modes/configs/cpu leg)")
-    ap.add_argument("--only", choices=["jacobi3d", "sor", "heat"], default=None,
+    ap.add_argument("--only", choices=["jacobi3d", "sor", "heat", "gsd2d"], default=None,
                     help="time one workload alone (small cases for profiling): --grid is its size "
                          "(heat: the largest side), --steps its steps or sweeps")
     ap.add_argument("--mode", choices=["batched", "async", "plain"], default="batched", help="with --only")
     ap.add_argument("--arrays", type=int, default=256, help="heat arrays, with --only heat")
     ap.add_argument("--variant", type=int, default=-1, help="force a kernel variant, with --only")
+    ap.add_argument("--autotfm", type=int, default=1, help="layouts for ACROSS loops with --only gsd2d: 1 the "
+                                                             "reference's transform, 0 natural, 2 chosen by the tuner")
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", "0"))  # under torchrun; --impl reference runs on rank 0 only
     if args.impl == "reference":
@@ -339,6 +341,8 @@ def run_only(args, g, stream):
     import torch
     g.force_variant(args.variant)
     g.set_mode(args.mode)
+    if args.only == "gsd2d":
+        return run_gsd2d(args, g, stream)
     if args.only == "jacobi3d":
         w = g.Jacobi(3, args.grid, SEED)
         cells, unit = (args.grid - 2) ** 3, "step"
@@ -362,6 +366,56 @@ def run_only(args, g, stream):
     g.force_variant(-1)
     print(json.dumps({"workload": args.only, "grid": args.grid, "mode": args.mode, "variant": args.variant,
                       "steps": args.steps, "ms_per_" + unit: ms, "cell-updates/s": cells / (ms * 1e-3)}), flush=True)
+
+
+def run_gsd2d(args, g, stream):
+    """2-D Gauss-Seidel ACROSS (two dependences) through the generated-shape
+    handler with one launch per diagonal: the array natural or diagonalised."""
+    import ctypes
+    import numpy as np
+    import torch
+    w = g.workloads()
+    w.wl_gsd2d_setup.argtypes = [ctypes.c_long, ctypes.c_long, ctypes.c_uint64]
+    w.wl_gsd2d_sweeps.argtypes = [ctypes.c_long, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                  ctypes.POINTER(ctypes.c_double)]
+    rt = g.runtime()
+    rt.dvmhgb_set_autotransform(1 if args.autotfm else 0)
+    n, k = args.grid, args.steps
+    m = np.zeros(max(k, 4))
+    mp = m.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+    w.wl_gsd2d_setup(n, n, SEED + 4)
+    g.reset_stats()
+    tuned = None
+    if args.autotfm == 2:
+        # the tuner's exploration (immediate execution), then its choice in the timed mode
+        rt.dvmhgb_set_tuning(1)
+        g.set_mode("plain")
+        w.wl_gsd2d_sweeps(5, 1, 1, 1, 0, mp)
+        best = (ctypes.c_double * 2)()
+        rt.dvmhgb_tuner_layout.argtypes = [ctypes.c_void_p, ctypes.POINTER(ctypes.c_double)]
+        choice = rt.dvmhgb_tuner_layout(ctypes.cast(w.loop_gsd2d_cuda, ctypes.c_void_p), best)
+        tuned = {"choice": ["natural", "transformed"][choice] if choice >= 0 else None,
+                 "best_ms_natural": best[0] * 1e3, "best_ms_transformed": best[1] * 1e3}
+        g.set_mode(args.mode)
+    for _ in range(2):  # the queue of k sweeps captured from each starting layout
+        w.wl_gsd2d_sweeps(k, 1, 1, 0, 0, mp)
+    g.sync()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    w.wl_gsd2d_sweeps(k, 1, 1, 0, 0, mp)
+    e1.record(stream)
+    g.sync()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / k
+    st = g.stats()
+    w.wl_gsd2d_free()
+    rt.dvmhgb_set_autotransform(1)
+    rt.dvmhgb_set_tuning(0)
+    cells = (n - 2) ** 2
+    print(json.dumps({"workload": "gsd2d", "grid": n, "mode": args.mode, "autotfm": args.autotfm, "sweeps": k,
+                      "ms_per_sweep": ms, "cell-updates/s": cells / (ms * 1e-3), "relayouts": st["relayouts"],
+                      "graph_replays": st["graph_replays"], "tuner": tuned}), flush=True)
 
 
 def extra_configs(g, stream):

@@ -250,6 +250,7 @@ struct SpecLoop : Obj {
     cudaStream_t stream = nullptr;
     int block[3] = {0, 0, 0};
     int variant = -1;  // tuner's kernel variant, -1 = handler default
+    int layout = -1;   // tuner's layout choice for autotransform (1 transform, 0 natural), -1 none
     std::vector<CudaRed> reds;
     std::vector<void *> scratch;  // device allocations owned by this execution
     std::vector<void *> hostScratch;  // pinned host allocations owned by this execution
@@ -358,5 +359,7 @@ bool tunerWants(const Loop *l);  // record timings of this loop shape
 int tunerVariant(const Loop *l, int nvariants, int dflt, bool bestOnly);
 void tunerPick(Loop *l, int block[3], int *variant);
 void tunerRecord(const Loop *l, const int block[3], int variant, double seconds);
+int tunerLayout(const Loop *l, bool explore);  // 1: the reference's transform, 0: natural
+void tunerRecordLayout(const Loop *l, int choice, double seconds);
 
 }  // namespace dvmhgb

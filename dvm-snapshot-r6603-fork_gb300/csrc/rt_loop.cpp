@@ -53,6 +53,7 @@ struct TimedExec {
     Loop *loopCopy;  // loop shape for the tuner (owned), may be null
     int block[3];
     int variant;
+    int layout;    // the tuner's layout choice in this execution, -1 none
     bool inGraph;  // owned by a cached graph (reused on every replay)
 };
 struct TimingTotal {
@@ -77,6 +78,7 @@ void collectTimings() {  // called after a stream synchronisation
             tt.ms += ms;
             tt.count++;
             if (t.loopCopy) tunerRecord(t.loopCopy, t.block, t.variant, ms * 1e-3);
+            if (t.loopCopy && t.layout >= 0) tunerRecordLayout(t.loopCopy, t.layout, ms * 1e-3);
         }
         if (!t.inGraph) {
             cudaEventDestroy(t.e0);
@@ -242,6 +244,7 @@ static void timeBegin(TimedExec &t, void *func) {
     t.loopCopy = nullptr;
     t.block[0] = t.block[1] = t.block[2] = 0;
     t.variant = -1;
+    t.layout = -1;
     t.inGraph = ctx.capturing;
     if (ctx.capturing) return;
     t.e0 = newEvent();
@@ -295,6 +298,7 @@ static void runSingle(Loop *l) {
     if (timingOn) {
         memcpy(t.block, s->block, sizeof t.block);
         t.variant = s->variant;
+        t.layout = s->layout;
         t.loopCopy = tunerWants(l) ? new Loop(*l) : nullptr;
         timeEnd(t);
     }
@@ -782,6 +786,14 @@ DvmType dvmh_loop_autotransform_C(DvmType curLoop, DvmType dvmDesc[]) {
     SpecLoop *s = specOf(curLoop, "dvmh_loop_autotransform");
     Array *a = arrayOf(dvmDesc, "dvmh_loop_autotransform");
     ensureDevBuffer(a);
+    if (settings.tuneMode && settings.autoTfm) {
+        // the tuner may keep this loop's arrays natural (explores only outside captures)
+        if (s->layout < 0) s->layout = tunerLayout(s->loop, !ctx.capturing);
+        if (s->layout == 0) {
+            makeNatural(a);
+            return 0;
+        }
+    }
     int state = autotransform(s->loop, a);
     if (state != 0) callTfm.push_back(a);
     return state;

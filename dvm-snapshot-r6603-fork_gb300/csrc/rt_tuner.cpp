@@ -89,6 +89,39 @@ void tunerRecord(const Loop *l, const int block[3], int variant, double seconds)
     if (it == vs.best.end() || seconds < it->second) vs.best[variant] = seconds;
 }
 
+// ---------------------------------------------------------------- online layout tuning of ACROSS loops
+//
+// For a loop whose handler asks for transforms, the tuner chooses between the
+// reference's layout (1) and the natural one (0): in immediate execution it
+// runs each twice in a row (the second run of each pays no relayout), then
+// keeps the faster; a captured graph takes the best known, or the
+// reference's layout before anything is known.
+
+struct LayoutTune {
+    double best[2] = {1e300, 1e300};
+    int runs[2] = {0, 0};
+};
+static std::unordered_map<uint64_t, LayoutTune> lstate;
+static std::unordered_map<void *, uint64_t> lastLayoutKey;  // handler -> its most recent loop shape
+
+int tunerLayout(const Loop *l, bool explore) {
+    LayoutTune &t = lstate[loopKey(l)];
+    lastLayoutKey[(void *)l->cuda.func] = loopKey(l);
+    if (explore) {
+        if (t.runs[1] < 2) return 1;
+        if (t.runs[0] < 2) return 0;
+    }
+    if (t.runs[0] == 0 || t.runs[1] == 0) return 1;
+    return t.best[0] < t.best[1] ? 0 : 1;
+}
+
+void tunerRecordLayout(const Loop *l, int choice, double seconds) {
+    if (choice < 0 || choice > 1) return;
+    LayoutTune &t = lstate[loopKey(l)];
+    t.runs[choice]++;
+    if (seconds < t.best[choice]) t.best[choice] = seconds;
+}
+
 // ---------------------------------------------------------------- synthetic loops: candidates, features
 
 static const int BLOCKS[][3] = {{32, 1, 1},  {64, 1, 1},  {128, 1, 1}, {256, 1, 1}, {512, 1, 1}, {1024, 1, 1},
@@ -306,6 +339,26 @@ int dvmhgb_tuner_time_synth_all(const dvmhgb_synth_loop *L, const dvmhgb_synth_c
     devFree(it);
     devFree(locs);
     return 0;
+}
+
+// The layout the tuner keeps for the most recent loop shape of a handler:
+// 0 natural, 1 the reference's transform, -1 while either is unmeasured;
+// best[2] (optional) gets the fastest seconds seen with each.
+int dvmhgb_tuner_layout(DvmHandlerFunc handler, double best[2]) {
+    auto k = lastLayoutKey.find((void *)handler);
+    if (k == lastLayoutKey.end()) return -1;
+    const LayoutTune &t = lstate[k->second];
+    if (best) {
+        best[0] = t.runs[0] ? t.best[0] : -1;
+        best[1] = t.runs[1] ? t.best[1] : -1;
+    }
+    if (t.runs[0] < 2 || t.runs[1] < 2) return -1;
+    return t.best[0] < t.best[1] ? 0 : 1;
+}
+
+void dvmhgb_set_tuning(int mode) {
+    GB_CHECK(mode >= 0 && mode <= 2, "unknown tuning mode %d", mode);
+    settings.tuneMode = mode;
 }
 
 long dvmhgb_tuner_db_size(void) { return (long)db.size(); }

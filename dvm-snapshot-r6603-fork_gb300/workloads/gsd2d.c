@@ -31,15 +31,15 @@ static DvmType A[64], B[64];
 void loop_gsd2d_cuda(DvmType *pLoopRef, DvmType A_hdr[], double *m_ptr);
 void loop_gsd2d_mirror_cuda(DvmType *pLoopRef, DvmType B_hdr[], DvmType A_hdr[]);
 
-/* m_out[t] = m after sweep t (readEach) or m_out[0] = m after the last sweep;
- * a_out (n0*n1) = A; b_out (n0*n1) = B when mirror.  dir0 / dir1: +1 forward,
- * -1 backward loops. */
-int wl_gsd2d_run(long n0, long n1, long sweeps, uint64_t seed, int dir0, int dir1, int readEach, int mirror,
-                 double *m_out, double *a_out, double *b_out) {
-    static double m;
-    long i, j, t, st[2];
-    double *a, *b;
-    DvmType cur_region, cur_loop;
+static double m;
+static long N0, N1;
+
+/* A (n0 x n1) seeded, B (n0 x n1, aligned with A) */
+int wl_gsd2d_setup(long n0, long n1, uint64_t seed) {
+    long i, j, st[2];
+    double *a;
+    N0 = n0;
+    N1 = n1;
     dvmh_array_create_C(A, 2, -rt_DOUBLE, (DvmType)n0, 1L, 1L, (DvmType)n1, 1L, 1L);
     dvmh_distribute_C(A, 2, dvmh_distribution_block_C(1), dvmh_distribution_block_C(2));
     dvmh_array_create_C(B, 2, -rt_DOUBLE, (DvmType)n0, 0L, 0L, (DvmType)n1, 0L, 0L);
@@ -51,6 +51,14 @@ int wl_gsd2d_run(long n0, long n1, long sweeps, uint64_t seed, int dir0, int dir
             a[i * st[0] + j] =
                 (i == 0 || j == 0 || i == n0 - 1 || j == n1 - 1) ? 0.0 : wl_u01(seed, 17, (uint64_t)(i * n1 + j));
     dvmh_actual_array2_(A);
+    return 0;
+}
+
+/* `sweeps` sweeps; m_out[t] = m after sweep t (readEach) or m_out[0] = m after
+ * the last sweep.  dir0 / dir1: +1 forward, -1 backward loops. */
+int wl_gsd2d_sweeps(long sweeps, int dir0, int dir1, int readEach, int mirror, double *m_out) {
+    long t, n0 = N0, n1 = N1;
+    DvmType cur_region, cur_loop;
     for (t = 0; t < sweeps; t++) {
         m = 0;
         dvmh_actual_variable2_(&m);
@@ -85,15 +93,36 @@ int wl_gsd2d_run(long n0, long n1, long sweeps, uint64_t seed, int dir0, int dir
             m_out[readEach ? t : 0] = m;
         }
     }
+    return 0;
+}
+
+/* a_out (n0*n1) = A; b_out (n0*n1) = B when non-null */
+int wl_gsd2d_fetch(double *a_out, double *b_out) {
+    long i, st[2];
+    double *a = (double *)dvmh_get_natural_base_C(0, A), *b;
     dvmh_get_actual_array2_(A);
-    for (i = 0; i < n0; i++) memcpy(a_out + i * n1, a + i * st[0], sizeof(double) * n1);
-    if (mirror) {
+    wl_strides(A, 2, st);
+    for (i = 0; i < N0; i++) memcpy(a_out + i * N1, a + i * st[0], sizeof(double) * N1);
+    if (b_out) {
         dvmh_get_actual_array2_(B);
         b = (double *)dvmh_get_natural_base_C(0, B);
         wl_strides(B, 2, st);
-        for (i = 0; i < n0; i++) memcpy(b_out + i * n1, b + i * st[0], sizeof(double) * n1);
+        for (i = 0; i < N0; i++) memcpy(b_out + i * N1, b + i * st[0], sizeof(double) * N1);
     }
+    return 0;
+}
+
+int wl_gsd2d_free(void) {
     dvmh_array_free_C(B);
     dvmh_array_free_C(A);
     return 0;
+}
+
+/* the whole program: setup, sweeps, fetch (b_out when mirror), free */
+int wl_gsd2d_run(long n0, long n1, long sweeps, uint64_t seed, int dir0, int dir1, int readEach, int mirror,
+                 double *m_out, double *a_out, double *b_out) {
+    wl_gsd2d_setup(n0, n1, seed);
+    wl_gsd2d_sweeps(sweeps, dir0, dir1, readEach, mirror, m_out);
+    wl_gsd2d_fetch(a_out, mirror ? b_out : 0);
+    return wl_gsd2d_free();
 }

@@ -75,9 +75,18 @@ void dvmhgb_force_variant(int v);
  * numbered along the diagonal the loop sweeps (two or more).  Off, arrays
  * stay natural and autotransform reports 0.  Either way a device copy is
  * natural again before host copies and before any handler that did not ask
- * for the transform.  The tuner may also choose per loop (dvmhgb_tuner_*). */
+ * for the transform.  With tuning on (DVMH_OPT_PARAMS / dvmhgb_set_tuning),
+ * the tuner times each loop shape with the transform and without (twice
+ * each, in immediate execution) and keeps the faster. */
 void dvmhgb_set_autotransform(int on);
 int dvmhgb_get_autotransform(void);
+/* The layout the tuner keeps for the latest loop shape of a handler: 0
+ * natural, 1 transformed, -1 not yet measured both ways; best[0..1] (may be
+ * null) = fastest seconds seen natural / transformed (-1 = none). */
+int dvmhgb_tuner_layout(DvmHandlerFunc handler, double best[2]);
+/* Online tuning of CUDA blocks, variants and layouts: 0 off, 1 exhaustive,
+ * 2 model-guided (the same as DVMH_OPT_PARAMS at start-up). */
+void dvmhgb_set_tuning(int mode);
 
 /* Self-test of the integer-pipe FP64 operations against the FP64 unit on n
  * random operand pairs: mismatches[0..3] = add, sub, mul, division by 6. */

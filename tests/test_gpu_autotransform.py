@@ -29,6 +29,7 @@ def g():
     yield g
     g.set_mode("batched")
     g.runtime().dvmhgb_set_autotransform(1)
+    g.runtime().dvmhgb_set_tuning(0)
 
 
 def run(g, n0, n1, sweeps, seed, dirs=(1, 1), read_each=1, mirror=0):
@@ -96,3 +97,28 @@ def test_larger_grid_int_and_long_index(g):
     n0, n1, sweeps, seed = 300, 257, 2, 8
     m, a, b, s = run(g, n0, n1, sweeps, seed, dirs=(1, -1), read_each=1, mirror=0)
     check(m, a, b, n0, n1, sweeps, seed, (1, -1), 1, 0)
+
+
+def test_tuner_chooses_layout(g):
+    # tuning on: the loop runs twice transformed, twice natural, then keeps the faster layout;
+    # the results stay exact whichever layout each sweep ran in
+    rt, w = g.runtime(), g.workloads()
+    rt.dvmhgb_tuner_layout.argtypes = [ctypes.c_void_p, ctypes.POINTER(ctypes.c_double)]
+    rt.dvmhgb_tuner_layout.restype = ctypes.c_int
+    handler = ctypes.cast(w.loop_gsd2d_cuda, ctypes.c_void_p)
+    g.set_mode("plain")
+    rt.dvmhgb_set_autotransform(1)
+    rt.dvmhgb_set_tuning(1)
+    try:
+        n0, n1, sweeps, seed = 64, 48, 7, 21
+        m, a, b, s = run(g, n0, n1, sweeps, seed, dirs=(1, -1), read_each=1, mirror=0)
+        check(m, a, b, n0, n1, sweeps, seed, (1, -1), 1, 0)
+        best = (ctypes.c_double * 2)()
+        choice = rt.dvmhgb_tuner_layout(handler, best)
+        assert choice in (0, 1), (choice, list(best))
+        assert best[0] > 0 and best[1] > 0
+        # transformed for two sweeps, natural for two, then the choice (plus get_actual)
+        assert s["relayouts"] >= 2, s
+    finally:
+        rt.dvmhgb_set_tuning(0)
+        g.set_mode("batched")
