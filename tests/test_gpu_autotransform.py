@@ -122,3 +122,59 @@ def test_tuner_chooses_layout(g):
     finally:
         rt.dvmhgb_set_tuning(0)
         g.set_mode("batched")
+
+
+def rec2d_sequential(n0, n1, sweeps, seed):
+    L = orc.lib()
+    a = np.array([[L.orc_u01(seed, 19, i * n1 + j) for j in range(n1)] for i in range(n0)])
+    los = []
+    for _ in range(sweeps):
+        for j in range(1, n1):
+            a[:, j] = a[:, j] * 0.5 + a[:, j - 1] * 0.25
+        los.append(min(a[:, 1:].min(), 1.0))  # MIN of the loop, then the initial value 1.0
+    return np.array(los), a
+
+
+@pytest.mark.parametrize("mode", ["plain", "async", "batched"])
+@pytest.mark.parametrize("tfm", [1, 0])
+def test_one_dependence_permuted(g, mode, tfm):
+    # a recurrence along j over independent rows: with transforms the rows' axis is stored
+    # innermost (a permuted layout, header state 1), so the threads of one launch are adjacent
+    g.set_mode(mode)
+    rt, w = g.runtime(), g.workloads()
+    rt.dvmhgb_set_autotransform(tfm)
+    w.wl_rec2d_run.argtypes = [ctypes.c_long, ctypes.c_long, ctypes.c_long, ctypes.c_uint64,
+                               ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)]
+    n0, n1, sweeps, seed = 37, 52, 3, 4
+    lo = np.zeros(sweeps)
+    a = np.zeros(n0 * n1)
+    g.reset_stats()
+    assert w.wl_rec2d_run(n0, n1, sweeps, seed, orc.P(lo), orc.P(a)) == 0
+    s = g.stats()
+    lo_ref, a_ref = rec2d_sequential(n0, n1, sweeps, seed)
+    assert np.array_equal(a.reshape(n0, n1), a_ref)
+    assert np.array_equal(lo, lo_ref)
+    # transposed once for the time loop, back once for get_actual
+    assert s["relayouts"] == (2 if tfm else 0), s
+
+
+@pytest.mark.parametrize("mode", ["plain", "batched"])
+@pytest.mark.parametrize("tfm", [1, 0])
+def test_two_dependences_with_an_outer_axis(g, mode, tfm):
+    # rank 3: the two dependent axes diagonalised as one plane, the independent outer axis
+    # striding over whole planes; every plane is the 2-D program with its own seed
+    g.set_mode(mode)
+    rt, w = g.runtime(), g.workloads()
+    rt.dvmhgb_set_autotransform(tfm)
+    w.wl_gsd3d_run.argtypes = [ctypes.c_long, ctypes.c_long, ctypes.c_long, ctypes.c_long, ctypes.c_uint64,
+                               ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)]
+    n0, n1, n2, sweeps, seed = 5, 19, 27, 3, 40
+    m = np.zeros(sweeps)
+    a = np.zeros(n0 * n1 * n2)
+    g.reset_stats()
+    assert w.wl_gsd3d_run(n0, n1, n2, sweeps, seed, orc.P(m), orc.P(a)) == 0
+    s = g.stats()
+    planes = [orc.gsd2d_run(n1, n2, sweeps, seed + k) for k in range(n0)]
+    assert np.array_equal(a.reshape(n0, n1 * n2), np.stack([p[1] for p in planes]))
+    assert np.array_equal(m, np.max(np.stack([p[0] for p in planes]), axis=0))
+    assert s["relayouts"] == (2 if tfm else 0), s
