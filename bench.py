@@ -467,7 +467,50 @@ def extra_configs(g, stream):
     res["batched_over_plain"] = res["batched"]["value"] / res["plain"]["value"]
     out["heat_batched_256"] = {"unit": "cell-updates/s", "bytes_per_cell": 16, "cells": cells, **res}
     g.set_mode("batched")
+    out["gsd2d_layouts_2048"] = gsd2d_layouts(g, stream, 2048, 2)
     return out
+
+
+def gsd2d_layouts(g, stream, n, k):
+    """A generated two-dependence ACROSS handler (one launch per diagonal) with its
+    array natural, diagonalised as the reference chooses, and as the tuner chooses."""
+    import ctypes
+    import numpy as np
+    import torch
+    w, rt = g.workloads(), g.runtime()
+    w.wl_gsd2d_setup.argtypes = [ctypes.c_long, ctypes.c_long, ctypes.c_uint64]
+    w.wl_gsd2d_sweeps.argtypes = [ctypes.c_long, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                  ctypes.POINTER(ctypes.c_double)]
+    rt.dvmhgb_tuner_layout.argtypes = [ctypes.c_void_p, ctypes.POINTER(ctypes.c_double)]
+    m = np.zeros(8)
+    mp = m.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+    res = {}
+    for name, tfm, tune in (("natural", 0, 0), ("diagonal", 1, 0), ("tuned", 1, 1)):
+        rt.dvmhgb_set_autotransform(tfm)
+        w.wl_gsd2d_setup(n, n, SEED + 4)
+        if tune:
+            rt.dvmhgb_set_tuning(1)
+            g.set_mode("plain")
+            w.wl_gsd2d_sweeps(5, 1, 1, 1, 0, mp)  # the tuner's exploration
+            g.set_mode("batched")
+        for _ in range(2):
+            w.wl_gsd2d_sweeps(k, 1, 1, 0, 0, mp)
+        g.sync()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        w.wl_gsd2d_sweeps(k, 1, 1, 0, 0, mp)
+        e1.record(stream)
+        g.sync()
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / k
+        res[name] = {"ms_per_sweep": ms, "value": (n - 2) ** 2 / (ms * 1e-3)}
+        if tune:
+            choice = rt.dvmhgb_tuner_layout(ctypes.cast(w.loop_gsd2d_cuda, ctypes.c_void_p), None)
+            res[name]["choice"] = ["natural", "diagonal"][choice] if choice >= 0 else None
+            rt.dvmhgb_set_tuning(0)
+        w.wl_gsd2d_free()
+    rt.dvmhgb_set_autotransform(1)
+    return {"unit": "cell-updates/s", "launches_per_sweep": 2 * n - 5, **res}
 
 
 if __name__ == "__main__":
