@@ -1,5 +1,8 @@
-// CUDA handler of gsd2d.c in the shape cdvmh generates for an ACROSS loop with
-// two dependences when it is asked for automatic transforms
+// CUDA handler of gsd2d.c in the shape cdvmh generates for an ACROSS loop when
+// it is asked for automatic transforms (cdvmh/src/across.cpp:2788-2894): the
+// handler counts the loop's dependences (dvmh_loop_get_dependency_mask_C; a
+// dependent axis with a single iteration has no dependence) and calls the
+// case handler for that count.  The two-dependence case
 // (cdvmh/src/across.cpp:1393-1437, 1960-2170):
 //   - dvmh_loop_autotransform_C first, then the natural base and the header
 //     with its extended parameters; the kernel indexes the array through the
@@ -9,6 +12,8 @@
 //     from the largest index of the first loop axis down;
 //   - each block folds its cells' MAX in shared memory and folds that into its
 //     own reduction slot, which accumulates over all launches.
+// The one-dependence case (cdvmh/src/across.cpp:1700-1940) launches once per
+// value of the dependent index, the independent one across the threads.
 #include <cuda_runtime.h>
 
 #include <cassert>
@@ -97,9 +102,70 @@ Arr2<IndexT> arrayOf(double *base, const DvmType hdr[], DvmType tfm, const DvmTy
     return A;
 }
 
+// one launch per value of the dependent index (coords[idxs_0]); the independent
+// index runs across the threads
+template <typename IndexT>
+__global__ void loop_gsd2d_1_kernel(Arr2<IndexT> A, double m, double m_grid[], IndexT num_elem_1, IndexT base_0,
+                                    IndexT base_1, IndexT step_1, IndexT idxs_0, IndexT idxs_1) {
+    extern __shared__ double m_block[];
+    const unsigned nt = blockDim.x * blockDim.y * blockDim.z;
+    const unsigned t = threadIdx.x + blockDim.x * (threadIdx.y + blockDim.y * threadIdx.z);
+    const IndexT id = (IndexT)blockIdx.x * nt + t;
+    if (id < num_elem_1) {
+        IndexT coords[2];
+        coords[idxs_0] = base_0;
+        coords[idxs_1] = base_1 + id * step_1;
+        const IndexT i = coords[0], j = coords[1];
+        const double old = A(i, j);
+        const double v = (((A(i - 1, j) + A(i + 1, j)) + A(i, j - 1)) + A(i, j + 1)) * 0.25;
+        A(i, j) = v;
+        const double d = fabs(v - old);
+        m = d > m ? d : m;
+    }
+    m_block[t] = m;
+    __syncthreads();
+    for (unsigned s = 1; s < nt; s <<= 1) {
+        if (t % (2 * s) == 0 && t + s < nt) m_block[t] = m_block[t + s] > m_block[t] ? m_block[t + s] : m_block[t];
+        __syncthreads();
+    }
+    if (t == 0) m_grid[blockIdx.x] = m_block[0] > m_grid[blockIdx.x] ? m_block[0] : m_grid[blockIdx.x];
+}
+
 }  // namespace
 
-extern "C" void loop_gsd2d_cuda(DvmType *pLoopRef, DvmType A_hdr[], double *m_ptr) {
+extern "C" void loop_gsd2d_cuda_1_case(DvmType *pLoopRef, DvmType A_hdr[], double *m_ptr, int dependency_mask) {
+    (void)m_ptr;
+    DvmType loop_ref = *pLoopRef;
+    DvmType device_num = dvmh_loop_get_device_num_C(loop_ref);
+    dvmh_loop_autotransform_C(loop_ref, A_hdr);
+    double *A = (double *)dvmh_get_natural_base_C(device_num, A_hdr);
+    DvmType A_devHdr[5], A_extendedParams[7];
+    DvmType A_typeOfTransform = dvmh_fill_header_C(device_num, A, A_hdr, A_devHdr, A_extendedParams);
+    assert(A_typeOfTransform == 0 || A_typeOfTransform == 1 || A_typeOfTransform == 2);
+    if (A_typeOfTransform == 2) A_typeOfTransform += 4 * A_extendedParams[6];
+    DvmType boundsLow[2], boundsHigh[2], loopSteps[2], idxs[2];
+    dvmh_loop_fill_bounds_C(loop_ref, boundsLow, boundsHigh, loopSteps);
+    dvmh_change_filled_bounds2_C(boundsLow, boundsHigh, loopSteps, 2, dependency_mask, idxs);
+    dim3 threads(256, 1, 1);
+    cudaStream_t stream;
+    DvmType shared = 8;
+    dvmh_loop_cuda_get_config_C(loop_ref, shared, 0, &threads, &stream, &shared);
+    const long nt = (long)threads.x * threads.y * threads.z;
+    const long M0 = (boundsHigh[0] - boundsLow[0]) / loopSteps[0] + 1;  // the dependent axis
+    const long M1 = (boundsHigh[1] - boundsLow[1]) / loopSteps[1] + 1;
+    const Arr2<long long> Ah = arrayOf<long long>(A, A_devHdr, A_typeOfTransform, A_extendedParams);
+    double m, *m_grid;
+    dvmh_loop_cuda_register_red_C(loop_ref, 1, (void **)&m_grid, 0);
+    dvmh_loop_red_init_C(loop_ref, 1, &m, 0);
+    dvmh_loop_cuda_red_prepare_C(loop_ref, 1, (M1 + nt - 1) / nt, 1);
+    const dim3 blocks((unsigned)((M1 + nt - 1) / nt), 1, 1);
+    for (long q = 0; q < M0; q++)
+        loop_gsd2d_1_kernel<long long><<<blocks, threads, shared, stream>>>(
+            Ah, m, m_grid, M1, boundsLow[0] + q * loopSteps[0], boundsLow[1], loopSteps[1], idxs[0], idxs[1]);
+    dvmh_loop_cuda_red_finish_C(loop_ref, 1);
+}
+
+extern "C" void loop_gsd2d_cuda_3_case(DvmType *pLoopRef, DvmType A_hdr[], double *m_ptr, int dependency_mask) {
     (void)m_ptr;
     DvmType loop_ref = *pLoopRef;
     DvmType device_num = dvmh_loop_get_device_num_C(loop_ref);
@@ -112,8 +178,7 @@ extern "C" void loop_gsd2d_cuda(DvmType *pLoopRef, DvmType A_hdr[], double *m_pt
 
     DvmType boundsLow[2], boundsHigh[2], loopSteps[2], idxs[2];
     dvmh_loop_fill_bounds_C(loop_ref, boundsLow, boundsHigh, loopSteps);
-    dvmh_change_filled_bounds2_C(boundsLow, boundsHigh, loopSteps, 2, dvmh_loop_get_dependency_mask_C(loop_ref),
-                                 idxs);
+    dvmh_change_filled_bounds2_C(boundsLow, boundsHigh, loopSteps, 2, dependency_mask, idxs);
     int kernelIndexT = dvmh_loop_guess_index_type_C(loop_ref);
     if (kernelIndexT == rt_LONG) kernelIndexT = (sizeof(long) <= sizeof(int) ? rt_INT : rt_LLONG);
     assert(kernelIndexT == rt_INT || kernelIndexT == rt_LLONG);
@@ -130,6 +195,19 @@ extern "C" void loop_gsd2d_cuda(DvmType *pLoopRef, DvmType A_hdr[], double *m_pt
     else
         sweep<long long>(loop_ref, arrayOf<long long>(A, A_devHdr, A_typeOfTransform, A_extendedParams), boundsLow,
                          loopSteps, M0, M1, threads, stream, shared);
+}
+
+// the handler: the case for the loop's number of dependences
+extern "C" void loop_gsd2d_cuda(DvmType *pLoopRef, DvmType A_hdr[], double *m_ptr) {
+    int dependency_mask = (int)dvmh_loop_get_dependency_mask_C(*pLoopRef);
+    int dependency_mask_tmp = dependency_mask;
+    int dependency_num = 0;
+    while (dependency_mask_tmp) {
+        dependency_mask_tmp &= (dependency_mask_tmp - 1);
+        ++dependency_num;
+    }
+    if (dependency_num == 1) loop_gsd2d_cuda_1_case(pLoopRef, A_hdr, m_ptr, dependency_mask);
+    else if (dependency_num == 2) loop_gsd2d_cuda_3_case(pLoopRef, A_hdr, m_ptr, dependency_mask);
 }
 
 // The mirror loop B = 2 A over the whole array, in cdvmh's plain shape (no

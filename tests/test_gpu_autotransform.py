@@ -178,3 +178,21 @@ def test_two_dependences_with_an_outer_axis(g, mode, tfm):
     assert np.array_equal(a.reshape(n0, n1 * n2), np.stack([p[1] for p in planes]))
     assert np.array_equal(m, np.max(np.stack([p[0] for p in planes]), axis=0))
     assert s["relayouts"] == (2 if tfm else 0), s
+
+
+@pytest.mark.parametrize("mode", ["plain", "batched"])
+@pytest.mark.parametrize("tfm", [1, 0])
+@pytest.mark.parametrize("shape,moved", [((3, 30), True), ((30, 3), False), ((3, 3), False)])
+def test_dispatcher_single_iteration_axes(g, mode, tfm, shape, moved):
+    # a dependent axis with one iteration carries no dependence: the generated handler's
+    # dispatcher counts one and takes the one-dependence case; with the rows' axis the only
+    # independent one (3 x n), the reference's rule stores it innermost (a transposed layout)
+    g.set_mode(mode)
+    g.runtime().dvmhgb_set_autotransform(tfm)
+    n0, n1 = shape
+    m, a, b, s = run(g, n0, n1, 3, 6, dirs=(1, -1), read_each=1, mirror=1)
+    check(m, a, b, n0, n1, 3, 6, (1, -1), 1, 1)
+    if tfm and moved:
+        assert s["relayouts"] >= 2, s
+    elif not tfm:
+        assert s["relayouts"] == 0, s
