@@ -333,6 +333,7 @@ void fillDesc(Array *a);
 void queueFlush();  // run or replay everything queued (batched mode)
 bool queueBusy();
 void loopsAtExit();
+void graphsForget(const Array *a);  // drop the cached graphs that name a freed array
 void noteSwap(Array *a);          // a device buffer swap, recorded when a graph is being captured
 void noteLayout(Array *a);        // a layout change, likewise
 bool inHandlerCall();             // a handler is running

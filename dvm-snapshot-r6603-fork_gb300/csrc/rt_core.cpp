@@ -449,6 +449,7 @@ void dvmh_array_free_C(DvmType dvmDesc[]) {
     GB_CHECK(!st.curRegion, "dvmh_array_free inside a region");
     queueFlush();
     streamSync();
+    graphsForget(a);
     if (a->dev) devFree(a->dev);
     if (a->devAlt) devFree(a->devAlt);
     if (a->host) hostFree(a->host);

@@ -412,6 +412,7 @@ static std::vector<uint64_t> signature(const std::vector<Loop *> &q) {
             sigAdd(s, (uint64_t)l->cuda.params[i]);
             if (isArrayDesc(l->cuda.params[i])) {
                 Array *a = (Array *)((const DvmType *)l->cuda.params[i])[0];
+                sigAdd(s, (uint64_t)a);  // the object the graph's swap and layout records name
                 sigAdd(s, (uint64_t)a->dev);
                 sigAdd(s, (uint64_t)a->devAlt);
                 uint64_t lay = (uint64_t)a->tdiag;
@@ -514,6 +515,23 @@ void queueFlush() {
     }
     for (Loop *l : q) deleteLoop(l);
     if (settings.syncEachLoop) streamSync();
+}
+
+// An array is freed: no cached graph may name it any more (a later array could
+// reuse its descriptor and buffers, and the graph's records would then name a
+// dead object).
+void graphsForget(const Array *a) {
+    for (auto it = graphCache.begin(); it != graphCache.end();) {
+        bool names = std::find(it->sig.begin(), it->sig.end(), (uint64_t)a) != it->sig.end();
+        for (const Array *x : it->swaps) names = names || x == a;
+        for (auto &pl : it->layouts) names = names || pl.first == a;
+        if (names) {
+            dropGraph(*it);
+            it = graphCache.erase(it);
+        } else {
+            ++it;
+        }
+    }
 }
 
 void loopsAtExit() {

@@ -196,3 +196,15 @@ def test_dispatcher_single_iteration_axes(g, mode, tfm, shape, moved):
         assert s["relayouts"] >= 2, s
     elif not tfm:
         assert s["relayouts"] == 0, s
+
+
+def test_freed_arrays_leave_no_cached_graphs(g):
+    # a program run twice: the second run's arrays reuse the first run's descriptors and
+    # (pooled) device buffers, but graphs recorded for the freed arrays are not replayed
+    g.set_mode("batched")
+    g.runtime().dvmhgb_set_autotransform(1)
+    n0, n1, sweeps, seed = 24, 20, 3, 12
+    for rep in range(2):
+        m, a, b, s = run(g, n0, n1, sweeps, seed, dirs=(1, 1), read_each=1, mirror=1)
+        check(m, a, b, n0, n1, sweeps, seed, (1, 1), 1, 1)
+        assert s["graphs_captured"] >= 1, (rep, s)
