@@ -468,7 +468,42 @@ def extra_configs(g, stream):
     out["heat_batched_256"] = {"unit": "cell-updates/s", "bytes_per_cell": 16, "cells": cells, **res}
     g.set_mode("batched")
     out["gsd2d_layouts_2048"] = gsd2d_layouts(g, stream, 2048, 2)
+    out["jacobi2d_1024"] = jacobi2d(g, stream, 1024, 100)
     return out
+
+
+def jacobi2d(g, stream, n, iters):
+    """The 2-D Jacobi configuration (1024^2, 100 iterations of update + renew + stencil
+    with a MAX reduction each), on the GPU in every mode, beside the CPU port."""
+    import torch
+    from oracle import orc
+    res = {}
+    for mode in ("batched", "async", "plain"):
+        g.set_mode(mode)
+        j = g.Jacobi(2, n, SEED)
+        j.run(3)
+        g.sync()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        j.run(iters)
+        e1.record(stream)
+        g.sync()
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / iters
+        j.close()
+        res[mode] = {"ms_per_iteration": ms, "value": (n - 2) ** 2 / (ms * 1e-3)}
+    g.set_mode("batched")
+    L = orc.lib()
+    threads = L.orc_max_threads()
+    A, B = orc.jacobi_init(2, n, SEED)
+    L.orc_jacobi_step(2, n, orc.P(A), orc.P(B), threads)
+    t0 = time.time()
+    for _ in range(iters):
+        L.orc_jacobi_step(2, n, orc.P(A), orc.P(B), threads)
+    dt = time.time() - t0
+    res["cpu_port"] = {"value": (n - 2) ** 2 * iters / dt, "cores": threads,
+                       "ms_per_iteration": 1e3 * dt / iters}
+    return {"unit": "cell-updates/s", "bytes_per_cell": 32, **res}
 
 
 def gsd2d_layouts(g, stream, n, k):
