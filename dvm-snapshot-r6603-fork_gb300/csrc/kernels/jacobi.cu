@@ -633,7 +633,7 @@ St2Geom st2Geom(const long lo[2], const long hi[2]) {
     if (chunks < 1) chunks = 1;
     if (chunks > ni) chunks = ni;
     long ichunk = (ni + chunks - 1) / chunks;
-    if (ichunk < 16 && ni >= 16) ichunk = 16;
+    if (ichunk < 4 && ni >= 4) ichunk = 4;  // halo rows cost 2 / ichunk extra reads
     g.ichunk = (int)ichunk;
     long gy = (ni + ichunk - 1) / ichunk;
     g.ok = g.ok && gx < (1L << 31) && gy < 65536;

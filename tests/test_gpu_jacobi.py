@@ -50,10 +50,11 @@ def test_jacobi2d_cpu_config_golden(g, golden):
     assert sha(A) == c["A_sha256"] and sha(B) == c["B_sha256"]
 
 
-@pytest.mark.parametrize("rank,n,iters", [(3, 5, 2), (3, 33, 4), (3, 66, 3), (3, 129, 2), (2, 5, 3), (2, 65, 6),
-                                          (2, 300, 5)])
+@pytest.mark.parametrize("rank,n,iters", [(3, 5, 2), (3, 33, 4), (3, 66, 3), (3, 129, 2), (2, 5, 3), (2, 6, 3),
+                                          (2, 7, 2), (2, 11, 4), (2, 65, 6), (2, 300, 5), (2, 1027, 2)])
 def test_jacobi_vs_oracle_sizes(g, rank, n, iters):
-    """Ragged sizes: extents around the 64-element tiles and 16-row tiles."""
+    """Ragged sizes: extents around the 64-element tiles and the 2-D kernels' row chunks
+    (4 rows at the least: interiors of 3, 4, 5, 9 and 1025 rows)."""
     seed = 1000 + n
     e_ref, A_ref, B_ref = orc.jacobi_run(rank, n, iters, seed, threads=8)
     for mode in MODES:
