@@ -190,7 +190,7 @@ def main():
     ap.add_argument("--impl", default="gb300")
     ap.add_argument("--grid", type=int, default=N_DEFAULT)
     ap.add_argument("--quick", action="store_true", help="headline only (no extra modes/configs/cpu leg)")
-    ap.add_argument("--only", choices=["jacobi3d", "sor", "heat", "gsd2d"], default=None,
+    ap.add_argument("--only", choices=["jacobi3d", "jacobi2d", "sor", "heat", "gsd2d"], default=None,
                     help="time one workload alone (small cases for profiling): --grid is its size "
                          "(heat: the largest side), --steps its steps or sweeps")
     ap.add_argument("--mode", choices=["batched", "async", "plain"], default="batched", help="with --only")
@@ -346,6 +346,9 @@ def run_only(args, g, stream):
     if args.only == "jacobi3d":
         w = g.Jacobi(3, args.grid, SEED)
         cells, unit = (args.grid - 2) ** 3, "step"
+    elif args.only == "jacobi2d":
+        w = g.Jacobi(2, args.grid, SEED)
+        cells, unit = (args.grid - 2) ** 2, "iteration"
     elif args.only == "sor":
         w = g.Sor(args.grid, 1.5, SEED + 2)
         cells, unit = (args.grid - 2) ** 3, "sweep"
