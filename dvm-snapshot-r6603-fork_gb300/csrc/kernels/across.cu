@@ -309,8 +309,8 @@ bool geo(const long st[3], const long ext[3], const long lo[3], const long hi[3]
     return true;
 }
 
-// variant -> TK: 0 -> 32, 1 -> 16, 2 -> 8
-int tkOf(int variant) { return variant == 0 ? 32 : (variant == 1 ? 16 : (variant == 2 ? 8 : 0)); }
+// variant -> TK: 0 -> 32, 1 -> 16, 2 -> 8; 3: streaming columns (items as for TK = 64: one per 64-wide chunk)
+int tkOf(int variant) { return variant == 0 ? 32 : (variant == 1 ? 16 : (variant == 2 ? 8 : (variant == 3 ? 64 : 0))); }
 
 template <int TK>
 int sweepT(double *A, const Geo &g, const double *wDev, double *items, void *scratch, int *status, cudaStream_t s) {
@@ -334,6 +334,232 @@ int sweepT(double *A, const Geo &g, const double *wDev, double *items, void *scr
     long gridCap = (ntiles + WPB - 1) / WPB;
     if (grid > gridCap) grid = gridCap;
     kSorWave<TK><<<(unsigned)grid, NT, smem, s>>>(A, g, wDev, done, counter, items, status);
+    dvmhgb_count_launches(1);
+    return cudaGetLastError() == cudaSuccess ? 0 : -1;
+}
+
+// ---------------------------------------------------------------- streaming columns (variant 3)
+//
+// One warp owns a column of 4 x 8 rows (lane (li, lj) -> row (i0 + li, j0 + lj))
+// and streams it along k: at step s lane (li, lj) updates position
+// p = s - li - lj, so a cell sees its -i / -j / -k neighbours new and its
+// +i / +j / +k neighbours old, the values the sequential order gives it.
+// Neighbour rows inside the column come by warp shuffles: the new value a lane
+// computed one step earlier (-i, -j) and the old value a lane holds one
+// position ahead (+i, +j).  The column's -i / -j faces are the last rows of
+// the predecessor columns (a-1, b) and (a, b-1), read through L2 once they are
+// published; its +i / +j faces are old values.  Every SC steps a column
+// publishes how many leading positions all its rows have stored (after a
+// fence); a successor waits (bounded) for the positions it reads.  A column
+// has one skew ramp for the whole sweep, where a tile has one per TK
+// positions: on GB300 an FP64 warp instruction costs the same whatever its
+// active lanes, so the ramps were a third of the tiles' update instructions.
+// Residual: every lane keeps (nv - old)^2 of its recent positions in shared
+// memory; after each group the positions all lanes have finished enter the
+// canonical pairwise tree of their 64-wide chunk, with every lane at the same
+// position (warp-uniform branches).  One item per row and 64-wide chunk.
+constexpr int SC = 16;            // steps per group (publication granularity)
+constexpr int SKEW = TI + TJ - 2;  // the last lane's lag behind lane 0
+constexpr int SQR = 32;           // positions of squares kept per lane (>= SC + SKEW)
+constexpr int SWPB = 4;           // column-warps per CTA
+constexpr int SNT = 32 * SWPB;
+
+struct SGeo {
+    long s0, s1;
+    long e0, e1, e2;
+    long lo0, lo1, lo2, hi0, hi1, hi2;
+    long na, nb, nk;  // columns along i and j; positions along k
+    long nj;          // rows per i in the item layout
+    long kc0, nch;    // first 64-wide chunk of k; chunks per row
+};
+
+// columns are handed out by diagonal d = a + b; #{(a, b) in box : a + b < d}
+__device__ __forceinline__ long long below2(long long m) { return m > 0 ? m * (m + 1) / 2 : 0; }
+__device__ __forceinline__ void colAt(const SGeo &g, long idx, long &a, long &b) {
+    long lo = 0, hi = g.na + g.nb - 2;  // last d with count(< d) <= idx
+    while (lo < hi) {
+        const long mid = (lo + hi + 1) >> 1;
+        const long long c = below2(mid) - below2(mid - g.na) - below2(mid - g.nb) + below2(mid - g.na - g.nb);
+        if (c <= idx) lo = mid;
+        else hi = mid - 1;
+    }
+    const long d = lo;
+    const long long before = below2(d) - below2(d - g.na) - below2(d - g.nb) + below2(d - g.na - g.nb);
+    const long amin = d - (g.nb - 1) > 0 ? d - (g.nb - 1) : 0;
+    a = amin + (idx - (long)before);
+    b = d - a;
+}
+
+__device__ __forceinline__ double ldAt(const double *A, const SGeo &g, long i, long j, long k) {
+    return (i >= 0 && i < g.e0 && j >= 0 && j < g.e1 && k >= 0 && k < g.e2) ? __ldcg(A + i * g.s0 + j * g.s1 + k)
+                                                                             : 0.0;
+}
+
+// bounded wait until *f >= want; false (status written, counter stopped) when it runs out
+__device__ __forceinline__ bool waitProgress(const int *f, int want, int *status, unsigned *counter) {
+    long n = 0;
+    while (ldAcquire(f) < want) {
+        if (++n > SPIN_LIMIT) {
+            atomicExch(status, ERR_SOR_TIMEOUT);
+            atomicOr(counter, 0x80000000u);
+            return false;
+        }
+        __nanosleep(64);
+    }
+    return true;
+}
+
+__global__ void __launch_bounds__(SNT) kSorStream(double *A, SGeo g, const double *wPtr, int *prog, unsigned *counter,
+                                                  double *items, int *status) {
+    __shared__ double sqs[SWPB][32][SQR + 1];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, li = lane / TJ, lj = lane % TJ, sk = li + lj;
+    double *sq = sqs[warp][lane];
+    const double w = *wPtr;
+    const double c1 = 1.0 - w, c2 = w / 6.0;  // loop invariants, rounded as in the source expression
+    const long ncols = g.na * g.nb;
+    const int nk = (int)g.nk;
+    while (true) {
+        long idx = 0;
+        if (lane == 0) idx = (long)atomicAdd(counter, 1u);  // >= 2^31 once a warp has failed
+        idx = __shfl_sync(0xffffffffu, idx, 0);
+        if (idx >= ncols) break;
+        long a, b;
+        colAt(g, idx, a, b);
+        const long i = g.lo0 + a * TI + li, j = g.lo1 + b * TJ + lj;
+        const bool row = i <= g.hi0 && j <= g.hi1;
+        // the faces a boundary lane reads: -i / +i (li = 0 / TI-1), -j / +j (lj = 0 / TJ-1)
+        const long fi = li == 0 ? i - 1 : i + 1, fj = lj == 0 ? j - 1 : j + 1;
+        const bool hasFi = li == 0 || li == TI - 1, hasFj = lj == 0 || lj == TJ - 1;
+        const int *predI = a > 0 ? prog + (a - 1) * g.nb + b : nullptr;
+        const int *predJ = b > 0 ? prog + a * g.nb + (b - 1) : nullptr;
+        double res = ldAt(A, g, i, j, g.lo2 - 1);  // the value at the position before p: the k - 1 neighbour
+        double stk[6];
+#pragma unroll
+        for (int l = 0; l < 6; l++) stk[l] = -0.0;
+        int done = 0;  // positions whose squares have entered the trees
+        const int G = (nk + SKEW + SC - 1) / SC;
+        for (int gr = 0; gr < G; gr++) {
+            const int p0 = gr * SC - sk;  // this lane's first position in the group
+            // 1. the predecessors' rows up to the group's last position (lane (0, 0) reaches gr*SC + SC - 1)
+            const int want = min(nk, gr * SC + SC);
+            int fail = 0;
+            if (lane == 0 && predI && !waitProgress(predI, want, status, counter)) fail = 1;
+            if (lane == 1 && predJ && !waitProgress(predJ, want, status, counter)) fail = 1;
+            if (__any_sync(0xffffffffu, fail)) return;
+            __syncwarp();  // orders the acquiring lanes' loads before every lane's face loads
+            // 2. the group's values: own row positions p0 .. p0 + SC (one ahead), the faces p0 .. p0 + SC - 1
+            double own[SC + 1], fI[SC], fJ[SC];
+#pragma unroll
+            for (int u = 0; u <= SC; u++) own[u] = ldAt(A, g, i, j, g.lo2 + p0 + u);
+#pragma unroll
+            for (int u = 0; u < SC; u++) {
+                fI[u] = hasFi ? ldAt(A, g, fi, j, g.lo2 + p0 + u) : 0.0;
+                fJ[u] = hasFj ? ldAt(A, g, i, fj, g.lo2 + p0 + u) : 0.0;
+            }
+            // 3. the steps
+#pragma unroll
+            for (int u = 0; u < SC; u++) {
+                const int p = p0 + u;
+                const double cur = own[u], nxt = own[u + 1];
+                const double upI = __shfl_up_sync(0xffffffffu, res, TJ), dnI = __shfl_down_sync(0xffffffffu, nxt, TJ);
+                const double upJ = __shfl_up_sync(0xffffffffu, res, 1), dnJ = __shfl_down_sync(0xffffffffu, nxt, 1);
+                const double xim = li == 0 ? fI[u] : upI, xip = li == TI - 1 ? fI[u] : dnI;
+                const double xjm = lj == 0 ? fJ[u] : upJ, xjp = lj == TJ - 1 ? fJ[u] : dnJ;
+                if (row && p >= 0 && p < nk) {
+                    // A[i-1] + A[i+1] + A[j-1] + A[j+1] + A[k-1] + A[k+1], left to right
+                    const double sum = ((((xim + xip) + xjm) + xjp) + res) + nxt;
+                    const double nv = c1 * cur + c2 * sum;
+                    A[i * g.s0 + j * g.s1 + g.lo2 + p] = nv;
+                    const double dl = nv - cur;
+                    sq[p & (SQR - 1)] = dl * dl;
+                    res = nv;
+                } else {
+                    res = cur;
+                }
+            }
+            // 4. publish the positions every row has stored
+            const int fin = min(nk, max(0, gr * SC + SC - SKEW));
+            __threadfence();
+            __syncwarp();
+            if (lane == 0) stRelease(prog + a * g.nb + b, gr == G - 1 ? nk : fin);
+            // 5. the residual of the finished positions, every lane at the same position
+            const int upto = gr == G - 1 ? nk : fin;
+            for (; done < upto; done++) {
+                const long k = g.lo2 + done;
+                const int q = (int)(k & 63);
+                double v = row ? sq[done & (SQR - 1)] : -0.0;
+#pragma unroll
+                for (int l = 0; l < 6; l++) {
+                    if (!((q >> l) & 1)) {
+                        stk[l] = v;
+                        break;
+                    }
+                    v = stk[l] + v;
+                }
+                if (q == 63 || done == nk - 1) {
+                    // the chunk's remaining positions are the identity: complete its tree
+                    double root = v;
+                    if (q != 63) {
+                        root = -0.0;
+                        for (int qq = q + 1; qq <= 63; qq++) {
+                            double x = -0.0;
+                            for (int l = 0; l < 6; l++) {
+                                if (!((qq >> l) & 1)) {
+                                    stk[l] = x;
+                                    break;
+                                }
+                                x = stk[l] + x;
+                            }
+                            root = x;
+                        }
+                    }
+                    if (row) items[((i - g.lo0) * g.nj + (j - g.lo1)) * g.nch + ((k >> 6) - g.kc0)] = root;
+#pragma unroll
+                    for (int l = 0; l < 6; l++) stk[l] = -0.0;
+                }
+            }
+            __syncwarp();
+        }
+    }
+}
+
+int sweepStream(double *A, const Geo &g0, const double *wDev, double *items, void *scratch, int *status,
+                cudaStream_t s) {
+    SGeo g;
+    g.s0 = g0.s0;
+    g.s1 = g0.s1;
+    g.e0 = g0.e0;
+    g.e1 = g0.e1;
+    g.e2 = g0.e2;
+    g.lo0 = g0.lo0;
+    g.lo1 = g0.lo1;
+    g.lo2 = g0.lo2;
+    g.hi0 = g0.hi0;
+    g.hi1 = g0.hi1;
+    g.hi2 = g0.hi2;
+    g.na = g0.na;
+    g.nb = g0.nb;
+    g.nk = g0.hi2 - g0.lo2 + 1;
+    g.nj = g0.nj;
+    g.kc0 = g0.lo2 / 64;
+    g.nch = g0.hi2 / 64 - g0.lo2 / 64 + 1;
+    const long ncols = g.na * g.nb;
+    if (ncols >= (1L << 30) || g.nk >= (1L << 30) || g.lo2 < 1) return -1;
+    unsigned *counter = (unsigned *)scratch;
+    int *prog = (int *)scratch + 64;  // counter on its own 256-byte line
+    if (cudaMemsetAsync(scratch, 0, (size_t)(ncols + 64) * sizeof(int), s) != cudaSuccess) return -1;
+    static int occ = 0, sms = 0;
+    if (!occ) {
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kSorStream, SNT, 0);
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        if (occ < 1) occ = 1;
+    }
+    long grid = (long)occ * sms;  // all CTAs resident at once: waits always resolve
+    const long gridCap = (ncols + SWPB - 1) / SWPB;
+    if (grid > gridCap) grid = gridCap;
+    kSorStream<<<(unsigned)grid, SNT, 0, s>>>(A, g, wDev, prog, counter, items, status);
     dvmhgb_count_launches(1);
     return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }
@@ -362,6 +588,7 @@ int dvmhgb_sor3d_sweep(double *A, const long st[3], const long ext[3], const lon
     if (!tk || !A || !wDev || !items || !scratch || !status || !geo(st, ext, lo, hi, 64 / tk, g)) return -1;
     cudaStream_t s = (cudaStream_t)stream;
     switch (tk) {
+        case 64: return sweepStream(A, g, wDev, items, scratch, status, s);
         case 32: return sweepT<32>(A, g, wDev, items, scratch, status, s);
         case 16: return sweepT<16>(A, g, wDev, items, scratch, status, s);
         default: return sweepT<8>(A, g, wDev, items, scratch, status, s);

@@ -39,11 +39,11 @@ def close_sum(a, b, n):
     return np.all(np.abs(a - b) <= 2 * gamma * np.abs(b) + 1e-300)
 
 
-@pytest.mark.parametrize("variant", [0, 1, 2])
+@pytest.mark.parametrize("variant", [0, 1, 2, 3])
 @pytest.mark.parametrize("mode", MODES)
 def test_sor_golden(g, golden, mode, variant):
     g.set_mode(mode)
-    g.force_variant(variant)  # tile depth along k: 32, 16, 8
+    g.force_variant(variant)  # tile depth along k: 32, 16, 8; 3: streaming columns
     for name, c in golden.items():
         if c["prog"] != "sor3d":
             continue
@@ -58,7 +58,7 @@ def test_sor_golden(g, golden, mode, variant):
         assert close_sum(res, unhex(c["s"]), (n - 2) ** 3), name
 
 
-@pytest.mark.parametrize("variant", [0, 1, 2])
+@pytest.mark.parametrize("variant", [0, 1, 2, 3])
 @pytest.mark.parametrize("n", [4, 9, 17, 66, 75, 131])
 def test_sor_sizes_vs_oracle(g, n, variant):
     seq, canon, A_ref = orc.sor_run(n, 3, 1.5, 77 + n)

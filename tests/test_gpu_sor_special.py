@@ -38,7 +38,7 @@ def special_grid(n, seed):
     return A.ravel().copy()
 
 
-@pytest.mark.parametrize("variant", [0, 1, 2])
+@pytest.mark.parametrize("variant", [0, 1, 2, 3])
 @pytest.mark.parametrize("omega", [1.5, 1.25, 1.0])
 def test_sor_kernel_special_values(g, variant, omega):
     import torch
