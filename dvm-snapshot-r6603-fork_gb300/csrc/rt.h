@@ -68,6 +68,7 @@ struct Settings {
     bool fuse = true;
     bool hostProf = false;      // DVMH_GB_HOSTPROF: time the ABI entry points on the host
     bool autoTfm = true;        // DVMH_GB_AUTOTFM: honour dvmh_loop_autotransform_C (else keep natural layouts)
+    bool reduceDeps = false;    // DVMH_REDUCE_DEPS: no dependence on ACROSS axes with one iteration
 };
 extern Settings settings;
 
@@ -326,6 +327,7 @@ void ensureHostActual(Array *a);
 void ensureVarDev(Var *v);
 void varH2D(Var *v);
 void varD2H(Var *v);
+void varForgetStaging(const Var *v);  // the variable is dropped: its pinned staging buffer too
 void fillDesc(Array *a);
 
 // ---------------------------------------------------------------- loops / batching (rt_loop.cpp)
@@ -333,7 +335,7 @@ void fillDesc(Array *a);
 void queueFlush();  // run or replay everything queued (batched mode)
 bool queueBusy();
 void loopsAtExit();
-void graphsForget(const Array *a);  // drop the cached graphs that name a freed array
+void graphsForget(const Obj *a);  // drop the cached graphs that name a freed array or variable
 void noteSwap(Array *a);          // a device buffer swap, recorded when a graph is being captured
 void noteLayout(Array *a);        // a layout change, likewise
 bool inHandlerCall();             // a handler is running
@@ -348,6 +350,8 @@ void makeNatural(Array *a);
 // state dvmh_fill_header_C reports (0 natural, 1 permuted, 2 diagonalised)
 int autotransform(const Loop *l, Array *a);
 int layoutState(const Array *a);
+// the loop axis (1-based) that array axis `axis` (0-based) follows, 0 if none
+int loopAxisOf(const Loop *l, const Array *a, int axis);
 // header coefficients and diagonal parameters of the current device layout
 void layoutHeader(const Array *a, long coef[], long ext7[7]);
 void alignIdentity(AlignMap &m, const Obj *self, int rank);

@@ -40,6 +40,14 @@ void fatal(const char *kind, const char *file, int line, const char *fmt, ...) {
     fprintf(stderr, "libdvmh_gb %s at %s:%ld (%s:%d): %s\n", kind, st.file.empty() ? "?" : st.file.c_str(), st.line,
             base ? base + 1 : file, line, buf);
     fflush(stderr);
+    // DVMH_GB_ERROR_LOG: the same line appended to a file (for hosts that capture stderr)
+    if (const char *path = getenv("DVMH_GB_ERROR_LOG")) {
+        if (FILE *f = fopen(path, "a")) {
+            fprintf(f, "libdvmh_gb %s at %s:%ld (%s:%d): %s\n", kind, st.file.empty() ? "?" : st.file.c_str(),
+                    st.line, base ? base + 1 : file, line, buf);
+            fclose(f);
+        }
+    }
     // reference convention: user errors exit(1), internal errors abort (rts/dvmh/dvmh_log.h:75-100)
     if (!strcmp(kind, "internal"))
         abort();
@@ -122,6 +130,7 @@ static void loadSettings() {
     if (const char *h = getenv("DVMH_GB_HOSTPROF")) settings.hostProf = atoi(h) != 0;
     if (const char *f = getenv("DVMH_GB_FUSE")) settings.fuse = atoi(f) != 0;
     if (const char *t = getenv("DVMH_GB_AUTOTFM")) settings.autoTfm = atoi(t) != 0;
+    if (const char *r = getenv("DVMH_REDUCE_DEPS")) settings.reduceDeps = atoi(r) != 0;
 }
 
 static void track(Obj *o) { liveObjs.insert(o); }
@@ -158,6 +167,17 @@ Var *varAt(const void *addr, size_t *off) {
     return nullptr;
 }
 
+// forget a variable: its cached graphs, its device copy, its registry entry
+static void dropVar(Var *v) {
+    streamSync();
+    graphsForget(v);
+    if (v->dev) devFree(v->dev);
+    varForgetStaging(v);
+    st.vars.erase(v->addr);
+    untrack(v);
+    delete v;
+}
+
 Var *varGet(const void *addr, size_t size) {
     auto it = st.vars.find((const char *)addr);
     if (it != st.vars.end()) {
@@ -172,9 +192,26 @@ Var *varGet(const void *addr, size_t size) {
         }
         return v;
     }
-    size_t off;
-    Var *outer = varAt(addr, &off);
-    GB_CHECK(!outer, "variable at %p overlaps the registered variable '%s'", addr, outer ? outer->name.c_str() : "");
+    // variables known from earlier regions and loops that overlap the new one: the
+    // program's memory there now holds something else -- unless the current
+    // region registered them, they are forgotten (their device copies with them)
+    const char *lo = (const char *)addr, *hi = lo + size;
+    auto first = st.vars.upper_bound(lo);
+    if (first != st.vars.begin()) --first;
+    std::vector<Var *> stale;
+    for (auto it = first; it != st.vars.end() && it->first < hi; ++it)
+        if (it->second->addr + it->second->size > lo) stale.push_back(it->second);
+    if (!stale.empty()) {
+        queueFlush();  // queued loops may still name them
+        for (Var *o : stale) {
+            bool inRegion = false;
+            if (st.curRegion)
+                for (auto &rv : st.curRegion->vars) inRegion = inRegion || rv.var == o;
+            GB_CHECK(!inRegion, "variable at %p overlaps the variable '%s' registered in this region", addr,
+                     o->name.c_str());
+            dropVar(o);
+        }
+    }
     Var *v = new Var();
     v->addr = (const char *)addr;
     v->size = size;

@@ -298,6 +298,17 @@ void varH2D(Var *v) {
     stats.h2d_bytes += (long)v->size;
 }
 
+void varForgetStaging(const Var *v) {
+    auto it = staging.find(v);
+    if (it == staging.end()) return;
+    if (it->second.done) {
+        cudaEventSynchronize(it->second.done);
+        cudaEventDestroy(it->second.done);
+    }
+    if (it->second.buf) hostFree(it->second.buf);
+    staging.erase(it);
+}
+
 void varD2H(Var *v) {
     GB_PROF("varD2H");
     GB_INTERNAL(v->dev, "variable without a device copy");

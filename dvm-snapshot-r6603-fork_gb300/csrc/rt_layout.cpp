@@ -144,6 +144,16 @@ static bool correspondence(const Loop *l, const Array *a, int corr[]) {
     return true;
 }
 
+int loopAxisOf(const Loop *l, const Array *a, int axis) {
+    if (l->map.root && l->map.root == a->align.root) {
+        for (int r = 0; r < l->map.rank; r++)
+            if (a->align.ax[r] == axis + 1) return l->map.ax[r] <= l->rank ? l->map.ax[r] : 0;
+        return 0;
+    }
+    // no common distribution root known: the mapped array's own axes
+    return axis < MAXR ? l->arrAxisToLoop[axis] : 0;
+}
+
 // position (0-based) of the n-th lowest set bit, -1 if there are fewer
 static int nthBit(unsigned long v, int n) {
     for (int i = 0; i < 64; i++)

@@ -421,6 +421,7 @@ static std::vector<uint64_t> signature(const std::vector<Loop *> &q) {
             } else {
                 size_t off = 0;
                 Var *v = varAt(l->cuda.params[i], &off);
+                sigAdd(s, (uint64_t)v);
                 sigAdd(s, v ? (uint64_t)(v->dev + off) : 0);
             }
         }
@@ -437,6 +438,8 @@ static std::vector<uint64_t> signature(const std::vector<Loop *> &q) {
             sigAdd(s, (uint64_t)r.vtype);
             sigAdd(s, (uint64_t)r.addr);
             sigAdd(s, (uint64_t)r.locAddr);
+            sigAdd(s, (uint64_t)r.var);
+            sigAdd(s, (uint64_t)r.locVar);
             sigAdd(s, (uint64_t)(r.var ? r.var->dev : nullptr));
             sigAdd(s, (uint64_t)(r.locVar ? r.locVar->dev : nullptr));
         }
@@ -517,10 +520,10 @@ void queueFlush() {
     if (settings.syncEachLoop) streamSync();
 }
 
-// An array is freed: no cached graph may name it any more (a later array could
-// reuse its descriptor and buffers, and the graph's records would then name a
-// dead object).
-void graphsForget(const Array *a) {
+// An array or a variable is dropped: no cached graph may name it any more (a
+// later object could reuse its descriptor and buffers, and the graph's records
+// would then name a dead object).
+void graphsForget(const Obj *a) {
     for (auto it = graphCache.begin(); it != graphCache.end();) {
         bool names = std::find(it->sig.begin(), it->sig.end(), (uint64_t)a) != it->sig.end();
         for (const Array *x : it->swaps) names = names || x == a;
@@ -760,16 +763,19 @@ void dvmh_loop_perform_C(DvmType curLoop) {
              "parallel loop outside a region: this runtime executes parallel loops on the GPU only, inside regions");
     GB_CHECK(l->hasCuda, "loop at %s:%ld has no CUDA handler: this runtime executes parallel loops on the GPU only",
              l->file.c_str(), l->line);
-    // dependency mask from ACROSS widths (loop.cpp:1117-1150)
+    // dependency mask from ACROSS widths (loop.cpp:1117-1150): the loop axis each
+    // dependent array axis follows; an axis with one iteration keeps its
+    // dependence unless DVMH_REDUCE_DEPS asks to drop it, as in the reference
     int firstDep = -1;
     for (auto &ac : l->across)
         for (int j = 0; j < ac.arr->rank; j++)
             if (ac.lo[j] > 0 || ac.hi[j] > 0) {
-                int la = (j < MAXR) ? l->arrAxisToLoop[j] : 0;
+                int la = loopAxisOf(l, ac.arr, j);
                 GB_CHECK(la > 0, "ACROSS array %s has a dependence on axis %d that is not tied to the loop",
                          ac.arr->name.c_str(), j + 1);
                 if (firstDep == -1 || la < firstDep) firstDep = la;
-                if (!l->empty && l->lo[la - 1] != l->hi[la - 1]) l->depMask |= 1L << (l->rank - la);
+                if (!settings.reduceDeps || (!l->empty && l->lo[la - 1] != l->hi[la - 1]))
+                    l->depMask |= 1L << (l->rank - la);
             }
     if (firstDep > 0 && l->depMask == 0) l->depMask |= 1L << (l->rank - firstDep);
     if (l->empty) {
@@ -1036,6 +1042,11 @@ void dvmhgb_set_autotransform(int on) {
 }
 
 int dvmhgb_get_autotransform(void) { return settings.autoTfm ? 1 : 0; }
+
+void dvmhgb_set_reduce_dependences(int on) {
+    queueFlush();
+    settings.reduceDeps = on != 0;
+}
 
 void dvmhgb_flush(void) { queueFlush(); }
 

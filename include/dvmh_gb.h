@@ -84,6 +84,10 @@ int dvmhgb_get_autotransform(void);
  * natural, 1 transformed, -1 not yet measured both ways; best[0..1] (may be
  * null) = fastest seconds seen natural / transformed (-1 = none). */
 int dvmhgb_tuner_layout(DvmHandlerFunc handler, double best[2]);
+/* ACROSS dependences of loop axes with a single iteration: kept by default
+ * (the reference's DVMH_REDUCE_DEPS=0); on (environment DVMH_REDUCE_DEPS=1),
+ * such an axis gets no dependence bit unless no other axis has one. */
+void dvmhgb_set_reduce_dependences(int on);
 /* Online tuning of CUDA blocks, variants and layouts: 0 off, 1 exhaustive,
  * 2 model-guided (the same as DVMH_OPT_PARAMS at start-up). */
 void dvmhgb_set_tuning(int mode);

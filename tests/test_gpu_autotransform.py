@@ -182,20 +182,32 @@ def test_two_dependences_with_an_outer_axis(g, mode, tfm):
 
 @pytest.mark.parametrize("mode", ["plain", "batched"])
 @pytest.mark.parametrize("tfm", [1, 0])
+@pytest.mark.parametrize("reduce", [0, 1])
 @pytest.mark.parametrize("shape,moved", [((3, 30), True), ((30, 3), False), ((3, 3), False)])
-def test_dispatcher_single_iteration_axes(g, mode, tfm, shape, moved):
-    # a dependent axis with one iteration carries no dependence: the generated handler's
-    # dispatcher counts one and takes the one-dependence case; with the rows' axis the only
-    # independent one (3 x n), the reference's rule stores it innermost (a transposed layout)
+def test_dispatcher_single_iteration_axes(g, mode, tfm, reduce, shape, moved):
+    # a dependent axis with one iteration keeps its dependence (the reference's default) and
+    # the generated handler's dispatcher takes the two-dependence case; with dependences
+    # reduced it has none, the dispatcher counts one and takes the one-dependence case, and
+    # with the rows' axis the only independent one (3 x n) the reference's rule stores it
+    # innermost (a transposed layout).  The results are the sequential loop's either way.
+    rt = g.runtime()
     g.set_mode(mode)
-    g.runtime().dvmhgb_set_autotransform(tfm)
-    n0, n1 = shape
-    m, a, b, s = run(g, n0, n1, 3, 6, dirs=(1, -1), read_each=1, mirror=1)
-    check(m, a, b, n0, n1, 3, 6, (1, -1), 1, 1)
-    if tfm and moved:
-        assert s["relayouts"] >= 2, s
-    elif not tfm:
-        assert s["relayouts"] == 0, s
+    rt.dvmhgb_set_autotransform(tfm)
+    rt.dvmhgb_set_reduce_dependences(reduce)
+    try:
+        n0, n1 = shape
+        m, a, b, s = run(g, n0, n1, 3, 6, dirs=(1, -1), read_each=1, mirror=1)
+        check(m, a, b, n0, n1, 3, 6, (1, -1), 1, 1)
+        if not tfm:
+            assert s["relayouts"] == 0, s
+        elif not reduce or moved:
+            # two dependences: the array's plane is diagonalised; one: the rows' axis goes innermost
+            assert s["relayouts"] >= 2, s
+        else:
+            # one dependence, and the array's innermost axis already follows the independent loop axis
+            assert s["relayouts"] == 0, s
+    finally:
+        rt.dvmhgb_set_reduce_dependences(0)
 
 
 def test_freed_arrays_leave_no_cached_graphs(g):

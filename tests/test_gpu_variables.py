@@ -1,0 +1,54 @@
+"""Scalars registered in regions live in the runtime's variable registry by
+host address.  A program may free such memory and later register a new
+variable that overlaps an old one (another program's reduction buffer, a
+temporary): the old registration is forgotten -- with its device copy and any
+cached graph that named it -- instead of being reported as a conflict."""
+import ctypes
+
+import numpy as np
+import pytest
+
+import __graft_entry__ as ge
+
+pytestmark = pytest.mark.gpu
+
+INTENT_INOUT, DEVICE_TYPE_CUDA = 3, 2
+
+
+@pytest.fixture(scope="module")
+def rt():
+    ge.build()
+    _, g = ge.package()
+    g.init()
+    rt = g.runtime()
+    rt.dvmh_region_create_C.restype = ctypes.c_long
+    rt.dvmh_region_create_C.argtypes = [ctypes.c_long]
+    rt.dvmh_region_register_scalar_C.argtypes = [ctypes.c_long, ctypes.c_long, ctypes.c_void_p, ctypes.c_long,
+                                                 ctypes.c_char_p]
+    rt.dvmh_region_execute_on_targets_C.argtypes = [ctypes.c_long, ctypes.c_long]
+    rt.dvmh_region_end_C.argtypes = [ctypes.c_long]
+    rt.dvmh_actual_variable2_.argtypes = [ctypes.c_void_p]
+    rt.dvmh_get_actual_variable2_.argtypes = [ctypes.c_void_p]
+    return rt
+
+
+def region_with(rt, addr, size, name):
+    r = rt.dvmh_region_create_C(0)
+    rt.dvmh_region_register_scalar_C(r, INTENT_INOUT, addr, size, name)
+    rt.dvmh_region_execute_on_targets_C(r, DEVICE_TYPE_CUDA)
+    rt.dvmh_region_end_C(r)
+
+
+def test_overlapping_variables_from_earlier_regions(rt):
+    buf = np.arange(16, dtype=np.float64)
+    p = buf.ctypes.data
+    region_with(rt, p, 32, b"old")            # doubles 0..3
+    region_with(rt, p + 16, 32, b"shifted")   # doubles 2..5: overlaps the old one
+    region_with(rt, p + 8, 64, b"wider")      # doubles 1..8: overlaps the shifted one
+    region_with(rt, p, 128, b"whole")         # all of them
+    # the surviving registration round-trips the host values through the device
+    rt.dvmh_actual_variable2_(ctypes.c_void_p(p))
+    region_with(rt, p, 128, b"whole")
+    before = buf.copy()
+    rt.dvmh_get_actual_variable2_(ctypes.c_void_p(p))
+    assert np.array_equal(buf, before)
