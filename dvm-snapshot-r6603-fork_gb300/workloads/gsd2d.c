@@ -20,7 +20,10 @@
  *     region { parallel([i][j] on B[i][j]): B[i][j] = A[i][j] * 2 }   (all of B)
  * The mirror loop's handler does not ask for transforms: the runtime gives it
  * A in the natural layout, between two sweeps that work on the transformed one.
+ * The host handlers below are the sequential form (one slot); the reference
+ * runtime runs them in loop order, which is the order the results are pinned to.
  */
+#include <math.h>
 #include <string.h>
 
 #include "dvmhlib2.h"
@@ -28,8 +31,41 @@
 
 static DvmType A[64], B[64];
 
+#ifndef WL_NO_CUDA
 void loop_gsd2d_cuda(DvmType *pLoopRef, DvmType A_hdr[], double *m_ptr);
 void loop_gsd2d_mirror_cuda(DvmType *pLoopRef, DvmType B_hdr[], DvmType A_hdr[]);
+#endif
+
+void loop_gsd2d_host(DvmType *pLoopRef, DvmType A_hdr[], double *m_ptr) {
+    DvmType loop_ref = *pLoopRef;
+    DvmType device_num = dvmh_loop_get_device_num_C(loop_ref);
+    double (*a)[A_hdr[1]] = (double (*)[A_hdr[1]])dvmh_get_natural_base_C(device_num, A_hdr);
+    DvmType boundsLow[2], boundsHigh[2], loopSteps[2];
+    DvmType i, j;
+    double m;
+    (void)m_ptr;
+    dvmh_loop_fill_bounds_C(loop_ref, boundsLow, boundsHigh, loopSteps);
+    dvmh_loop_red_init_C(loop_ref, 1, &m, 0);
+    for (i = boundsLow[0]; loopSteps[0] > 0 ? i <= boundsHigh[0] : i >= boundsHigh[0]; i += loopSteps[0])
+        for (j = boundsLow[1]; loopSteps[1] > 0 ? j <= boundsHigh[1] : j >= boundsHigh[1]; j += loopSteps[1]) {
+            double old = a[i][j];
+            a[i][j] = (a[i - 1][j] + a[i + 1][j] + a[i][j - 1] + a[i][j + 1]) * 0.25;
+            m = fabs(a[i][j] - old) > m ? fabs(a[i][j] - old) : m;
+        }
+    dvmh_loop_red_post_C(loop_ref, 1, &m, 0);
+}
+
+void loop_gsd2d_mirror_host(DvmType *pLoopRef, DvmType B_hdr[], DvmType A_hdr[]) {
+    DvmType loop_ref = *pLoopRef;
+    DvmType device_num = dvmh_loop_get_device_num_C(loop_ref);
+    double (*b)[B_hdr[1]] = (double (*)[B_hdr[1]])dvmh_get_natural_base_C(device_num, B_hdr);
+    double (*a)[A_hdr[1]] = (double (*)[A_hdr[1]])dvmh_get_natural_base_C(device_num, A_hdr);
+    DvmType boundsLow[2], boundsHigh[2], loopSteps[2];
+    DvmType i, j;
+    dvmh_loop_fill_bounds_C(loop_ref, boundsLow, boundsHigh, loopSteps);
+    for (i = boundsLow[0]; i <= boundsHigh[0]; i++)
+        for (j = boundsLow[1]; j <= boundsHigh[1]; j++) b[i][j] = a[i][j] * 2.0;
+}
 
 static double m;
 static long N0, N1;
@@ -65,26 +101,34 @@ int wl_gsd2d_sweeps(long sweeps, int dir0, int dir1, int readEach, int mirror, d
         cur_region = dvmh_region_create_C(0);
         dvmh_region_register_array_C(cur_region, INTENT_INOUT, A, "A");
         dvmh_region_register_scalar_C(cur_region, INTENT_INOUT, &m, sizeof(m), "m");
-        dvmh_region_execute_on_targets_C(cur_region, DEVICE_TYPE_CUDA);
+        dvmh_region_execute_on_targets_C(cur_region, DEVICE_TYPE_HOST | DEVICE_TYPE_CUDA);
         cur_loop = dvmh_loop_create_C(cur_region, 2, (DvmType)(dir0 > 0 ? 1 : n0 - 2), (DvmType)(dir0 > 0 ? n0 - 2 : 1),
                                       (DvmType)dir0, (DvmType)(dir1 > 0 ? 1 : n1 - 2),
                                       (DvmType)(dir1 > 0 ? n1 - 2 : 1), (DvmType)dir1);
         dvmh_loop_map_C(cur_loop, A, 2, dvmh_alignment_linear_C(1, 1, 0), dvmh_alignment_linear_C(2, 1, 0));
         dvmh_loop_across_C(cur_loop, 0, A, 2, 1L, 1L, 1L, 1L);
         dvmh_loop_reduction_C(cur_loop, rf_MAX, &m, rt_DOUBLE, 1, 0, 0);
+        dvmh_loop_register_handler_C(cur_loop, DEVICE_TYPE_HOST, 0,
+                                     dvmh_handler_func_C((DvmHandlerFunc)loop_gsd2d_host, 2, A, &m));
+#ifndef WL_NO_CUDA
         dvmh_loop_register_handler_C(cur_loop, DEVICE_TYPE_CUDA, 0,
                                      dvmh_handler_func_C((DvmHandlerFunc)loop_gsd2d_cuda, 2, A, &m));
+#endif
         dvmh_loop_perform_C(cur_loop);
         dvmh_region_end_C(cur_region);
         if (mirror) {
             cur_region = dvmh_region_create_C(0);
             dvmh_region_register_array_C(cur_region, INTENT_IN, A, "A");
             dvmh_region_register_array_C(cur_region, INTENT_OUT, B, "B");
-            dvmh_region_execute_on_targets_C(cur_region, DEVICE_TYPE_CUDA);
+            dvmh_region_execute_on_targets_C(cur_region, DEVICE_TYPE_HOST | DEVICE_TYPE_CUDA);
             cur_loop = dvmh_loop_create_C(cur_region, 2, 0L, (DvmType)(n0 - 1), 1L, 0L, (DvmType)(n1 - 1), 1L);
             dvmh_loop_map_C(cur_loop, B, 2, dvmh_alignment_linear_C(1, 1, 0), dvmh_alignment_linear_C(2, 1, 0));
+            dvmh_loop_register_handler_C(cur_loop, DEVICE_TYPE_HOST, 0,
+                                         dvmh_handler_func_C((DvmHandlerFunc)loop_gsd2d_mirror_host, 2, B, A));
+#ifndef WL_NO_CUDA
             dvmh_loop_register_handler_C(cur_loop, DEVICE_TYPE_CUDA, 0,
                                          dvmh_handler_func_C((DvmHandlerFunc)loop_gsd2d_mirror_cuda, 2, B, A));
+#endif
             dvmh_loop_perform_C(cur_loop);
             dvmh_region_end_C(cur_region);
         }

@@ -10,6 +10,9 @@
  *   heat         count lo hi steps coef seed
  *                -> sides[count] (int64), then per step: sums[count], mins[count],
  *                   locs[count][2] (int32), then the final arrays in order
+ *   gsd2d        n0 n1 sweeps seed dir0 dir1 mirror
+ *                -> m[sweeps] (read after every sweep), A[n0*n1], then B[n0*n1]
+ *                   when mirror
  * Run with DVMH_NUM_THREADS=1 for the sequential (order-exact) oracle.
  */
 #include <stdio.h>
@@ -31,6 +34,8 @@ int wl_sor3d_fetch(double *a_out);
 int wl_heat_setup(const wl_heat_params *p, long *sides_out);
 int wl_heat_run(long steps, double *sums_out, double *mins_out, int *locs_out);
 int wl_heat_fetch(long k, double *u_out);
+int wl_gsd2d_run(long n0, long n1, long sweeps, uint64_t seed, int dir0, int dir1, int readEach, int mirror,
+                 double *m_out, double *a_out, double *b_out);
 
 static void put(FILE *f, const void *p, size_t bytes) {
     if (fwrite(p, 1, bytes, f) != bytes) {
@@ -116,6 +121,17 @@ int main(int argc, char **argv) {
             put(f, u, sizeof(double) * sides[k] * sides[k]);
             free(u);
         }
+    } else if (!strcmp(argv[1], "gsd2d")) {
+        long n0 = atol(argv[3]), n1 = atol(argv[4]), sweeps = atol(argv[5]);
+        uint64_t seed = strtoull(argv[6], 0, 10);
+        int dir0 = atoi(argv[7]), dir1 = atoi(argv[8]), mirror = atoi(argv[9]);
+        double *m = malloc(sizeof(double) * sweeps), *a = malloc(sizeof(double) * n0 * n1),
+               *b = malloc(sizeof(double) * n0 * n1);
+        wl_gsd2d_run(n0, n1, sweeps, seed, dir0, dir1, 1, mirror, m, a, b);
+        put(f, m, sizeof(double) * sweeps);
+        put(f, a, sizeof(double) * n0 * n1);
+        if (mirror)
+            put(f, b, sizeof(double) * n0 * n1);
     } else {
         fprintf(stderr, "unknown program %s\n", argv[1]);
         return 2;

@@ -38,6 +38,14 @@ CASES = [
     ("sor3d_n70_sw2", "sor3d", [70, 2, 1.5, 20261205], False),
     ("heat_c5_s3", "heat", [5, 5, 40, 3, 0.2, 13], True),
     ("heat_c24_s6", "heat", [24, 3, 150, 6, 0.2, 20261206], False),
+    ("gsd2d_9x7_fwd_mirror", "gsd2d", [9, 7, 3, 31, 1, 1, 1], True),
+    ("gsd2d_6x11_slash", "gsd2d", [6, 11, 2, 32, 1, -1, 0], True),
+    # The reference crashes (SIGSEGV in libdvm's across_) when an axis with a
+    # single iteration runs backward, so the single-row case runs it forward.
+    ("gsd2d_3x30_rowback", "gsd2d", [3, 30, 2, 33, 1, -1, 0], True),
+    ("gsd2d_4x30_back", "gsd2d", [4, 30, 2, 34, -1, -1, 1], True),
+    ("gsd2d_96x200_mixed", "gsd2d", [96, 200, 4, 20261207, -1, 1, 1], False),
+    ("gsd2d_257x129_fwd", "gsd2d", [257, 129, 3, 20261208, 1, 1, 0], False),
 ]
 
 
@@ -82,6 +90,19 @@ def case(name, prog, params, full):
         rec["A_sha256"] = sha(A)
         if full:
             rec["A"] = hx(A)
+    elif prog == "gsd2d":
+        n0, n1, sw, mirror = params[0], params[1], params[2], params[6]
+        d = np.frombuffer(raw, dtype="<f8")
+        rec["m"] = hx(d[:sw])
+        A = d[sw:sw + n0 * n1]
+        rec["A_sha256"] = sha(A)
+        if full:
+            rec["A"] = hx(A)
+        if mirror:
+            B = d[sw + n0 * n1:sw + 2 * n0 * n1]
+            rec["B_sha256"] = sha(B)
+            if full:
+                rec["B"] = hx(B)
     else:
         cnt, steps = params[0], params[3]
         off = 0

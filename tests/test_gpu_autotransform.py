@@ -7,6 +7,7 @@ when the loop runs its two axes in opposite directions); a mirror loop whose
 handler does not ask for transforms reads the array in the natural layout in
 between.  Everything is checked bit for bit against the sequential loop."""
 import ctypes
+import hashlib
 
 import numpy as np
 import pytest
@@ -51,6 +52,28 @@ def check(m, a, b, n0, n1, sweeps, seed, dirs, read_each, mirror):
         assert m[0] == m_ref[-1]
     if mirror:
         assert np.array_equal(b, a_ref * 2.0)
+
+
+def sha(x):
+    return hashlib.sha256(np.ascontiguousarray(x, dtype="<f8").tobytes()).hexdigest()
+
+
+@pytest.mark.parametrize("mode", ["plain", "batched"])
+@pytest.mark.parametrize("tfm", [1, 0])
+def test_golden(g, golden, mode, tfm):
+    """The reference runtime's own outputs (its host handlers, sequential
+    order) for the program, with and without transformed layouts."""
+    g.set_mode(mode)
+    g.runtime().dvmhgb_set_autotransform(tfm)
+    cases = [(k, c) for k, c in golden.items() if c["prog"] == "gsd2d"]
+    assert cases
+    for name, c in cases:
+        n0, n1, sw, seed, d0, d1, mirror = c["params"]
+        m, a, b, _ = run(g, n0, n1, sw, seed, dirs=(d0, d1), read_each=1, mirror=mirror)
+        assert [float(x).hex() for x in m] == c["m"], name
+        assert sha(a) == c["A_sha256"], name
+        if mirror:
+            assert sha(b) == c["B_sha256"], name
 
 
 @pytest.mark.parametrize("mode", ["plain", "async", "batched"])

@@ -24,7 +24,7 @@ def jac_cases(golden):
 
 def test_golden_present(golden):
     progs = {v["prog"] for v in golden.values()}
-    assert progs == {"jac2d", "jac3d", "sor3d", "heat"}
+    assert progs == {"jac2d", "jac3d", "sor3d", "heat", "gsd2d"}
 
 
 @pytest.mark.parametrize("rank", [2, 3])
@@ -83,6 +83,22 @@ def test_heat_vs_reference(golden):
                 assert np.array_equal(f, unhex(c["final"][k])), name
             else:
                 assert sha(f) == c["final_sha256"][k], name
+
+
+def test_gsd2d_vs_reference(golden):
+    """The two-dependence ACROSS loop in every direction, and the mirror loop
+    B = 2 A run between sweeps."""
+    for name, c in golden.items():
+        if c["prog"] != "gsd2d":
+            continue
+        n0, n1, sw, seed, d0, d1, mirror = c["params"]
+        m, A = orc.gsd2d_run(n0, n1, sw, seed, d0, d1)
+        assert np.array_equal(m, unhex(c["m"])), name
+        assert sha(A) == c["A_sha256"], name
+        if "A" in c:
+            assert np.array_equal(A, unhex(c["A"])), name
+        if mirror:
+            assert sha(A * 2.0) == c["B_sha256"], name
 
 
 def test_pairwise_tree_identity():
