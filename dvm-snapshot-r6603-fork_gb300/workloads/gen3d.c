@@ -22,8 +22,42 @@
 static DvmType A[64], B[64];
 static long n12v, n2v;  /* plane and row sizes, used by the loop body for lc */
 
+#ifndef WL_NO_CUDA
 void loop_gen3d_cuda(DvmType *pLoopRef, DvmType A_hdr[], DvmType B_hdr[], long *n12_ptr, long *n2_ptr, double *s_ptr,
                      double *mx_ptr, long *lc_ptr);
+#endif
+
+/* the sequential host form, loop order */
+void loop_gen3d_host(DvmType *pLoopRef, DvmType A_hdr[], DvmType B_hdr[], long *n12_ptr, long *n2_ptr, double *s_ptr,
+                     double *mx_ptr, long *lc_ptr) {
+    DvmType loop_ref = *pLoopRef;
+    DvmType device_num = dvmh_loop_get_device_num_C(loop_ref);
+    double (*a)[A_hdr[1] / A_hdr[2]][A_hdr[2]] =
+        (double (*)[A_hdr[1] / A_hdr[2]][A_hdr[2]])dvmh_get_natural_base_C(device_num, A_hdr);
+    double (*b)[B_hdr[1] / B_hdr[2]][B_hdr[2]] =
+        (double (*)[B_hdr[1] / B_hdr[2]][B_hdr[2]])dvmh_get_natural_base_C(device_num, B_hdr);
+    long n12 = *n12_ptr, n2 = *n2_ptr;
+    DvmType boundsLow[3], boundsHigh[3], loopSteps[3];
+    DvmType i, j, k;
+    double s, mx;
+    long lc;
+    (void)s_ptr, (void)mx_ptr, (void)lc_ptr;
+    dvmh_loop_fill_bounds_C(loop_ref, boundsLow, boundsHigh, loopSteps);
+    dvmh_loop_red_init_C(loop_ref, 1, &s, 0);
+    dvmh_loop_red_init_C(loop_ref, 2, &mx, &lc);
+    for (i = boundsLow[0]; i <= boundsHigh[0]; i++)
+        for (j = boundsLow[1]; j <= boundsHigh[1]; j++)
+            for (k = boundsLow[2]; k <= boundsHigh[2]; k++) {
+                b[i][j][k] = a[i - 1][j][k] + 0.5 * a[i][j][k + 1];
+                s = s + b[i][j][k];
+                if (b[i][j][k] > mx) {
+                    mx = b[i][j][k];
+                    lc = i * n12 + j * n2 + k;
+                }
+            }
+    dvmh_loop_red_post_C(loop_ref, 1, &s, 0);
+    dvmh_loop_red_post_C(loop_ref, 2, &mx, &lc);
+}
 
 /* One run of the program on an n0 x n1 x n2 grid.  A CUDA block (bx, by, bz) > 0
  * is set on the loop as the program's cuda_block clause would; 0 keeps the
@@ -66,7 +100,7 @@ int wl_gen3d_run(long n0, long n1, long n2, uint64_t seed, int bx, int by, int b
     dvmh_region_register_scalar_C(cur_region, INTENT_INOUT, s, sizeof(*s), "s");
     dvmh_region_register_scalar_C(cur_region, INTENT_INOUT, mx, sizeof(*mx), "mx");
     dvmh_region_register_scalar_C(cur_region, INTENT_INOUT, lc, sizeof(*lc), "lc");
-    dvmh_region_execute_on_targets_C(cur_region, DEVICE_TYPE_CUDA);
+    dvmh_region_execute_on_targets_C(cur_region, DEVICE_TYPE_HOST | DEVICE_TYPE_CUDA);
     dvmh_shadow_renew_C(A, 0, 0);
     cur_loop = dvmh_loop_create_C(cur_region, 3, 1L, (DvmType)(n0 - 2), 1L, 1L, (DvmType)(n1 - 2), 1L, 1L,
                                   (DvmType)(n2 - 2), 1L);
@@ -75,8 +109,12 @@ int wl_gen3d_run(long n0, long n1, long n2, uint64_t seed, int bx, int by, int b
     if (bx > 0) dvmh_loop_set_cuda_block_C(cur_loop, bx, by, bz);
     dvmh_loop_reduction_C(cur_loop, rf_SUM, s, rt_DOUBLE, 1, 0, 0);
     dvmh_loop_reduction_C(cur_loop, rf_MAXLOC, mx, rt_DOUBLE, 1, lc, sizeof(*lc));
+    dvmh_loop_register_handler_C(cur_loop, DEVICE_TYPE_HOST, 0,
+                                 dvmh_handler_func_C((DvmHandlerFunc)loop_gen3d_host, 7, A, B, &n12v, &n2v, s, mx, lc));
+#ifndef WL_NO_CUDA
     dvmh_loop_register_handler_C(cur_loop, DEVICE_TYPE_CUDA, 0,
                                  dvmh_handler_func_C((DvmHandlerFunc)loop_gen3d_cuda, 7, A, B, &n12v, &n2v, s, mx, lc));
+#endif
     dvmh_loop_perform_C(cur_loop);
     dvmh_region_end_C(cur_region);
     dvmh_get_actual_variable2_(s);

@@ -22,9 +22,59 @@
 
 static DvmType X[64], V[64];
 
+#ifndef WL_NO_CUDA
 void loop_genred_cuda(DvmType *pLoopRef, DvmType X_hdr[], DvmType V_hdr[], double *ds_ptr, double *dp_ptr,
                       int *imn_ptr, float *fmx_ptr, int *ia_ptr, int *io_ptr, int *ix_ptr, double *dml_ptr,
                       long *lc_ptr);
+#endif
+
+/* the sequential host form (cdvmh's host handler: reduction variables
+ * initialised by the runtime, the loop in its own order, results posted) */
+void loop_genred_host(DvmType *pLoopRef, DvmType X_hdr[], DvmType V_hdr[], double *ds_ptr, double *dp_ptr,
+                      int *imn_ptr, float *fmx_ptr, int *ia_ptr, int *io_ptr, int *ix_ptr, double *dml_ptr,
+                      long *lc_ptr) {
+    DvmType loop_ref = *pLoopRef;
+    DvmType device_num = dvmh_loop_get_device_num_C(loop_ref);
+    double *x = (double *)dvmh_get_natural_base_C(device_num, X_hdr);
+    int *v = (int *)dvmh_get_natural_base_C(device_num, V_hdr);
+    DvmType lo, hi, st, i;
+    double ds, dp, dml;
+    int imn, ia, io, ix;
+    float fmx;
+    long lc;
+    (void)ds_ptr, (void)dp_ptr, (void)imn_ptr, (void)fmx_ptr, (void)ia_ptr, (void)io_ptr, (void)ix_ptr;
+    (void)dml_ptr, (void)lc_ptr;
+    dvmh_loop_fill_bounds_C(loop_ref, &lo, &hi, &st);
+    dvmh_loop_red_init_C(loop_ref, 1, &ds, 0);
+    dvmh_loop_red_init_C(loop_ref, 2, &dp, 0);
+    dvmh_loop_red_init_C(loop_ref, 3, &imn, 0);
+    dvmh_loop_red_init_C(loop_ref, 4, &fmx, 0);
+    dvmh_loop_red_init_C(loop_ref, 5, &ia, 0);
+    dvmh_loop_red_init_C(loop_ref, 6, &io, 0);
+    dvmh_loop_red_init_C(loop_ref, 7, &ix, 0);
+    dvmh_loop_red_init_C(loop_ref, 8, &dml, &lc);
+    for (i = lo; st > 0 ? i <= hi : i >= hi; i += st) {
+        ds = ds + x[i];
+        dp = dp * (1.0 + x[i] / 65536.0);
+        imn = v[i] < imn ? v[i] : imn;
+        fmx = (float)x[i] > fmx ? (float)x[i] : fmx;
+        ia &= v[i] | 0x0F0F0F0F;
+        io |= v[i] & 0x00FF00FF;
+        ix ^= v[i];
+        if (x[i] < dml) {
+            dml = x[i];
+            lc = i;
+        }
+    }
+    dvmh_loop_red_post_C(loop_ref, 1, &ds, 0);
+    dvmh_loop_red_post_C(loop_ref, 2, &dp, 0);
+    dvmh_loop_red_post_C(loop_ref, 3, &imn, 0);
+    dvmh_loop_red_post_C(loop_ref, 4, &fmx, 0);
+    dvmh_loop_red_post_C(loop_ref, 5, &ia, 0);
+    dvmh_loop_red_post_C(loop_ref, 6, &io, 0);
+    dvmh_loop_red_post_C(loop_ref, 7, &ix, 0);
+    dvmh_loop_red_post_C(loop_ref, 8, &dml, &lc);
+}
 
 /* red: the eight reduction variables' initial values in, results out:
  * ds, dp, dml (double[3]), imn, ia, io, ix (int[4]), fmx (float[1]), lc (long[1]). */
@@ -76,7 +126,7 @@ int wl_genred_run(long n, long start, long end, long step, uint64_t seed, int bx
     dvmh_region_register_scalar_C(cur_region, INTENT_INOUT, &ix, sizeof(ix), "ix");
     dvmh_region_register_scalar_C(cur_region, INTENT_INOUT, &dml, sizeof(dml), "dml");
     dvmh_region_register_scalar_C(cur_region, INTENT_INOUT, &lcv, sizeof(lcv), "lc");
-    dvmh_region_execute_on_targets_C(cur_region, DEVICE_TYPE_CUDA);
+    dvmh_region_execute_on_targets_C(cur_region, DEVICE_TYPE_HOST | DEVICE_TYPE_CUDA);
     cur_loop = dvmh_loop_create_C(cur_region, 1, (DvmType)start, (DvmType)end, (DvmType)step);
     dvmh_loop_map_C(cur_loop, X, 1, dvmh_alignment_linear_C(1, 1, 0));
     if (bx > 0) dvmh_loop_set_cuda_block_C(cur_loop, bx, 1, 1);
@@ -88,9 +138,14 @@ int wl_genred_run(long n, long start, long end, long step, uint64_t seed, int bx
     dvmh_loop_reduction_C(cur_loop, rf_OR, &io, rt_INT, 1, 0, 0);
     dvmh_loop_reduction_C(cur_loop, rf_XOR, &ix, rt_INT, 1, 0, 0);
     dvmh_loop_reduction_C(cur_loop, rf_MINLOC, &dml, rt_DOUBLE, 1, &lcv, sizeof(lcv));
+    dvmh_loop_register_handler_C(cur_loop, DEVICE_TYPE_HOST, 0,
+                                 dvmh_handler_func_C((DvmHandlerFunc)loop_genred_host, 11, X, V, &ds, &dp, &imn, &fmx,
+                                                     &ia, &io, &ix, &dml, &lcv));
+#ifndef WL_NO_CUDA
     dvmh_loop_register_handler_C(cur_loop, DEVICE_TYPE_CUDA, 0,
                                  dvmh_handler_func_C((DvmHandlerFunc)loop_genred_cuda, 11, X, V, &ds, &dp, &imn, &fmx,
                                                      &ia, &io, &ix, &dml, &lcv));
+#endif
     dvmh_loop_perform_C(cur_loop);
     dvmh_region_end_C(cur_region);
     dvmh_get_actual_variable2_(&ds);

@@ -41,6 +41,15 @@ def lib():
         L.orc_gsd2d_sweep.argtypes = [ctypes.c_long, ctypes.c_long, ctypes.c_int, ctypes.c_int, _dp]
         L.orc_diag_index.restype = ctypes.c_long
         L.orc_diag_index.argtypes = [ctypes.c_long, ctypes.c_long, ctypes.c_long, ctypes.c_long, ctypes.c_int]
+        L.orc_genred.argtypes = [ctypes.c_long] * 4 + [ctypes.c_uint64, _dp, ctypes.POINTER(ctypes.c_int),
+                                                        ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_long)]
+        L.orc_gs2d_init.argtypes = [ctypes.c_long, ctypes.c_uint64, _dp]
+        L.orc_gs2d_sweep.restype = ctypes.c_double
+        L.orc_gs2d_sweep.argtypes = [ctypes.c_long, _dp]
+        L.orc_rec2d_init.argtypes = [ctypes.c_long, ctypes.c_long, ctypes.c_uint64, _dp]
+        L.orc_rec2d_sweep.restype = ctypes.c_double
+        L.orc_rec2d_sweep.argtypes = [ctypes.c_long, ctypes.c_long, _dp]
+        L.orc_gen3d.argtypes = [ctypes.c_long] * 3 + [ctypes.c_uint64, _dp, _dp, ctypes.POINTER(ctypes.c_long), _dp]
         L.orc_max_threads.restype = ctypes.c_int
         _L = L
     return _L
@@ -107,3 +116,45 @@ def gsd2d_run(n0, n1, sweeps, seed, dir0=1, dir1=1):
     L.orc_gsd2d_init(n0, n1, seed, P(A))
     m = [L.orc_gsd2d_sweep(n0, n1, dir0, dir1, P(A)) for _ in range(sweeps)]
     return np.array(m), A
+
+
+def gs2d_run(n, sweeps, seed):
+    A = np.zeros(n * n)
+    L = lib()
+    L.orc_gs2d_init(n, seed, P(A))
+    s = [L.orc_gs2d_sweep(n, P(A)) for _ in range(sweeps)]
+    return np.array(s), A
+
+
+def rec2d_run(n0, n1, sweeps, seed):
+    A = np.zeros(n0 * n1)
+    L = lib()
+    L.orc_rec2d_init(n0, n1, seed, P(A))
+    lo = [L.orc_rec2d_sweep(n0, n1, P(A)) for _ in range(sweeps)]
+    return np.array(lo), A
+
+
+def gsd3d_run(n0, n1, n2, sweeps, seed):
+    """plane k is the 2-D program with seed + k; m = MAX over the planes per sweep"""
+    planes = [gsd2d_run(n1, n2, sweeps, seed + k) for k in range(n0)]
+    m = np.max(np.stack([p[0] for p in planes]), axis=0)
+    return m, np.concatenate([p[1] for p in planes])
+
+
+def gen3d_run(n0, n1, n2, seed, s, mx, lc):
+    """returns (s, mx, lc, B) of the sequential loop; B dense n0*n1*n2"""
+    B = np.zeros(n0 * n1 * n2)
+    sv, mv = ctypes.c_double(s), ctypes.c_double(mx)
+    lv = ctypes.c_long(lc)
+    lib().orc_gen3d(n0, n1, n2, seed, ctypes.byref(sv), ctypes.byref(mv), ctypes.byref(lv), P(B))
+    return sv.value, mv.value, lv.value, B
+
+
+def genred_run(n, start, end, step, seed, init):
+    """init = (ds, dp, dml, imn, ia, io, ix, fmx, lc); returns the results in the same order."""
+    d3 = np.array(init[0:3], dtype=np.float64)
+    i4 = (ctypes.c_int * 4)(*[int(x) for x in init[3:7]])
+    f1 = (ctypes.c_float * 1)(init[7])
+    lc = (ctypes.c_long * 1)(int(init[8]))
+    lib().orc_genred(n, start, end, step, seed, P(d3), i4, f1, lc)
+    return (float(d3[0]), float(d3[1]), float(d3[2]), i4[0], i4[1], i4[2], i4[3], f1[0], lc[0])

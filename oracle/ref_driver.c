@@ -10,6 +10,12 @@
  *   heat         count lo hi steps coef seed
  *                -> sides[count] (int64), then per step: sums[count], mins[count],
  *                   locs[count][2] (int32), then the final arrays in order
+ *   genred       n start end step seed ds dp dml imn ia io ix fmx lc   (initial values)
+ *                -> ds dp dml (f64), imn ia io ix (int32), fmx (f32), lc (int64)
+ *   gen3d        n0 n1 n2 seed s mx lc  -> s, mx (f64), lc (int64), B[n0*n1*n2]
+ *   rec2d        n0 n1 sweeps seed      -> lo[sweeps], A[n0*n1]
+ *   gsd3d        n0 n1 n2 sweeps seed   -> m[sweeps], A[n0*n1*n2]
+ *   gs2d         n sweeps seed          -> s[sweeps], A[n*n]
  *   gsd2d        n0 n1 sweeps seed dir0 dir1 mirror
  *                -> m[sweeps] (read after every sweep), A[n0*n1], then B[n0*n1]
  *                   when mirror
@@ -34,6 +40,13 @@ int wl_sor3d_fetch(double *a_out);
 int wl_heat_setup(const wl_heat_params *p, long *sides_out);
 int wl_heat_run(long steps, double *sums_out, double *mins_out, int *locs_out);
 int wl_heat_fetch(long k, double *u_out);
+int wl_genred_run(long n, long start, long end, long step, uint64_t seed, int bx, double *d3, int *i4, float *f1,
+                  long *lc);
+int wl_gen3d_run(long n0, long n1, long n2, uint64_t seed, int bx, int by, int bz, double *s, double *mx, long *lc,
+                 double *b_out);
+int wl_rec2d_run(long n0, long n1, long sweeps, uint64_t seed, double *lo_out, double *a_out);
+int wl_gsd3d_run(long n0, long n1, long n2, long sweeps, uint64_t seed, double *m_out, double *a_out);
+int wl_gs2d_run(long n, long sweeps, uint64_t seed, double *s_out, double *a_out);
 int wl_gsd2d_run(long n0, long n1, long sweeps, uint64_t seed, int dir0, int dir1, int readEach, int mirror,
                  double *m_out, double *a_out, double *b_out);
 
@@ -121,6 +134,44 @@ int main(int argc, char **argv) {
             put(f, u, sizeof(double) * sides[k] * sides[k]);
             free(u);
         }
+    } else if (!strcmp(argv[1], "genred")) {
+        long n = atol(argv[3]), start = atol(argv[4]), end = atol(argv[5]), step = atol(argv[6]);
+        uint64_t seed = strtoull(argv[7], 0, 10);
+        double d3[3] = {atof(argv[8]), atof(argv[9]), atof(argv[10])};
+        int i4[4] = {atoi(argv[11]), (int)strtol(argv[12], 0, 0), (int)strtol(argv[13], 0, 0),
+                     (int)strtol(argv[14], 0, 0)};
+        float f1[1] = {(float)atof(argv[15])};
+        long lc[1] = {atol(argv[16])};
+        wl_genred_run(n, start, end, step, seed, 0, d3, i4, f1, lc);
+        put(f, d3, sizeof(d3));
+        put(f, i4, sizeof(i4));
+        put(f, f1, sizeof(f1));
+        put(f, lc, sizeof(lc));
+    } else if (!strcmp(argv[1], "gen3d")) {
+        long n0 = atol(argv[3]), n1 = atol(argv[4]), n2 = atol(argv[5]);
+        uint64_t seed = strtoull(argv[6], 0, 10);
+        double s = atof(argv[7]), mx = atof(argv[8]);
+        long lc = atol(argv[9]);
+        double *b = malloc(sizeof(double) * n0 * n1 * n2);
+        wl_gen3d_run(n0, n1, n2, seed, 0, 0, 0, &s, &mx, &lc, b);
+        put(f, &s, sizeof(s));
+        put(f, &mx, sizeof(mx));
+        put(f, &lc, sizeof(lc));
+        put(f, b, sizeof(double) * n0 * n1 * n2);
+    } else if (!strcmp(argv[1], "rec2d") || !strcmp(argv[1], "gs2d") || !strcmp(argv[1], "gsd3d")) {
+        int r3 = !strcmp(argv[1], "gsd3d"), sq = !strcmp(argv[1], "gs2d");
+        long n0 = atol(argv[3]), n1 = sq ? n0 : atol(argv[4]), n2 = r3 ? atol(argv[5]) : 1;
+        long sweeps = atol(argv[sq ? 4 : (r3 ? 6 : 5)]);
+        uint64_t seed = strtoull(argv[sq ? 5 : (r3 ? 7 : 6)], 0, 10);
+        double *r = malloc(sizeof(double) * sweeps), *a = malloc(sizeof(double) * n0 * n1 * n2);
+        if (r3)
+            wl_gsd3d_run(n0, n1, n2, sweeps, seed, r, a);
+        else if (sq)
+            wl_gs2d_run(n0, sweeps, seed, r, a);
+        else
+            wl_rec2d_run(n0, n1, sweeps, seed, r, a);
+        put(f, r, sizeof(double) * sweeps);
+        put(f, a, sizeof(double) * n0 * n1 * n2);
     } else if (!strcmp(argv[1], "gsd2d")) {
         long n0 = atol(argv[3]), n1 = atol(argv[4]), sweeps = atol(argv[5]);
         uint64_t seed = strtoull(argv[6], 0, 10);

@@ -313,6 +313,126 @@ double orc_gsd2d_sweep(long n0, long n1, int dir0, int dir1, double *A) {
     return Max(m, 0.0);
 }
 
+/*
+ * Gauss-Seidel over an n x n array, SUM of the new values
+ * (dvm-snapshot-r6603-fork_gb300/workloads/gs2d.c): the sequential loop over the
+ * interior; returns (0 + sum) + 0, the handler's sum combined with the
+ * global start and the initial value 0 (rts/dvmh/loop.cpp:37-113).
+ */
+void orc_gs2d_init(long n, uint64_t seed, double *A) {
+    for (long i = 0; i < n; i++)
+        for (long j = 0; j < n; j++)
+            A[i * n + j] = (i == 0 || j == 0 || i == n - 1 || j == n - 1) ? 0.0 : orc_u01(seed, 13, (uint64_t)(i * n + j));
+}
+
+double orc_gs2d_sweep(long n, double *A) {
+    double s = 0.0;
+    for (long i = 1; i < n - 1; i++)
+        for (long j = 1; j < n - 1; j++) {
+            A[i * n + j] = (((A[(i - 1) * n + j] + A[(i + 1) * n + j]) + A[i * n + j - 1]) + A[i * n + j + 1]) * 0.25;
+            s = s + A[i * n + j];
+        }
+    return (0.0 + s) + 0.0;
+}
+
+/*
+ * The recurrence A[i][j] = A[i][j] * 0.5 + A[i][j-1] * 0.25 along j over
+ * independent rows, MIN of the new values with the initial value 1.0
+ * (dvm-snapshot-r6603-fork_gb300/workloads/rec2d.c).
+ */
+void orc_rec2d_init(long n0, long n1, uint64_t seed, double *A) {
+    for (long i = 0; i < n0; i++)
+        for (long j = 0; j < n1; j++) A[i * n1 + j] = orc_u01(seed, 19, (uint64_t)(i * n1 + j));
+}
+
+double orc_rec2d_sweep(long n0, long n1, double *A) {
+    double lo = 1.0;  /* MIN: the handler starts at the initial value */
+    for (long i = 0; i < n0; i++)
+        for (long j = 1; j < n1; j++) {
+            A[i * n1 + j] = A[i * n1 + j] * 0.5 + A[i * n1 + j - 1] * 0.25;
+            lo = A[i * n1 + j] < lo ? A[i * n1 + j] : lo;
+        }
+    return lo < 1.0 ? lo : 1.0;
+}
+
+/*
+ * One pass of the 3-D loop B = A[i-1][j][k] + 0.5 * A[i][j][k+1] over the
+ * interior with SUM and MAXLOC (dvm-snapshot-r6603-fork_gb300/workloads/gen3d.c),
+ * in loop order; s, mx, lc: initial values in, results out, combined as the
+ * reference's engine does (rts/dvmh/loop.cpp:37-113: SUM from the identity,
+ * MAXLOC from the initial value, strict >).  B (dense) is 0 outside the loop.
+ */
+void orc_gen3d(long n0, long n1, long n2, uint64_t seed, double *s, double *mx, long *lc, double *B) {
+    double acc = 0.0, m = *mx;
+    long loc = *lc;
+    const long cells = n0 * n1 * n2;
+    double *A = (double *)malloc(sizeof(double) * (size_t)cells);
+    for (long q = 0; q < cells; q++) {
+        A[q] = orc_u01(seed, 7, (uint64_t)q);
+        B[q] = 0.0;
+    }
+    for (long i = 1; i < n0 - 1; i++)
+        for (long j = 1; j < n1 - 1; j++)
+            for (long k = 1; k < n2 - 1; k++) {
+                const long q = (i * n1 + j) * n2 + k;
+                const double v = A[q - n1 * n2] + 0.5 * A[q + 1];
+                B[q] = v;
+                acc = acc + v;
+                if (v > m) {
+                    m = v;
+                    loc = q;
+                }
+            }
+    free(A);
+    *s = (0.0 + acc) + *s;
+    *mx = m;
+    *lc = loc;
+}
+
+/*
+ * The eight reductions of a 1-D loop with a signed step
+ * (dvm-snapshot-r6603-fork_gb300/workloads/genred.c), in loop order, combined
+ * as the reference's engine combines them (rts/dvmh/loop.cpp:37-113): the
+ * handler's SUM, PROD and XOR start at the identity, MIN, MAX, AND, OR and
+ * MINLOC at the variable's initial value; the global value starts the same
+ * way, takes the handler's result, then the initial value once more.
+ * d3 = {ds, dp, dml}, i4 = {imn, ia, io, ix}, f1 = {fmx}, lc: initial values
+ * in, results out.
+ */
+void orc_genred(long n, long start, long end, long step, uint64_t seed, double *d3, int *i4, float *f1, long *lc) {
+    double ds = 0.0, dp = 1.0, dml = d3[2];
+    int imn = i4[0], ia = i4[1], io = i4[2], ix = 0;
+    float fmx = f1[0];
+    long loc = lc[0];
+    if (step != 0)
+        for (long i = start; step > 0 ? i <= end : i >= end; i += step) {
+            if (i < 0 || i >= n) break;
+            double x = orc_u01(seed, 11, (uint64_t)i);
+            int v = (int)(orc_u01(seed, 12, (uint64_t)i) * 2147483647.0) - 1073741824;
+            ds = ds + x;
+            dp = dp * (1.0 + x / 65536.0);
+            imn = v < imn ? v : imn;
+            fmx = (float)x > fmx ? (float)x : fmx;
+            ia &= v | 0x0F0F0F0F;
+            io |= v & 0x00FF00FF;
+            ix ^= v;
+            if (x < dml) {
+                dml = x;
+                loc = i;
+            }
+        }
+    /* global: identity (+) handler (+) initial, for the order-sensitive two */
+    d3[0] = (0.0 + ds) + d3[0];
+    d3[1] = (1.0 * dp) * d3[1];
+    d3[2] = dml;
+    i4[0] = imn;
+    i4[1] = ia;
+    i4[2] = io;
+    i4[3] = (0 ^ ix) ^ i4[3];
+    f1[0] = fmx;
+    lc[0] = loc;
+}
+
 /* position of (x, y) in the diagonal numbering of an Rx x Ry plane
  * (rts/dvmh/util.cpp:1009-1055), by walking the diagonals: cells ordered by
  * d = x + y (slash: x + Ry - 1 - y), inside a diagonal along y when Rx < Ry

@@ -38,6 +38,27 @@ CASES = [
     ("sor3d_n70_sw2", "sor3d", [70, 2, 1.5, 20261205], False),
     ("heat_c5_s3", "heat", [5, 5, 40, 3, 0.2, 13], True),
     ("heat_c24_s6", "heat", [24, 3, 150, 6, 0.2, 20261206], False),
+    # genred: n start end step seed, then the initial values ds dp dml imn ia io ix fmx lc
+    ("genred_n1000_s7", "genred", [1000, 3, 990, 7, 1017, 0.125, 1.5, 0.75, 123, -1, 256, 1515870810, -2.0, -9], True),
+    ("genred_n5000_sm13", "genred", [5000, 4990, 2, -13, 5017, 0.125, 1.5, 0.75, 123, -1, 256, 1515870810, -2.0, -9],
+     True),
+    ("genred_n300000_s1", "genred", [300000, 0, 299999, 1, 300017, 0.125, 1.5, 0.75, 123, -1, 256, 1515870810, -2.0,
+                                     -9], True),
+    ("genred_empty", "genred", [100, 50, 10, 1, 117, 0.125, 1.5, 0.75, 123, -1, 256, 1515870810, -2.0, -9], True),
+    ("genred_n777_sm1", "genred", [777, 776, 0, -1, 794, 0.125, 1.5, 0.75, 123, -1, 256, 1515870810, -2.0, -9], True),
+    ("genred_n777_keep", "genred", [777, 0, 776, 3, 795, -3.5, 0.25, 0.0, -2147483648, 0, -1, 0, 2.0, 41], True),
+    # gen3d: n0 n1 n2 seed, then the initial values s mx lc
+    ("gen3d_6x7x9", "gen3d", [6, 7, 9, 3, 0.5, -1.0, -5], True),
+    ("gen3d_3x3x3", "gen3d", [3, 3, 3, 12, 0.0, -1.0, -1], True),
+    ("gen3d_40x33x70_keep", "gen3d", [40, 33, 70, 20261210, -7.25, 5.0, 77], False),
+    ("gen3d_64x64x64", "gen3d", [64, 64, 64, 20261211, 0.0, -1.0, -1], False),
+    ("rec2d_5x9_sw2", "rec2d", [5, 9, 2, 3], True),
+    ("rec2d_37x52_sw3", "rec2d", [37, 52, 3, 4], False),
+    ("rec2d_1x40_sw2", "rec2d", [1, 40, 2, 8], True),
+    ("gsd3d_3x6x7_sw2", "gsd3d", [3, 6, 7, 2, 4], True),
+    ("gsd3d_5x19x27_sw3", "gsd3d", [5, 19, 27, 3, 40], False),
+    ("gs2d_n8_sw2", "gs2d", [8, 2, 5], True),
+    ("gs2d_n61_sw3", "gs2d", [61, 3, 20261209], False),
     ("gsd2d_9x7_fwd_mirror", "gsd2d", [9, 7, 3, 31, 1, 1, 1], True),
     ("gsd2d_6x11_slash", "gsd2d", [6, 11, 2, 32, 1, -1, 0], True),
     # The reference crashes (SIGSEGV in libdvm's across_) when an axis with a
@@ -87,6 +108,29 @@ def case(name, prog, params, full):
         d = np.frombuffer(raw, dtype="<f8")
         rec["s"] = hx(d[:sw])
         A = d[sw:sw + n ** 3]
+        rec["A_sha256"] = sha(A)
+        if full:
+            rec["A"] = hx(A)
+    elif prog == "genred":
+        rec["d3"] = hx(np.frombuffer(raw[0:24], dtype="<f8"))
+        rec["i4"] = [int(x) for x in np.frombuffer(raw[24:40], dtype="<i4")]
+        rec["f1"] = hx(np.frombuffer(raw[40:44], dtype="<f4"))
+        rec["lc"] = int(np.frombuffer(raw[44:52], dtype="<i8")[0])
+    elif prog == "gen3d":
+        cells = params[0] * params[1] * params[2]
+        rec["s_mx"] = hx(np.frombuffer(raw[0:16], dtype="<f8"))
+        rec["lc"] = int(np.frombuffer(raw[16:24], dtype="<i8")[0])
+        B = np.frombuffer(raw[24:24 + 8 * cells], dtype="<f8")
+        rec["B_sha256"] = sha(B)
+        if full:
+            rec["B"] = hx(B)
+    elif prog in ("rec2d", "gsd3d", "gs2d"):
+        cells = {"rec2d": lambda p: p[0] * p[1], "gsd3d": lambda p: p[0] * p[1] * p[2],
+                 "gs2d": lambda p: p[0] * p[0]}[prog](params)
+        sw = params[{"rec2d": 2, "gsd3d": 3, "gs2d": 1}[prog]]
+        d = np.frombuffer(raw, dtype="<f8")
+        rec["r"] = hx(d[:sw])
+        A = d[sw:sw + cells]
         rec["A_sha256"] = sha(A)
         if full:
             rec["A"] = hx(A)

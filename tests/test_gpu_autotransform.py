@@ -76,6 +76,33 @@ def test_golden(g, golden, mode, tfm):
             assert sha(b) == c["B_sha256"], name
 
 
+@pytest.mark.parametrize("mode", ["plain", "batched"])
+@pytest.mark.parametrize("tfm", [1, 0])
+@pytest.mark.parametrize("prog", ["rec2d", "gsd3d", "gs2d"])
+def test_golden_other_programs(g, golden, mode, tfm, prog):
+    """The reference runtime's outputs for the one-dependence recurrence
+    (permuted layout), the rank-3 program (diagonal plane under an outer
+    axis) and the one-thread Gauss-Seidel handler."""
+    g.set_mode(mode)
+    g.runtime().dvmhgb_set_autotransform(tfm)
+    w = g.workloads()
+    D, U, L = ctypes.POINTER(ctypes.c_double), ctypes.c_uint64, ctypes.c_long
+    w.wl_rec2d_run.argtypes = [L, L, L, U, D, D]
+    w.wl_gsd3d_run.argtypes = [L, L, L, L, U, D, D]
+    w.wl_gs2d_run.argtypes = [L, L, U, D, D]
+    cases = [(k, c) for k, c in golden.items() if c["prog"] == prog]
+    assert cases
+    for name, c in cases:
+        p = c["params"]
+        sw = p[{"rec2d": 2, "gsd3d": 3, "gs2d": 1}[prog]]
+        cells = {"rec2d": p[0] * p[1], "gsd3d": p[0] * p[1] * p[2], "gs2d": p[0] * p[0]}[prog]
+        r = np.zeros(sw)
+        a = np.zeros(cells)
+        assert getattr(w, "wl_%s_run" % prog)(*p, orc.P(r), orc.P(a)) == 0
+        assert [float(x).hex() for x in r] == c["r"], name
+        assert sha(a) == c["A_sha256"], name
+
+
 @pytest.mark.parametrize("mode", ["plain", "async", "batched"])
 @pytest.mark.parametrize("tfm", [1, 0])
 def test_modes_and_switch(g, mode, tfm):

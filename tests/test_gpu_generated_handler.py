@@ -104,3 +104,30 @@ def test_generated_shape_handler(g, shape, block, mode):
     assert lc.value == (((q[0] + 1) * n1 + q[1] + 1) * n2 + q[2] + 1 if vmax > 0.5 else -7)
     blk = block if block[0] else (32, 4, 2)
     assert s.value == expected_sum(b, blk, 0.25), (mode, shape, block)
+
+
+@pytest.mark.parametrize("mode", ["plain", "batched"])
+@pytest.mark.parametrize("block", [(0, 0, 0), (64, 2, 1)])
+def test_reference_golden(g, golden, mode, block):
+    """The reference runtime's own results (host handler, loop order): B and
+    MAXLOC bit for bit; SUM, folded per thread here, within n * 2^-53 * sum |b|
+    of the reference's sequential value (all terms positive)."""
+    import hashlib
+    g.set_mode(mode)
+    w = g.workloads()
+    w.wl_gen3d_run.argtypes = [ctypes.c_long] * 3 + [ctypes.c_uint64] + [ctypes.c_int] * 3 + [
+        ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_long),
+        ctypes.POINTER(ctypes.c_double)]
+    cases = [(k, c) for k, c in golden.items() if c["prog"] == "gen3d"]
+    assert cases
+    for name, c in cases:
+        n0, n1, n2, seed, s0, mx0, lc0 = c["params"]
+        s, mx, lc = ctypes.c_double(s0), ctypes.c_double(mx0), ctypes.c_long(lc0)
+        bout = np.zeros(n0 * n1 * n2)
+        assert w.wl_gen3d_run(n0, n1, n2, seed, *block, ctypes.byref(s), ctypes.byref(mx), ctypes.byref(lc),
+                              bout.ctypes.data_as(ctypes.POINTER(ctypes.c_double))) == 0
+        assert hashlib.sha256(bout.astype("<f8").tobytes()).hexdigest() == c["B_sha256"], name
+        assert mx.value.hex() == c["s_mx"][1] and lc.value == c["lc"], name
+        ref_s = float.fromhex(c["s_mx"][0])
+        cnt = max(0, (n0 - 2) * (n1 - 2) * (n2 - 2))
+        assert abs(s.value - ref_s) <= cnt * 2.0 ** -53 * (float(np.abs(bout).sum()) + abs(s0)), name

@@ -103,3 +103,36 @@ def test_generated_reductions(g, case, mode):
             assert (got[k] & 0xFFFFFFFF) == (want & 0xFFFFFFFF), (k, mode, case)
         else:
             assert got[k] == want, (k, mode, case, got[k], want)
+
+
+@pytest.mark.parametrize("mode", ["plain", "batched"])
+def test_reference_golden(g, golden, mode):
+    """The reference runtime's own results (its host handler, loop order):
+    MIN / MAX / AND / OR / XOR / MINLOC and the location bit for bit; SUM and
+    PROD, which the generated handler folds per thread, within the forward
+    error bound of the reference's sequential value (n additions: n * 2^-53 *
+    sum |x|; n multiplications by factors near 1: 2n * 2^-53 * |product|)."""
+    g.set_mode(mode)
+    w = g.workloads()
+    w.wl_genred_run.argtypes = [ctypes.c_long] * 4 + [ctypes.c_uint64, ctypes.c_int, ctypes.POINTER(ctypes.c_double),
+                                                      ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_float),
+                                                      ctypes.POINTER(ctypes.c_long)]
+    cases = [(k, c) for k, c in golden.items() if c["prog"] == "genred"]
+    assert cases
+    u = 2.0 ** -53
+    for name, c in cases:
+        n, start, end, step, seed = c["params"][:5]
+        init = c["params"][5:]
+        d3 = (ctypes.c_double * 3)(*init[0:3])
+        i4 = (ctypes.c_int * 4)(*init[3:7])
+        f1 = (ctypes.c_float * 1)(init[7])
+        lc = (ctypes.c_long * 1)(init[8])
+        assert w.wl_genred_run(n, start, end, step, seed, 0, d3, i4, f1, lc) == 0
+        ref_d = [float.fromhex(x) for x in c["d3"]]
+        cnt = max(0, (end - start) // step + 1)
+        assert abs(d3[0] - ref_d[0]) <= cnt * u * (abs(ref_d[0]) + abs(init[0])) + 0.0, name
+        assert abs(d3[1] - ref_d[1]) <= 2 * cnt * u * abs(ref_d[1]), name
+        assert float(d3[2]).hex() == c["d3"][2], name
+        assert list(i4) == c["i4"], name
+        assert float(f1[0]).hex() == c["f1"][0], name
+        assert lc[0] == c["lc"], name

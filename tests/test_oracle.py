@@ -24,7 +24,7 @@ def jac_cases(golden):
 
 def test_golden_present(golden):
     progs = {v["prog"] for v in golden.values()}
-    assert progs == {"jac2d", "jac3d", "sor3d", "heat", "gsd2d"}
+    assert progs == {"jac2d", "jac3d", "sor3d", "heat", "gsd2d", "genred", "rec2d", "gsd3d", "gs2d", "gen3d"}
 
 
 @pytest.mark.parametrize("rank", [2, 3])
@@ -99,6 +99,49 @@ def test_gsd2d_vs_reference(golden):
             assert np.array_equal(A, unhex(c["A"])), name
         if mirror:
             assert sha(A * 2.0) == c["B_sha256"], name
+
+
+@pytest.mark.parametrize("prog", ["rec2d", "gsd3d", "gs2d"])
+def test_across_programs_vs_reference(golden, prog):
+    """One-dependence recurrence (MIN), a diagonal plane under an independent
+    outer axis (MAX), one-thread Gauss-Seidel (SUM in loop order)."""
+    run = {"rec2d": orc.rec2d_run, "gsd3d": orc.gsd3d_run, "gs2d": orc.gs2d_run}[prog]
+    cases = [(k, c) for k, c in golden.items() if c["prog"] == prog]
+    assert cases
+    for name, c in cases:
+        r, A = run(*c["params"])
+        assert np.array_equal(r, unhex(c["r"])), name
+        assert sha(A) == c["A_sha256"], name
+        if "A" in c:
+            assert np.array_equal(A, unhex(c["A"])), name
+
+
+def test_gen3d_vs_reference(golden):
+    """SUM in loop order and MAXLOC (strict >, initial value kept when never
+    exceeded) of a 3-D parallel loop that reads a shadow edge."""
+    cases = [(k, c) for k, c in golden.items() if c["prog"] == "gen3d"]
+    assert cases
+    for name, c in cases:
+        s, mx, lc, B = orc.gen3d_run(*c["params"])
+        assert [s.hex(), mx.hex()] == c["s_mx"], name
+        assert lc == c["lc"], name
+        assert sha(B) == c["B_sha256"], name
+        if "B" in c:
+            assert np.array_equal(B, unhex(c["B"])), name
+
+
+def test_genred_vs_reference(golden):
+    """Eight reductions of four types with signed steps, an empty loop, and
+    initial values that the loop never improves on."""
+    for name, c in golden.items():
+        if c["prog"] != "genred":
+            continue
+        n, start, end, step, seed = c["params"][:5]
+        r = orc.genred_run(n, start, end, step, seed, c["params"][5:])
+        assert [float(x).hex() for x in r[0:3]] == c["d3"], name
+        assert list(r[3:7]) == c["i4"], name
+        assert float(r[7]).hex() == c["f1"][0], name
+        assert r[8] == c["lc"], name
 
 
 def test_pairwise_tree_identity():
