@@ -50,6 +50,9 @@ def lib():
         L.orc_rec2d_sweep.restype = ctypes.c_double
         L.orc_rec2d_sweep.argtypes = [ctypes.c_long, ctypes.c_long, _dp]
         L.orc_gen3d.argtypes = [ctypes.c_long] * 3 + [ctypes.c_uint64, _dp, _dp, ctypes.POINTER(ctypes.c_long), _dp]
+        _fp = ctypes.POINTER(ctypes.c_float)
+        L.orc_jacperf.restype = ctypes.c_long
+        L.orc_jacperf.argtypes = [ctypes.c_int, ctypes.c_long, ctypes.c_long, _fp, _fp, _fp]
         L.orc_max_threads.restype = ctypes.c_int
         _L = L
     return _L
@@ -148,6 +151,16 @@ def gen3d_run(n0, n1, n2, seed, s, mx, lc):
     lv = ctypes.c_long(lc)
     lib().orc_gen3d(n0, n1, n2, seed, ctypes.byref(sv), ctypes.byref(mv), ctypes.byref(lv), P(B))
     return sv.value, mv.value, lv.value, B
+
+
+def jacperf_run(rank, L, itmax):
+    """FP32 Jacobi benchmark: (iterations run, eps per iteration, A, B) as float32"""
+    fp = ctypes.POINTER(ctypes.c_float)
+    eps = np.zeros(itmax, dtype=np.float32)
+    A = np.zeros(L ** rank, dtype=np.float32)
+    B = np.zeros(L ** rank, dtype=np.float32)
+    its = lib().orc_jacperf(rank, L, itmax, eps.ctypes.data_as(fp), A.ctypes.data_as(fp), B.ctypes.data_as(fp))
+    return its, eps[:its], A, B
 
 
 def genred_run(n, start, end, step, seed, init):

@@ -13,6 +13,8 @@
  *   genred       n start end step seed ds dp dml imn ia io ix fmx lc   (initial values)
  *                -> ds dp dml (f64), imn ia io ix (int32), fmx (f32), lc (int64)
  *   gen3d        n0 n1 n2 seed s mx lc  -> s, mx (f64), lc (int64), B[n0*n1*n2]
+ *   jacperf      rank L itmax full      -> iterations run (int64), eps[itmax] (f32, 0 past
+ *                                          the last), then A, B (f32, L^rank) when full
  *   rec2d        n0 n1 sweeps seed      -> lo[sweeps], A[n0*n1]
  *   gsd3d        n0 n1 n2 sweeps seed   -> m[sweeps], A[n0*n1*n2]
  *   gs2d         n sweeps seed          -> s[sweeps], A[n*n]
@@ -44,6 +46,7 @@ int wl_genred_run(long n, long start, long end, long step, uint64_t seed, int bx
                   long *lc);
 int wl_gen3d_run(long n0, long n1, long n2, uint64_t seed, int bx, int by, int bz, double *s, double *mx, long *lc,
                  double *b_out);
+long wl_jacperf_run(int rank, long L, long itmax, float *eps_out, float *a_out, float *b_out);
 int wl_rec2d_run(long n0, long n1, long sweeps, uint64_t seed, double *lo_out, double *a_out);
 int wl_gsd3d_run(long n0, long n1, long n2, long sweeps, uint64_t seed, double *m_out, double *a_out);
 int wl_gs2d_run(long n, long sweeps, uint64_t seed, double *s_out, double *a_out);
@@ -158,6 +161,21 @@ int main(int argc, char **argv) {
         put(f, &mx, sizeof(mx));
         put(f, &lc, sizeof(lc));
         put(f, b, sizeof(double) * n0 * n1 * n2);
+    } else if (!strcmp(argv[1], "jacperf")) {
+        int rank = atoi(argv[3]), full = atoi(argv[6]);
+        long L = atol(argv[4]), itmax = atol(argv[5]), its, cells = rank == 3 ? L * L * L : L * L;
+        float *e = calloc((size_t)itmax, sizeof(float)), *a = 0, *b = 0;
+        if (full) {
+            a = malloc(sizeof(float) * cells);
+            b = malloc(sizeof(float) * cells);
+        }
+        its = wl_jacperf_run(rank, L, itmax, e, a, b);
+        put(f, &its, sizeof(its));
+        put(f, e, sizeof(float) * itmax);
+        if (full) {
+            put(f, a, sizeof(float) * cells);
+            put(f, b, sizeof(float) * cells);
+        }
     } else if (!strcmp(argv[1], "rec2d") || !strcmp(argv[1], "gs2d") || !strcmp(argv[1], "gsd3d")) {
         int r3 = !strcmp(argv[1], "gsd3d"), sq = !strcmp(argv[1], "gs2d");
         long n0 = atol(argv[3]), n1 = sq ? n0 : atol(argv[4]), n2 = r3 ? atol(argv[5]) : 1;

@@ -390,6 +390,59 @@ void orc_gen3d(long n0, long n1, long n2, uint64_t seed, double *s, double *mx, 
 }
 
 /*
+ * The reference's FP32 Jacobi benchmarks (examples/Performance/jac2d_perf.c
+ * and jac3d_perf.c; dvm-snapshot-r6603-fork_gb300/workloads/jacperf.c): A = 0,
+ * B = c + sum of indices inside (c = 3 in 2-D, 4 in 3-D), then per iteration
+ * eps = MAX |B - A|, A = B over the interior and B = (sum of the 2r
+ * neighbours of A in the program's order) / (2r)f, stopping after the first
+ * iteration with eps < 0.5.  All arithmetic in float.  eps_out[it] per
+ * iteration; A, B dense L^rank.  Returns the iterations run.
+ */
+long orc_jacperf(int rank, long L, long itmax, float *eps_out, float *A, float *B) {
+    const long n2 = L * L, planes = rank == 3 ? L : 1, rows = L;
+    long it, done = 0;
+    /* rank 2 is the 3-D walk with one plane and no plane neighbours */
+    for (long i = 0; i < planes; i++)
+        for (long j = 0; j < rows; j++)
+            for (long k = 0; k < L; k++) {
+                const long q = (i * L + j) * L + k;
+                A[q] = 0.0f;
+                if (rank == 3)
+                    B[q] = (i == 0 || j == 0 || k == 0 || i == L - 1 || j == L - 1 || k == L - 1) ? 0.0f
+                                                                                                  : (float)(4 + i + j + k);
+                else
+                    B[q] = (j == 0 || k == 0 || j == L - 1 || k == L - 1) ? 0.0f : (float)(3 + j + k);
+            }
+    const long i0 = rank == 3 ? 1 : 0, i1 = rank == 3 ? L - 2 : 0;
+    for (it = 1; it <= itmax; it++) {
+        float eps = 0.0f;
+#pragma omp parallel for collapse(2) reduction(max : eps) schedule(static)
+        for (long i = i0; i <= i1; i++)
+            for (long j = 1; j <= L - 2; j++)
+                for (long k = 1; k <= L - 2; k++) {
+                    const long q = (i * L + j) * L + k;
+                    float tmp = fabsf(B[q] - A[q]);
+                    eps = tmp > eps ? tmp : eps;
+                    A[q] = B[q];
+                }
+#pragma omp parallel for collapse(2) schedule(static)
+        for (long i = i0; i <= i1; i++)
+            for (long j = 1; j <= L - 2; j++)
+                for (long k = 1; k <= L - 2; k++) {
+                    const long q = (i * L + j) * L + k;
+                    if (rank == 3)
+                        B[q] = (A[q - n2] + A[q - L] + A[q - 1] + A[q + 1] + A[q + L] + A[q + n2]) / 6.0f;
+                    else
+                        B[q] = (A[q - L] + A[q - 1] + A[q + 1] + A[q + L]) / 4.0f;
+                }
+        eps_out[it - 1] = eps;
+        done = it;
+        if (eps < 0.5f) break;
+    }
+    return done;
+}
+
+/*
  * The eight reductions of a 1-D loop with a signed step
  * (dvm-snapshot-r6603-fork_gb300/workloads/genred.c), in loop order, combined
  * as the reference's engine combines them (rts/dvmh/loop.cpp:37-113): the

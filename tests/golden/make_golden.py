@@ -47,6 +47,14 @@ CASES = [
     ("genred_empty", "genred", [100, 50, 10, 1, 117, 0.125, 1.5, 0.75, 123, -1, 256, 1515870810, -2.0, -9], True),
     ("genred_n777_sm1", "genred", [777, 776, 0, -1, 794, 0.125, 1.5, 0.75, 123, -1, 256, 1515870810, -2.0, -9], True),
     ("genred_n777_keep", "genred", [777, 0, 776, 3, 795, -3.5, 0.25, 0.0, -2147483648, 0, -1, 0, 2.0, 41], True),
+    # jacperf: rank L itmax (the reference's FP32 benchmarks; the last two are their
+    # full configurations, whose final eps the examples verify)
+    ("jacperf3_L12_it5", "jacperf", [3, 12, 5], True),
+    ("jacperf2_L20_it7", "jacperf", [2, 20, 7], True),
+    ("jacperf2_L10_it100", "jacperf", [2, 10, 100], True),
+    ("jacperf3_L67_it9", "jacperf", [3, 67, 9], False),
+    ("jacperf3_L384_it100", "jacperf", [3, 384, 100], False),
+    ("jacperf2_L8000_it100", "jacperf", [2, 8000, 100], False),
     # gen3d: n0 n1 n2 seed, then the initial values s mx lc
     ("gen3d_6x7x9", "gen3d", [6, 7, 9, 3, 0.5, -1.0, -5], True),
     ("gen3d_3x3x3", "gen3d", [3, 3, 3, 12, 0.0, -1.0, -1], True),
@@ -74,6 +82,10 @@ def sha(a):
     return hashlib.sha256(np.ascontiguousarray(a, dtype="<f8").tobytes()).hexdigest()
 
 
+def sha32(a):
+    return hashlib.sha256(np.ascontiguousarray(a, dtype="<f4").tobytes()).hexdigest()
+
+
 def hx(a):
     return [float(x).hex() for x in np.asarray(a, dtype=np.float64).ravel()]
 
@@ -83,9 +95,14 @@ def build():
 
 
 def run(prog, params):
+    # one thread (loop order) except for the FP32 benchmarks, whose only
+    # reduction is MAX: order-independent, so they may use every core
+    threads = str(os.cpu_count()) if prog == "jacperf" else "1"
+    if prog == "jacperf":
+        params = list(params) + [1]
     with tempfile.TemporaryDirectory() as td:
         out = os.path.join(td, "o.bin")
-        env = dict(os.environ, DVMH_NUM_THREADS="1", OMP_SCHEDULE="static")
+        env = dict(os.environ, DVMH_NUM_THREADS=threads, OMP_SCHEDULE="static")
         subprocess.check_call([DRIVER, prog, out] + [str(p) for p in params], cwd=td, env=env,
                               stdout=subprocess.DEVNULL)
         return open(out, "rb").read()
@@ -116,6 +133,18 @@ def case(name, prog, params, full):
         rec["i4"] = [int(x) for x in np.frombuffer(raw[24:40], dtype="<i4")]
         rec["f1"] = hx(np.frombuffer(raw[40:44], dtype="<f4"))
         rec["lc"] = int(np.frombuffer(raw[44:52], dtype="<i8")[0])
+    elif prog == "jacperf":
+        rank, L, itmax = params
+        cells = L ** rank
+        its = int(np.frombuffer(raw[0:8], dtype="<i8")[0])
+        rec["its"] = its
+        rec["eps"] = hx(np.frombuffer(raw[8:8 + 4 * its], dtype="<f4"))
+        off = 8 + 4 * itmax
+        A = np.frombuffer(raw[off:off + 4 * cells], dtype="<f4")
+        B = np.frombuffer(raw[off + 4 * cells:off + 8 * cells], dtype="<f4")
+        rec["A_sha256"], rec["B_sha256"] = sha32(A), sha32(B)
+        if full:
+            rec["A"], rec["B"] = hx(A), hx(B)
     elif prog == "gen3d":
         cells = params[0] * params[1] * params[2]
         rec["s_mx"] = hx(np.frombuffer(raw[0:16], dtype="<f8"))

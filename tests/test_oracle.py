@@ -24,7 +24,31 @@ def jac_cases(golden):
 
 def test_golden_present(golden):
     progs = {v["prog"] for v in golden.values()}
-    assert progs == {"jac2d", "jac3d", "sor3d", "heat", "gsd2d", "genred", "rec2d", "gsd3d", "gs2d", "gen3d"}
+    assert progs == {"jac2d", "jac3d", "sor3d", "heat", "gsd2d", "genred", "rec2d", "gsd3d", "gs2d", "gen3d",
+                     "jacperf"}
+
+
+# the reference examples' own verification (examples/Performance/jac3d_perf.c:92, jac2d_perf.c:89)
+KNOWN_ANSWERS = {(3, 384, 100): (5.058044, 1e-4), (2, 8000, 100): (58.37598, 1e-3)}
+
+
+def sha32(a):
+    return hashlib.sha256(np.ascontiguousarray(a, dtype="<f4").tobytes()).hexdigest()
+
+
+def test_jacperf_vs_reference(golden):
+    """The reference's FP32 Jacobi benchmarks, including both full
+    configurations (about 4 s each here) and an early stop at eps < 0.5."""
+    cases = [(k, c) for k, c in golden.items() if c["prog"] == "jacperf"]
+    assert {tuple(c["params"]) for _, c in cases} >= set(KNOWN_ANSWERS)
+    for name, c in cases:
+        its, eps, A, B = orc.jacperf_run(*c["params"])
+        assert its == c["its"], name
+        assert [float(x).hex() for x in eps] == c["eps"], name
+        assert sha32(A) == c["A_sha256"] and sha32(B) == c["B_sha256"], name
+        ka = KNOWN_ANSWERS.get(tuple(c["params"]))
+        if ka:
+            assert abs(float(eps[-1]) - ka[0]) < ka[1], name
 
 
 @pytest.mark.parametrize("rank", [2, 3])
