@@ -190,7 +190,7 @@ def main():
     ap.add_argument("--impl", default="gb300")
     ap.add_argument("--grid", type=int, default=N_DEFAULT)
     ap.add_argument("--quick", action="store_true", help="headline only (no extra modes/configs/cpu leg)")
-    ap.add_argument("--only", choices=["jacobi3d", "jacobi2d", "sor", "heat", "gsd2d"], default=None,
+    ap.add_argument("--only", choices=["jacobi3d", "jacobi2d", "sor", "heat", "gsd2d", "jacperf"], default=None,
                     help="time one workload alone (small cases for profiling): --grid is its size "
                          "(heat: the largest side), --steps its steps or sweeps")
     ap.add_argument("--mode", choices=["batched", "async", "plain"], default="batched", help="with --only")
@@ -343,6 +343,8 @@ def run_only(args, g, stream):
     g.set_mode(args.mode)
     if args.only == "gsd2d":
         return run_gsd2d(args, g, stream)
+    if args.only == "jacperf":
+        return run_jacperf(args, g)
     if args.only == "jacobi3d":
         w = g.Jacobi(3, args.grid, SEED)
         cells, unit = (args.grid - 2) ** 3, "step"
@@ -369,6 +371,24 @@ def run_only(args, g, stream):
     g.force_variant(-1)
     print(json.dumps({"workload": args.only, "grid": args.grid, "mode": args.mode, "variant": args.variant,
                       "steps": args.steps, "ms_per_" + unit: ms, "cell-updates/s": cells / (ms * 1e-3)}), flush=True)
+
+
+def run_jacperf(args, g):
+    """The FP32 Jacobi-3D benchmark program (--grid L, --steps iterations) once,
+    after one warm-up run of --warmup iterations; wall time of the whole program."""
+    import ctypes
+    import numpy as np
+    w = g.workloads()
+    fp = ctypes.POINTER(ctypes.c_float)
+    w.wl_jacperf_run.restype = ctypes.c_long
+    w.wl_jacperf_run.argtypes = [ctypes.c_int, ctypes.c_long, ctypes.c_long, fp, fp, fp]
+    eps = np.zeros(max(args.steps, args.warmup, 1), dtype=np.float32)
+    w.wl_jacperf_run(3, args.grid, max(args.warmup, 1), eps.ctypes.data_as(fp), None, None)
+    t0 = time.time()
+    its = w.wl_jacperf_run(3, args.grid, args.steps, eps.ctypes.data_as(fp), None, None)
+    dt = time.time() - t0
+    print(json.dumps({"workload": "jacperf3d_fp32", "grid": args.grid, "mode": args.mode, "iterations": its,
+                      "program_wall_ms": 1e3 * dt, "eps_last": float(eps[its - 1])}), flush=True)
 
 
 def run_gsd2d(args, g, stream):
@@ -472,7 +492,53 @@ def extra_configs(g, stream):
     g.set_mode("batched")
     out["gsd2d_layouts_2048"] = gsd2d_layouts(g, stream, 2048, 2)
     out["jacobi2d_1024"] = jacobi2d(g, stream, 1024, 100)
+    out["jacperf3d_fp32_384"] = jacperf(g, 3, 384, 5.058044, 1e-4)
+    out["jacperf2d_fp32_8000"] = jacperf(g, 2, 8000, 58.37598, 1e-3)
     return out
+
+
+def jacperf(g, rank, L, answer, tol):
+    """The reference's FP32 Jacobi benchmark programs (examples/Performance/
+    jac3d_perf.c, jac2d_perf.c) as whole programs through handlers in cdvmh's
+    generated shape: per iteration = (T(100 iterations) - T(10)) / 90 of the
+    program's wall time, which cancels allocation, the device init loop and
+    teardown; every iteration reads eps back as the program does.  verified =
+    the example's own check on eps after 100 iterations."""
+    import ctypes
+    import numpy as np
+    from oracle import orc
+    w = g.workloads()
+    fp = ctypes.POINTER(ctypes.c_float)
+    w.wl_jacperf_run.restype = ctypes.c_long
+    w.wl_jacperf_run.argtypes = [ctypes.c_int, ctypes.c_long, ctypes.c_long, fp, fp, fp]
+    eps = np.zeros(100, dtype=np.float32)
+    res = {}
+    for mode in ("batched", "plain"):
+        g.set_mode(mode)
+        w.wl_jacperf_run(rank, L, 3, eps.ctypes.data_as(fp), None, None)
+        t = {}
+        for its in (10, 100):
+            t0 = time.time()
+            w.wl_jacperf_run(rank, L, its, eps.ctypes.data_as(fp), None, None)
+            t[its] = time.time() - t0
+        ms = 1e3 * (t[100] - t[10]) / 90
+        res[mode] = {"ms_per_iteration": ms, "value": (L - 2) ** rank / (ms * 1e-3),
+                     "eps_100": float(eps[99]), "verified": bool(abs(float(eps[99]) - answer) < tol)}
+    g.set_mode("batched")
+    peak, _ = peaks()
+    for m in ("batched", "plain"):
+        res[m]["hbm_frac"] = res[m]["value"] * 20 / 1e9 / peak
+    # the CPU port (oracle restatement, every host thread), 10 iterations
+    L_ = orc.lib()
+    t0 = time.time()
+    orc.jacperf_run(rank, L, 10)
+    t10 = time.time() - t0
+    t0 = time.time()
+    orc.jacperf_run(rank, L, 1)
+    t1 = time.time() - t0
+    res["cpu_port"] = {"ms_per_iteration": 1e3 * (t10 - t1) / 9, "cores": L_.orc_max_threads()}
+    res["cpu_port"]["value"] = (L - 2) ** rank / (res["cpu_port"]["ms_per_iteration"] * 1e-3)
+    return {"unit": "cell-updates/s", "bytes_per_cell": 20, "dtype": "f32", "reference_check": [answer, tol], **res}
 
 
 def jacobi2d(g, stream, n, iters):

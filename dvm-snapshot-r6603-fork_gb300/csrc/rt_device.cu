@@ -498,9 +498,182 @@ __global__ void __launch_bounds__(FOLD_THREADS) kFold(int op, long count, long e
     }
 }
 
+// ---- the same tree, bandwidth-bound (one value per item: elemCount == 1)
+//
+// A block folds an aligned span of FOLD2_SPAN = 2048 items: each thread loads 8
+// consecutive items with vector loads and folds them as the three lowest tree
+// levels in registers, the warp folds its 32 threads' nodes by shuffles (lane
+// a takes lane a + w, a a multiple of 2w), and warp 0 folds the 8 warps' nodes.
+// Every node is the pairwise tree over an aligned power-of-two index range with
+// the identity beyond the last item, exactly as in kFold; spans of 2048 instead
+// of 1024 only add levels that combine a node with the identity.  That is why
+// this path is taken only for the operations where x (+) identity = x for every
+// non-NaN x (SUM, PROD, MAX, MIN, AND, OR, XOR and the LOC pair), not for the
+// logical EQU / EQ / NE.
+constexpr int FOLD2_THREADS = 256;
+constexpr int FOLD2_PER = 8;
+constexpr int FOLD2_SPAN = FOLD2_THREADS * FOLD2_PER;
+
+template <typename T>
+__device__ __forceinline__ T shflDown(T v, int w) {
+    if constexpr (sizeof(T) < 4)
+        return (T)__shfl_down_sync(0xffffffffu, (int)v, w);
+    else
+        return __shfl_down_sync(0xffffffffu, v, w);
+}
+
+// 8 consecutive values of a 16-byte aligned (8-byte for 1-byte types) address,
+// read once: streaming loads
+template <typename T>
+__device__ __forceinline__ void load8(const T *p, T v[8]) {
+    constexpr int B = (int)sizeof(T) * 8;
+    if constexpr (B % 16 == 0) {
+        uint4 r[B / 16];
+#pragma unroll
+        for (int i = 0; i < B / 16; i++) r[i] = __ldcs(reinterpret_cast<const uint4 *>(p) + i);
+        memcpy(v, r, B);
+    } else {
+        uint2 r = __ldcs(reinterpret_cast<const uint2 *>(p));
+        memcpy(v, &r, 8);
+    }
+}
+
+// d (+)= s, d the lower-index node; with LOC the lower index wins ties and an
+// identity node (index -1) never wins, as in kFold
+template <typename T, bool INT, bool LOC>
+__device__ __forceinline__ void step2(int op, T &d, long &di, T s, long si) {
+    if (LOC) {
+        T x = d;
+        const bool take = (di < 0 && si >= 0) || (si >= 0 && Comb<T, INT>::f(op, x, s));
+        if (take) {
+            d = s;
+            di = si;
+        }
+    } else {
+        Comb<T, INT>::f(op, d, s);
+    }
+}
+
+template <typename T, bool INT, bool LOC>
+__global__ void __launch_bounds__(FOLD2_THREADS) kFold2(int op, long count, const T *items, const long *itemIdx,
+                                                        T *out, long *outIdx, int final, T *dst, const char *locItems,
+                                                        long locSize, char *dstLoc) {
+    __shared__ T sw[FOLD2_THREADS / 32];
+    __shared__ long swi[FOLD2_THREADS / 32];
+    const T ident = identityOf<T>(op);
+    const long base = blockIdx.x * (long)FOLD2_SPAN + threadIdx.x * (long)FOLD2_PER;
+    T v[FOLD2_PER];
+    long vi[FOLD2_PER];
+    if (base + FOLD2_PER <= count) {
+        load8(items + base, v);
+        if (LOC) {
+            if (itemIdx)
+                load8(itemIdx + base, vi);
+            else
+#pragma unroll
+                for (int j = 0; j < FOLD2_PER; j++) vi[j] = base + j;
+        }
+    } else {
+#pragma unroll
+        for (int j = 0; j < FOLD2_PER; j++) {
+            const long i = base + j;
+            const bool in = i < count;
+            v[j] = in ? items[i] : ident;
+            vi[j] = in ? (itemIdx ? itemIdx[i] : i) : -1;
+        }
+    }
+#pragma unroll
+    for (int w = 1; w < FOLD2_PER; w <<= 1)
+#pragma unroll
+        for (int a = 0; a < FOLD2_PER; a += 2 * w) step2<T, INT, LOC>(op, v[a], vi[a], v[a + w], vi[a + w]);
+    T x = v[0];
+    long xi = LOC ? vi[0] : 0;
+    const int lane = threadIdx.x & 31;
+#pragma unroll
+    for (int w = 1; w < 32; w <<= 1) {
+        const T sv = shflDown(x, w);
+        const long si = LOC ? __shfl_down_sync(0xffffffffu, xi, w) : 0;
+        if ((lane & (2 * w - 1)) == 0) step2<T, INT, LOC>(op, x, xi, sv, si);
+    }
+    if (lane == 0) {
+        sw[threadIdx.x >> 5] = x;
+        swi[threadIdx.x >> 5] = xi;
+    }
+    __syncthreads();
+    if (threadIdx.x >= 32) return;
+    constexpr int NW = FOLD2_THREADS / 32;
+    x = lane < NW ? sw[lane] : ident;
+    xi = lane < NW ? swi[lane] : -1;
+#pragma unroll
+    for (int w = 1; w < NW; w <<= 1) {
+        const T sv = shflDown(x, w);
+        const long si = LOC ? __shfl_down_sync(0xffffffffu, xi, w) : 0;
+        if ((lane & (2 * w - 1)) == 0) step2<T, INT, LOC>(op, x, xi, sv, si);
+    }
+    if (lane != 0) return;
+    if (!final) {
+        out[blockIdx.x] = x;
+        if (LOC) outIdx[blockIdx.x] = xi;
+        return;
+    }
+    // (global start (+) loop value) (+) initial value, as kFold's final pass
+    const T init = dst[0];
+    T r;
+    switch (op) {
+        case rf_SUM: case rf_XOR: r = (T)0; break;
+        case rf_PROD: r = (T)1; break;
+        default: r = init;
+    }
+    bool fromLoop = false;
+    if (LOC) {
+        if (xi >= 0) fromLoop = Comb<T, INT>::f(op, r, x);
+    } else {
+        Comb<T, INT>::f(op, r, x);
+        Comb<T, INT>::f(op, r, init);
+    }
+    dst[0] = r;
+    if (LOC && fromLoop && dstLoc && locItems)
+        for (long b = 0; b < locSize; b++) dstLoc[b] = locItems[xi * locSize + b];
+}
+
+template <typename T, bool INT, bool LOC>
+static void fold2T(int op, long count, const void *items, const void *locItems, long locSize, void *dst, void *dstLoc,
+                   cudaStream_t s, std::vector<void *> &scratch) {
+    const T *cur = (const T *)items;
+    const long *curIdx = nullptr;
+    long n = count;
+    while (n > FOLD2_SPAN) {
+        const long blocks = (n + FOLD2_SPAN - 1) / FOLD2_SPAN;
+        T *out = (T *)devAlloc(sizeof(T) * blocks);
+        long *outIdx = LOC ? (long *)devAlloc(sizeof(long) * blocks) : nullptr;
+        scratch.push_back(out);
+        if (outIdx) scratch.push_back(outIdx);
+        kFold2<T, INT, LOC><<<(unsigned)blocks, FOLD2_THREADS, 0, s>>>(op, n, cur, curIdx, out, outIdx, 0, nullptr,
+                                                                      nullptr, 0, nullptr);
+        dvmhgb_count_launches(1);
+        cur = out;
+        curIdx = outIdx;
+        n = blocks;
+    }
+    kFold2<T, INT, LOC><<<1, FOLD2_THREADS, 0, s>>>(op, n, cur, curIdx, nullptr, nullptr, 1, (T *)dst,
+                                                   (const char *)locItems, locSize, (char *)dstLoc);
+    dvmhgb_count_launches(1);
+    GB_CUDA(cudaGetLastError());
+}
+
 template <typename T, bool INT>
 static void foldT(int op, long count, long elemCount, const void *items, const void *locItems, long locSize, void *dst,
                   void *dstLoc, cudaStream_t s, std::vector<void *> &scratch) {
+    const bool loc = op == rf_MINLOC || op == rf_MAXLOC;
+    const bool neutralPad = op == rf_SUM || op == rf_PROD || op == rf_MAX || op == rf_MIN || op == rf_AND ||
+                            op == rf_OR || op == rf_XOR || loc;
+    if (elemCount == 1 && neutralPad && ((uintptr_t)items & 15) == 0) {
+        if (loc)
+            fold2T<T, INT, true>(op, count, items, locItems, locSize, dst, dstLoc, s, scratch);
+        else
+            fold2T<T, INT, false>(op, count, items, locItems, locSize, dst, dstLoc, s, scratch);
+        return;
+    }
     const T *cur = (const T *)items;
     const long *curIdx = nullptr;
     long n = count;
