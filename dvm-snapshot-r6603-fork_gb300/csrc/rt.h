@@ -298,7 +298,7 @@ struct FoldJob {
     const void *items, *locItems;
     long locSize;
     void *dst, *dstLoc;
-    long blockBase;  // first of this job's 1024-item blocks in the batch (set by launchRedFoldBatch)
+    long blockBase;  // first of this job's 2048-item spans in the batch (set by launchRedFoldBatch)
 };
 bool foldBatchable(int op, int vtype, long count, long elemCount);
 void launchRedFoldBatch(const std::vector<FoldJob> &jobs, cudaStream_t s, std::vector<void *> &devScratch,

@@ -554,17 +554,23 @@ __device__ __forceinline__ void step2(int op, T &d, long &di, T s, long si) {
     }
 }
 
+// The node of aligned span `span` (items [span * FOLD2_SPAN, +FOLD2_SPAN), the
+// identity beyond `count`), computed by the whole CTA; true on thread 0, which
+// holds it in x (and its item index in xi for LOC ops).  itemIdx: the items'
+// indices (a previous pass's winners), null = their positions.  Vector loads
+// where the 8 items lie inside `count` on a 16-byte boundary.
 template <typename T, bool INT, bool LOC>
-__global__ void __launch_bounds__(FOLD2_THREADS) kFold2(int op, long count, const T *items, const long *itemIdx,
-                                                        T *out, long *outIdx, int final, T *dst, const char *locItems,
-                                                        long locSize, char *dstLoc) {
+__device__ __forceinline__ bool span2(int op, long count, const T *items, const long *itemIdx, long span, T &x,
+                                      long &xi) {
     __shared__ T sw[FOLD2_THREADS / 32];
     __shared__ long swi[FOLD2_THREADS / 32];
     const T ident = identityOf<T>(op);
-    const long base = blockIdx.x * (long)FOLD2_SPAN + threadIdx.x * (long)FOLD2_PER;
+    const long base = span * FOLD2_SPAN + threadIdx.x * (long)FOLD2_PER;
     T v[FOLD2_PER];
     long vi[FOLD2_PER];
-    if (base + FOLD2_PER <= count) {
+    const bool whole = base + FOLD2_PER <= count && ((uintptr_t)(items + base) & 15) == 0 &&
+                       (!LOC || !itemIdx || ((uintptr_t)(itemIdx + base) & 15) == 0);
+    if (whole) {
         load8(items + base, v);
         if (LOC) {
             if (itemIdx)
@@ -586,8 +592,8 @@ __global__ void __launch_bounds__(FOLD2_THREADS) kFold2(int op, long count, cons
     for (int w = 1; w < FOLD2_PER; w <<= 1)
 #pragma unroll
         for (int a = 0; a < FOLD2_PER; a += 2 * w) step2<T, INT, LOC>(op, v[a], vi[a], v[a + w], vi[a + w]);
-    T x = v[0];
-    long xi = LOC ? vi[0] : 0;
+    x = v[0];
+    xi = LOC ? vi[0] : 0;
     const int lane = threadIdx.x & 31;
 #pragma unroll
     for (int w = 1; w < 32; w <<= 1) {
@@ -600,7 +606,7 @@ __global__ void __launch_bounds__(FOLD2_THREADS) kFold2(int op, long count, cons
         swi[threadIdx.x >> 5] = xi;
     }
     __syncthreads();
-    if (threadIdx.x >= 32) return;
+    if (threadIdx.x >= 32) return false;
     constexpr int NW = FOLD2_THREADS / 32;
     x = lane < NW ? sw[lane] : ident;
     xi = lane < NW ? swi[lane] : -1;
@@ -610,13 +616,14 @@ __global__ void __launch_bounds__(FOLD2_THREADS) kFold2(int op, long count, cons
         const long si = LOC ? __shfl_down_sync(0xffffffffu, xi, w) : 0;
         if ((lane & (2 * w - 1)) == 0) step2<T, INT, LOC>(op, x, xi, sv, si);
     }
-    if (lane != 0) return;
-    if (!final) {
-        out[blockIdx.x] = x;
-        if (LOC) outIdx[blockIdx.x] = xi;
-        return;
-    }
-    // (global start (+) loop value) (+) initial value, as kFold's final pass
+    return lane == 0;
+}
+
+// (global start (+) loop value) (+) initial value into dst[0] (and the winner's
+// loc bytes into dstLoc), the combination kFold's final pass makes
+template <typename T, bool INT, bool LOC>
+__device__ __forceinline__ void finish2(int op, T x, long xi, T *dst, const char *locItems, long locSize,
+                                        char *dstLoc) {
     const T init = dst[0];
     T r;
     switch (op) {
@@ -634,6 +641,21 @@ __global__ void __launch_bounds__(FOLD2_THREADS) kFold2(int op, long count, cons
     dst[0] = r;
     if (LOC && fromLoop && dstLoc && locItems)
         for (long b = 0; b < locSize; b++) dstLoc[b] = locItems[xi * locSize + b];
+}
+
+template <typename T, bool INT, bool LOC>
+__global__ void __launch_bounds__(FOLD2_THREADS) kFold2(int op, long count, const T *items, const long *itemIdx,
+                                                        T *out, long *outIdx, int final, T *dst, const char *locItems,
+                                                        long locSize, char *dstLoc) {
+    T x;
+    long xi;
+    if (!span2<T, INT, LOC>(op, count, items, itemIdx, blockIdx.x, x, xi)) return;
+    if (final) {
+        finish2<T, INT, LOC>(op, x, xi, dst, locItems, locSize, dstLoc);
+    } else {
+        out[blockIdx.x] = x;
+        if (LOC) outIdx[blockIdx.x] = xi;
+    }
 }
 
 template <typename T, bool INT, bool LOC>
@@ -724,102 +746,54 @@ void launchRedFold(int op, int vtype, long count, long elemCount, const void *it
 
 // ---------------------------------------------------------------- segmented fold (batches)
 
-// One CTA per reduction: blocks of FOLD_SPAN items are folded by the pairwise
-// tree (as kFold does), block results are kept in shared memory and folded by
-// the pairwise tree again -- the same tree as the multi-pass fold, so the
-// result is identical -- then combined with the initial value.
-// pairwise tree over v[0..FOLD_SPAN) (and the item indices vi for LOC ops) in
-// shared memory; the result is left in v[0], vi[0]
-__device__ void foldSpan(int op, bool loc, double *v, long *vi) {
-    for (int w = 1; w < FOLD_SPAN; w <<= 1) {
-        int pairs = FOLD_SPAN / (2 * w);
-        for (int p = threadIdx.x; p < pairs; p += FOLD_THREADS) {
-            int a = p * 2 * w, b = a + w;
-            double d = v[a];
-            if (loc) {
-                bool take = (vi[a] < 0 && vi[b] >= 0) || (vi[b] >= 0 && combine<double>(op, d, v[b]));
-                if (take) {
-                    v[a] = v[b];
-                    vi[a] = vi[b];
-                }
-            } else {
-                combine<double>(op, d, v[b]);
-                v[a] = d;
-            }
-        }
-        __syncthreads();
-    }
-}
-
-// pass 1: one CTA per 1024-item block of every job (CTAs of all jobs at once)
-__global__ void __launch_bounds__(FOLD_THREADS) kFoldSegBlocks(const FoldJob *jobs, int njobs, double *bv, long *bi) {
-    __shared__ double sv[FOLD_SPAN];
-    __shared__ long si[FOLD_SPAN];
-    const long gb = blockIdx.x;
-    int lo = 0, hi = njobs - 1;  // the job whose blocks hold gb: last blockBase <= gb
+// Every reduction of a batch at once, by the tree of the single fold (kFold2):
+// pass 1 gives every aligned 2048-item span of every job its own CTA, pass 2
+// one CTA per job folds that job's span nodes (at most 2048: the spans are the
+// next level's items) and combines the result with the initial value.
+__device__ __forceinline__ int jobOf(const FoldJob *jobs, int njobs, long gb) {
+    int lo = 0, hi = njobs - 1;  // the last job with blockBase <= gb
     while (lo < hi) {
         const int mid = (lo + hi + 1) >> 1;
         if (jobs[mid].blockBase <= gb) lo = mid;
         else hi = mid - 1;
     }
-    const FoldJob &J = jobs[lo];
-    const int op = J.op;
-    const bool loc = (op == rf_MINLOC || op == rf_MAXLOC);
-    const double ident = identityOf<double>(op);
+    return lo;
+}
+
+__global__ void __launch_bounds__(FOLD2_THREADS) kFoldSegBlocks(const FoldJob *jobs, int njobs, double *bv, long *bi) {
+    const long gb = blockIdx.x;
+    const FoldJob &J = jobs[jobOf(jobs, njobs, gb)];
     const double *items = (const double *)J.items;
-    const long blk = gb - J.blockBase;
-    for (int h = 0; h < 2; h++) {
-        long i = blk * FOLD_SPAN + h * FOLD_THREADS + threadIdx.x;
-        bool in = i < J.count;
-        sv[h * FOLD_THREADS + threadIdx.x] = in ? items[i] : ident;
-        si[h * FOLD_THREADS + threadIdx.x] = in ? i : -1;
-    }
-    __syncthreads();
-    foldSpan(op, loc, sv, si);
-    if (threadIdx.x == 0) {
-        bv[gb] = sv[0];
-        bi[gb] = si[0];
+    double x;
+    long xi;
+    bool lead;
+    if (J.op == rf_MINLOC || J.op == rf_MAXLOC)
+        lead = span2<double, false, true>(J.op, J.count, items, nullptr, gb - J.blockBase, x, xi);
+    else
+        lead = span2<double, false, false>(J.op, J.count, items, nullptr, gb - J.blockBase, x, xi);
+    if (lead) {
+        bv[gb] = x;
+        bi[gb] = xi;
     }
 }
 
-// pass 2: one CTA per job, the pairwise tree over its block results (padded
-// with the identity) -- with pass 1 the same tree as the multi-pass fold --
-// then the combination with the initial value
-__global__ void __launch_bounds__(FOLD_THREADS) kFoldSegFinal(const FoldJob *jobs, const double *bv, const long *bi) {
-    __shared__ double sv[FOLD_SPAN];
-    __shared__ long si[FOLD_SPAN];
+__global__ void __launch_bounds__(FOLD2_THREADS) kFoldSegFinal(const FoldJob *jobs, const double *bv, const long *bi) {
     const FoldJob &J = jobs[blockIdx.x];
-    const int op = J.op;
-    const bool loc = (op == rf_MINLOC || op == rf_MAXLOC);
-    const double ident = identityOf<double>(op);
-    const long nblk = (J.count + FOLD_SPAN - 1) / FOLD_SPAN;
-    for (int h = 0; h < 2; h++) {
-        const int q = h * FOLD_THREADS + threadIdx.x;
-        sv[q] = q < nblk ? bv[J.blockBase + q] : ident;
-        si[q] = q < nblk ? bi[J.blockBase + q] : -1;
-    }
-    __syncthreads();
-    foldSpan(op, loc, sv, si);
-    if (threadIdx.x == 0) {
-        double *dst = (double *)J.dst;
-        double init = dst[0];
-        double r = (op == rf_SUM) ? 0.0 : (op == rf_PROD ? 1.0 : init);
-        long ri = si[0];
-        bool fromLoop = false;
-        if (loc) {
-            if (ri >= 0) fromLoop = combine<double>(op, r, sv[0]);
-        } else {
-            combine<double>(op, r, sv[0]);
-            combine<double>(op, r, init);
-        }
-        dst[0] = r;
-        if (loc && fromLoop && J.dstLoc && J.locItems)
-            for (long b = 0; b < J.locSize; b++) ((char *)J.dstLoc)[b] = ((const char *)J.locItems)[ri * J.locSize + b];
+    const long nblk = (J.count + FOLD2_SPAN - 1) / FOLD2_SPAN;
+    double x;
+    long xi;
+    if (J.op == rf_MINLOC || J.op == rf_MAXLOC) {
+        if (span2<double, false, true>(J.op, nblk, bv + J.blockBase, bi + J.blockBase, 0, x, xi))
+            finish2<double, false, true>(J.op, x, xi, (double *)J.dst, (const char *)J.locItems, J.locSize,
+                                         (char *)J.dstLoc);
+    } else {
+        if (span2<double, false, false>(J.op, nblk, bv + J.blockBase, nullptr, 0, x, xi))
+            finish2<double, false, false>(J.op, x, xi, (double *)J.dst, nullptr, 0, nullptr);
     }
 }
 
 bool foldBatchable(int op, int vtype, long count, long elemCount) {
-    return vtype == rt_DOUBLE && elemCount == 1 && count <= (long)FOLD_SPAN * FOLD_SPAN &&
+    return vtype == rt_DOUBLE && elemCount == 1 && count <= (long)FOLD2_SPAN * FOLD2_SPAN &&
            (op == rf_SUM || op == rf_PROD || op == rf_MAX || op == rf_MIN || op == rf_MINLOC || op == rf_MAXLOC);
 }
 
@@ -830,10 +804,10 @@ void launchRedFoldBatch(const std::vector<FoldJob> &jobs, cudaStream_t s, std::v
     FoldJob *h = (FoldJob *)hostAlloc(bytes);
     hostScratch.push_back(h);
     memcpy(h, jobs.data(), bytes);
-    long blocks = 0;  // 1024-item blocks of all jobs
+    long blocks = 0;  // 2048-item spans of all jobs
     for (size_t q = 0; q < jobs.size(); q++) {
         h[q].blockBase = blocks;
-        blocks += (h[q].count + FOLD_SPAN - 1) / FOLD_SPAN;
+        blocks += (h[q].count + FOLD2_SPAN - 1) / FOLD2_SPAN;
     }
     GB_INTERNAL(blocks < (1L << 31), "reduction batch too large");
     FoldJob *d = (FoldJob *)devAlloc(bytes);
@@ -843,8 +817,8 @@ void launchRedFoldBatch(const std::vector<FoldJob> &jobs, cudaStream_t s, std::v
     devScratch.push_back(bv);
     devScratch.push_back(bi);
     GB_CUDA(cudaMemcpyAsync(d, h, bytes, cudaMemcpyHostToDevice, s));
-    if (blocks > 0) kFoldSegBlocks<<<(unsigned)blocks, FOLD_THREADS, 0, s>>>(d, (int)jobs.size(), bv, bi);
-    kFoldSegFinal<<<(unsigned)jobs.size(), FOLD_THREADS, 0, s>>>(d, bv, bi);
+    if (blocks > 0) kFoldSegBlocks<<<(unsigned)blocks, FOLD2_THREADS, 0, s>>>(d, (int)jobs.size(), bv, bi);
+    kFoldSegFinal<<<(unsigned)jobs.size(), FOLD2_THREADS, 0, s>>>(d, bv, bi);
     dvmhgb_count_launches(2);
     GB_CUDA(cudaGetLastError());
 }
