@@ -76,10 +76,44 @@ void loop_genred_host(DvmType *pLoopRef, DvmType X_hdr[], DvmType V_hdr[], doubl
     dvmh_loop_red_post_C(loop_ref, 8, &dml, &lc);
 }
 
+/* Deterministic edge-value inputs (the reductions' order-sensitive cases):
+ *   0: +0, -0, -0.5, a subnormal, -inf (MAX of the float conversions is a
+ *      signed zero: the first in loop order wins; MINLOC ties at -inf)
+ *   1: 0.25, NaN, +inf, -0, the smallest subnormal (SUM and PROD are NaN; NaN
+ *      never enters a MIN/MAX/MINLOC slot: its comparisons are false)
+ *   2: every value 0.5 and every int 7 (MINLOC: the first in loop order)
+ * V: a multiplicative hash of the index over the whole int range. */
+int wl_genred_pattern(int pattern, long n, double *x, int *v) {
+    static const double p0[5] = {0.0, -0.0, -0.5, -1e-310, -__builtin_inf()};
+    static const double p1[5] = {0.25, __builtin_nan(""), __builtin_inf(), -0.0, 4.9406564584124654e-324};
+    long i;
+    for (i = 0; i < n; i++) {
+        uint64_t h = (uint64_t)(i + 1) * 0x9E3779B97F4A7C15ull;
+        int k = (int)((h >> 40) % 5);
+        x[i] = pattern == 0 ? p0[k] : pattern == 1 ? p1[k] : 0.5;
+        v[i] = pattern == 2 ? 7 : (int)(uint32_t)(h >> 32);
+    }
+    return 0;
+}
+
+static int genred(long n, long start, long end, long step, uint64_t seed, const double *xin, const int *vin, int bx,
+                  double *d3, int *i4, float *f1, long *lc);
+
 /* red: the eight reduction variables' initial values in, results out:
  * ds, dp, dml (double[3]), imn, ia, io, ix (int[4]), fmx (float[1]), lc (long[1]). */
 int wl_genred_run(long n, long start, long end, long step, uint64_t seed, int bx, double *d3, int *i4, float *f1,
                   long *lc) {
+    return genred(n, start, end, step, seed, 0, 0, bx, d3, i4, f1, lc);
+}
+
+/* the same program on given X (n doubles) and V (n ints) */
+int wl_genred_run_data(long n, long start, long end, long step, const double *x, const int *v, int bx, double *d3,
+                       int *i4, float *f1, long *lc) {
+    return genred(n, start, end, step, 0, x, v, bx, d3, i4, f1, lc);
+}
+
+static int genred(long n, long start, long end, long step, uint64_t seed, const double *xin, const int *vin, int bx,
+                  double *d3, int *i4, float *f1, long *lc) {
     static double ds, dp, dml;
     static int imn, ia, io, ix;
     static float fmx;
@@ -99,8 +133,8 @@ int wl_genred_run(long n, long start, long end, long step, uint64_t seed, int bx
     x = (double *)dvmh_get_natural_base_C(0, X);
     v = (int *)dvmh_get_natural_base_C(0, V);
     for (i = 0; i < n; i++) {
-        x[i] = wl_u01(seed, 11, (uint64_t)i);
-        v[i] = (int)(wl_u01(seed, 12, (uint64_t)i) * 2147483647.0) - 1073741824;
+        x[i] = xin ? xin[i] : wl_u01(seed, 11, (uint64_t)i);
+        v[i] = vin ? vin[i] : (int)(wl_u01(seed, 12, (uint64_t)i) * 2147483647.0) - 1073741824;
     }
     dvmh_actual_array2_(X);
     dvmh_actual_array2_(V);

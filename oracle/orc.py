@@ -50,6 +50,10 @@ def lib():
         L.orc_rec2d_sweep.restype = ctypes.c_double
         L.orc_rec2d_sweep.argtypes = [ctypes.c_long, ctypes.c_long, _dp]
         L.orc_gen3d.argtypes = [ctypes.c_long] * 3 + [ctypes.c_uint64, _dp, _dp, ctypes.POINTER(ctypes.c_long), _dp]
+        _ip = ctypes.POINTER(ctypes.c_int)
+        L.orc_genred_data.argtypes = [ctypes.c_long] * 4 + [_dp, _ip, _dp, _ip, ctypes.POINTER(ctypes.c_float),
+                                                            ctypes.POINTER(ctypes.c_long)]
+        L.orc_genred_pattern.argtypes = [ctypes.c_int, ctypes.c_long, _dp, _ip]
         _fp = ctypes.POINTER(ctypes.c_float)
         L.orc_jacperf.restype = ctypes.c_long
         L.orc_jacperf.argtypes = [ctypes.c_int, ctypes.c_long, ctypes.c_long, _fp, _fp, _fp]
@@ -161,6 +165,25 @@ def jacperf_run(rank, L, itmax):
     B = np.zeros(L ** rank, dtype=np.float32)
     its = lib().orc_jacperf(rank, L, itmax, eps.ctypes.data_as(fp), A.ctypes.data_as(fp), B.ctypes.data_as(fp))
     return its, eps[:its], A, B
+
+
+def genred_pattern(pattern, n):
+    x = np.zeros(n)
+    v = np.zeros(n, dtype=np.int32)
+    lib().orc_genred_pattern(pattern, n, P(x), v.ctypes.data_as(ctypes.POINTER(ctypes.c_int)))
+    return x, v
+
+
+def genred_run_data(n, start, end, step, x, v, init):
+    """genred_run on given inputs x (float64) and v (int32)"""
+    d3 = np.array(init[0:3], dtype=np.float64)
+    i4 = (ctypes.c_int * 4)(*[int(q) for q in init[3:7]])
+    f1 = (ctypes.c_float * 1)(init[7])
+    lc = (ctypes.c_long * 1)(int(init[8]))
+    v = np.ascontiguousarray(v, dtype=np.int32)
+    lib().orc_genred_data(n, start, end, step, P(np.ascontiguousarray(x, dtype=np.float64)),
+                          v.ctypes.data_as(ctypes.POINTER(ctypes.c_int)), P(d3), i4, f1, lc)
+    return (float(d3[0]), float(d3[1]), float(d3[2]), i4[0], i4[1], i4[2], i4[3], f1[0], lc[0])
 
 
 def genred_run(n, start, end, step, seed, init):

@@ -12,6 +12,8 @@
  *                   locs[count][2] (int32), then the final arrays in order
  *   genred       n start end step seed ds dp dml imn ia io ix fmx lc   (initial values)
  *                -> ds dp dml (f64), imn ia io ix (int32), fmx (f32), lc (int64)
+ *   genredx      n start end step pattern ds dp dml imn ia io ix fmx lc
+ *                -> as genred, on the inputs of wl_genred_pattern(pattern)
  *   gen3d        n0 n1 n2 seed s mx lc  -> s, mx (f64), lc (int64), B[n0*n1*n2]
  *   jacperf      rank L itmax full      -> iterations run (int64), eps[itmax] (f32, 0 past
  *                                          the last), then A, B (f32, L^rank) when full
@@ -44,6 +46,9 @@ int wl_heat_run(long steps, double *sums_out, double *mins_out, int *locs_out);
 int wl_heat_fetch(long k, double *u_out);
 int wl_genred_run(long n, long start, long end, long step, uint64_t seed, int bx, double *d3, int *i4, float *f1,
                   long *lc);
+int wl_genred_pattern(int pattern, long n, double *x, int *v);
+int wl_genred_run_data(long n, long start, long end, long step, const double *x, const int *v, int bx, double *d3,
+                       int *i4, float *f1, long *lc);
 int wl_gen3d_run(long n0, long n1, long n2, uint64_t seed, int bx, int by, int bz, double *s, double *mx, long *lc,
                  double *b_out);
 long wl_jacperf_run(int rank, long L, long itmax, float *eps_out, float *a_out, float *b_out);
@@ -137,15 +142,24 @@ int main(int argc, char **argv) {
             put(f, u, sizeof(double) * sides[k] * sides[k]);
             free(u);
         }
-    } else if (!strcmp(argv[1], "genred")) {
+    } else if (!strcmp(argv[1], "genred") || !strcmp(argv[1], "genredx")) {
         long n = atol(argv[3]), start = atol(argv[4]), end = atol(argv[5]), step = atol(argv[6]);
         uint64_t seed = strtoull(argv[7], 0, 10);
+        double *xs = 0;
+        int *vs = 0;
         double d3[3] = {atof(argv[8]), atof(argv[9]), atof(argv[10])};
         int i4[4] = {atoi(argv[11]), (int)strtol(argv[12], 0, 0), (int)strtol(argv[13], 0, 0),
                      (int)strtol(argv[14], 0, 0)};
         float f1[1] = {(float)atof(argv[15])};
         long lc[1] = {atol(argv[16])};
-        wl_genred_run(n, start, end, step, seed, 0, d3, i4, f1, lc);
+        if (!strcmp(argv[1], "genredx")) {
+            xs = malloc(sizeof(double) * n);
+            vs = malloc(sizeof(int) * n);
+            wl_genred_pattern((int)seed, n, xs, vs);
+            wl_genred_run_data(n, start, end, step, xs, vs, 0, d3, i4, f1, lc);
+        } else {
+            wl_genred_run(n, start, end, step, seed, 0, d3, i4, f1, lc);
+        }
         put(f, d3, sizeof(d3));
         put(f, i4, sizeof(i4));
         put(f, f1, sizeof(f1));

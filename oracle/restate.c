@@ -452,7 +452,34 @@ long orc_jacperf(int rank, long L, long itmax, float *eps_out, float *A, float *
  * d3 = {ds, dp, dml}, i4 = {imn, ia, io, ix}, f1 = {fmx}, lc: initial values
  * in, results out.
  */
+static void genred_loop(long n, long start, long end, long step, const double *xs, const int *vs, uint64_t seed,
+                        double *d3, int *i4, float *f1, long *lc);
+
 void orc_genred(long n, long start, long end, long step, uint64_t seed, double *d3, int *i4, float *f1, long *lc) {
+    genred_loop(n, start, end, step, 0, 0, seed, d3, i4, f1, lc);
+}
+
+/* the same loop on given inputs */
+void orc_genred_data(long n, long start, long end, long step, const double *x, const int *v, double *d3, int *i4,
+                     float *f1, long *lc) {
+    genred_loop(n, start, end, step, x, v, 0, d3, i4, f1, lc);
+}
+
+/* the program's edge-value inputs (workloads/genred.c wl_genred_pattern): a
+ * multiplicative hash of i + 1 picks one of five values; V is its high half */
+void orc_genred_pattern(int pattern, long n, double *x, int *v) {
+    const double p0[5] = {0.0, -0.0, -0.5, -1e-310, -INFINITY};
+    const double p1[5] = {0.25, NAN, INFINITY, -0.0, 4.9406564584124654e-324};
+    for (long i = 0; i < n; i++) {
+        const uint64_t h = (uint64_t)(i + 1) * 0x9E3779B97F4A7C15ull;
+        const int k = (int)((h >> 40) % 5);
+        x[i] = pattern == 0 ? p0[k] : pattern == 1 ? p1[k] : 0.5;
+        v[i] = pattern == 2 ? 7 : (int)(uint32_t)(h >> 32);
+    }
+}
+
+static void genred_loop(long n, long start, long end, long step, const double *xs, const int *vs, uint64_t seed,
+                        double *d3, int *i4, float *f1, long *lc) {
     double ds = 0.0, dp = 1.0, dml = d3[2];
     int imn = i4[0], ia = i4[1], io = i4[2], ix = 0;
     float fmx = f1[0];
@@ -460,8 +487,8 @@ void orc_genred(long n, long start, long end, long step, uint64_t seed, double *
     if (step != 0)
         for (long i = start; step > 0 ? i <= end : i >= end; i += step) {
             if (i < 0 || i >= n) break;
-            double x = orc_u01(seed, 11, (uint64_t)i);
-            int v = (int)(orc_u01(seed, 12, (uint64_t)i) * 2147483647.0) - 1073741824;
+            double x = xs ? xs[i] : orc_u01(seed, 11, (uint64_t)i);
+            int v = vs ? vs[i] : (int)(orc_u01(seed, 12, (uint64_t)i) * 2147483647.0) - 1073741824;
             ds = ds + x;
             dp = dp * (1.0 + x / 65536.0);
             imn = v < imn ? v : imn;

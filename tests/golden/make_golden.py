@@ -47,6 +47,13 @@ CASES = [
     ("genred_empty", "genred", [100, 50, 10, 1, 117, 0.125, 1.5, 0.75, 123, -1, 256, 1515870810, -2.0, -9], True),
     ("genred_n777_sm1", "genred", [777, 776, 0, -1, 794, 0.125, 1.5, 0.75, 123, -1, 256, 1515870810, -2.0, -9], True),
     ("genred_n777_keep", "genred", [777, 0, 776, 3, 795, -3.5, 0.25, 0.0, -2147483648, 0, -1, 0, 2.0, 41], True),
+    # genredx: genred on the edge-value patterns of wl_genred_pattern (the fifth parameter)
+    ("genredx_p0_n5000", "genredx", [5000, 0, 4999, 1, 0, 0.125, 1.5, 0.75, 123, -1, 256, 1515870810, -2.0, -9], True),
+    ("genredx_p0_n3001_sm3", "genredx", [3001, 3000, 0, -3, 0, 0.0, -1.0, 1.0, 0, -1, 0, 0, -1.0, 5], True),
+    ("genredx_p1_n4097", "genredx", [4097, 0, 4096, 1, 1, 0.125, 1.5, 0.75, 123, -1, 256, 1515870810, -2.0, -9], True),
+    ("genredx_p2_n70000", "genredx", [70000, 1, 69998, 2, 2, 0.125, 1.5, 0.75, 123, -1, 256, 1515870810, -2.0, -9],
+     True),
+    ("genredx_p2_n9000_sm1", "genredx", [9000, 8999, 0, -1, 2, 0.0, 1.0, 0.5, 7, -1, 0, 0, 0.5, 3], True),
     # jacperf: rank L itmax (the reference's FP32 benchmarks; the last two are their
     # full configurations, whose final eps the examples verify)
     ("jacperf3_L12_it5", "jacperf", [3, 12, 5], True),
@@ -128,7 +135,7 @@ def case(name, prog, params, full):
         rec["A_sha256"] = sha(A)
         if full:
             rec["A"] = hx(A)
-    elif prog == "genred":
+    elif prog in ("genred", "genredx"):
         rec["d3"] = hx(np.frombuffer(raw[0:24], dtype="<f8"))
         rec["i4"] = [int(x) for x in np.frombuffer(raw[24:40], dtype="<i4")]
         rec["f1"] = hx(np.frombuffer(raw[40:44], dtype="<f4"))

@@ -136,3 +136,44 @@ def test_reference_golden(g, golden, mode):
         assert list(i4) == c["i4"], name
         assert float(f1[0]).hex() == c["f1"][0], name
         assert lc[0] == c["lc"], name
+
+
+@pytest.mark.parametrize("mode", ["plain", "batched"])
+def test_edge_values_reference_golden(g, golden, mode):
+    """Signed zeros, subnormals, infinities, NaN and ties (wl_genred_pattern),
+    against the reference runtime's results: MAX of signed zeros and MINLOC
+    ties go to the first in loop order (the fold keeps the lower slot on ties,
+    slots follow loop order), MIN / AND / OR / XOR exact; SUM and PROD exact
+    where the reference's value is NaN or infinite, else within the error bound."""
+    g.set_mode(mode)
+    w = g.workloads()
+    D, I, F, Lp = (ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_float),
+                   ctypes.POINTER(ctypes.c_long))
+    w.wl_genred_pattern.argtypes = [ctypes.c_int, ctypes.c_long, D, I]
+    w.wl_genred_run_data.argtypes = [ctypes.c_long] * 4 + [D, I, ctypes.c_int, D, I, F, Lp]
+    cases = [(k, c) for k, c in golden.items() if c["prog"] == "genredx"]
+    assert len(cases) >= 5
+    u = 2.0 ** -53
+    for name, c in cases:
+        n, start, end, step, pattern = c["params"][:5]
+        init = c["params"][5:]
+        x = np.zeros(n)
+        v = np.zeros(n, dtype=np.int32)
+        assert w.wl_genred_pattern(pattern, n, x.ctypes.data_as(D), v.ctypes.data_as(I)) == 0
+        d3 = (ctypes.c_double * 3)(*init[0:3])
+        i4 = (ctypes.c_int * 4)(*init[3:7])
+        f1 = (ctypes.c_float * 1)(init[7])
+        lc = (ctypes.c_long * 1)(init[8])
+        assert w.wl_genred_run_data(n, start, end, step, x.ctypes.data_as(D), v.ctypes.data_as(I), 0, d3, i4, f1,
+                                    lc) == 0
+        cnt = max(0, (end - start) // step + 1)
+        for k, bound in ((0, lambda ref: cnt * u * (cnt * 0.5 + abs(init[0]))), (1, lambda ref: 2 * cnt * u * abs(ref))):
+            ref = float.fromhex(c["d3"][k])
+            if ref != ref or ref in (float("inf"), float("-inf")):
+                assert float(d3[k]).hex() == c["d3"][k], (name, k)
+            else:
+                assert abs(d3[k] - ref) <= bound(ref), (name, k, d3[k], ref)
+        assert float(d3[2]).hex() == c["d3"][2], name
+        assert list(i4) == c["i4"], name
+        assert float(f1[0]).hex() == c["f1"][0], name
+        assert lc[0] == c["lc"], name

@@ -24,8 +24,8 @@ def jac_cases(golden):
 
 def test_golden_present(golden):
     progs = {v["prog"] for v in golden.values()}
-    assert progs == {"jac2d", "jac3d", "sor3d", "heat", "gsd2d", "genred", "rec2d", "gsd3d", "gs2d", "gen3d",
-                     "jacperf"}
+    assert progs == {"jac2d", "jac3d", "sor3d", "heat", "gsd2d", "genred", "genredx", "rec2d", "gsd3d", "gs2d",
+                     "gen3d", "jacperf"}
 
 
 # the reference examples' own verification (examples/Performance/jac3d_perf.c:92, jac2d_perf.c:89)
@@ -163,6 +163,22 @@ def test_genred_vs_reference(golden):
         n, start, end, step, seed = c["params"][:5]
         r = orc.genred_run(n, start, end, step, seed, c["params"][5:])
         assert [float(x).hex() for x in r[0:3]] == c["d3"], name
+        assert list(r[3:7]) == c["i4"], name
+        assert float(r[7]).hex() == c["f1"][0], name
+        assert r[8] == c["lc"], name
+
+
+def test_genred_edge_values_vs_reference(golden):
+    """Signed zeros, subnormals, infinities, NaN and ties (wl_genred_pattern):
+    MAX of signed zeros and MINLOC ties go to the first in loop order, NaN
+    propagates through SUM and PROD and never wins a comparison."""
+    cases = [(k, c) for k, c in golden.items() if c["prog"] == "genredx"]
+    assert len(cases) >= 5
+    for name, c in cases:
+        n, start, end, step, pattern = c["params"][:5]
+        x, v = orc.genred_pattern(pattern, n)
+        r = orc.genred_run_data(n, start, end, step, x, v, c["params"][5:])
+        assert [float(q).hex() for q in r[0:3]] == c["d3"], name
         assert list(r[3:7]) == c["i4"], name
         assert float(r[7]).hex() == c["f1"][0], name
         assert r[8] == c["lc"], name
