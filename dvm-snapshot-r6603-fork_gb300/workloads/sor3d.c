@@ -30,7 +30,16 @@ static wl_sor_params P;
 
 #ifndef WL_NO_CUDA
 void loop_sor3d_cuda(DvmType *pLoopRef, DvmType A_hdr[], double *s_ptr, double *w_ptr);
+void loop_sor3d_gen_cuda(DvmType *pLoopRef, DvmType A_hdr[], double *s_ptr, double *w_ptr);
 #endif
+static int useGenerated;
+
+/* the CUDA handler the loop registers: 0 = sor3d_cuda.cu (the library's
+ * wavefront kernel), 1 = sor3d_gen_cuda.cu (cdvmh's generated hyperplane shape) */
+int wl_sor3d_use_generated(int on) {
+    useGenerated = on;
+    return 0;
+}
 
 void loop_sor3d_host(DvmType *pLoopRef, DvmType A_hdr[], double *s_ptr, double *w_ptr) {
     DvmType loop_ref = *pLoopRef;
@@ -99,7 +108,9 @@ double wl_sor3d_step(void) {
                                  dvmh_handler_func_C((DvmHandlerFunc)loop_sor3d_host, 3, A, &s, &w));
 #ifndef WL_NO_CUDA
     dvmh_loop_register_handler_C(cur_loop, DEVICE_TYPE_CUDA, 0,
-                                 dvmh_handler_func_C((DvmHandlerFunc)loop_sor3d_cuda, 3, A, &s, &w));
+                                 dvmh_handler_func_C((DvmHandlerFunc)(useGenerated ? loop_sor3d_gen_cuda
+                                                                                   : loop_sor3d_cuda),
+                                                     3, A, &s, &w));
 #endif
     dvmh_loop_perform_C(cur_loop);
     dvmh_region_end_C(cur_region);

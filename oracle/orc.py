@@ -31,6 +31,7 @@ def lib():
         L.orc_sor_init.argtypes = [ctypes.c_long, ctypes.c_uint64, _dp]
         L.orc_sor_sweep.restype = ctypes.c_double
         L.orc_sor_sweep.argtypes = [ctypes.c_long, ctypes.c_double, _dp, _dp]
+        L.orc_sor_sweep_cols.argtypes = [ctypes.c_long, ctypes.c_double, _dp, _dp]
         L.orc_heat_side.restype = ctypes.c_long
         L.orc_heat_side.argtypes = [ctypes.c_uint64, ctypes.c_long, ctypes.c_long, ctypes.c_long]
         L.orc_heat_init.argtypes = [ctypes.c_long, ctypes.c_uint64, ctypes.c_long, _dp, _dp]
@@ -90,6 +91,32 @@ def sor_run(n, sweeps, omega, seed):
         seq.append(lib().orc_sor_sweep(n, omega, P(A), ctypes.byref(c)))
         can.append(c.value)
     return np.array(seq), np.array(can), A
+
+
+def pairwise(v, op=np.add, ident=-0.0):
+    """the pairwise tree over slot indices, identity padding to a power of two"""
+    v = np.asarray(v, dtype=np.float64)
+    m = 1
+    while m < len(v):
+        m *= 2
+    v = np.concatenate([v, np.full(m - len(v), ident)])
+    while len(v) > 1:
+        v = op(v[0::2], v[1::2])
+    return float(v[0])
+
+
+def sor_run_columns(n, sweeps, omega, seed):
+    """SOR sweeps whose SUM is folded as the hyperplane handler folds it: per
+    (i, j) column in k order, then the pairwise tree over the columns, then
+    (0 + fold) + 0.  Returns (sums, A)."""
+    A = np.zeros(n ** 3)
+    lib().orc_sor_init(n, seed, P(A))
+    cols = np.zeros((n - 2) ** 2)
+    out = []
+    for _ in range(sweeps):
+        lib().orc_sor_sweep_cols(n, omega, P(A), P(cols))
+        out.append((0.0 + pairwise(cols)) + 0.0)
+    return np.array(out), A
 
 
 def heat_sides(count, lo, hi, seed):

@@ -227,6 +227,27 @@ double orc_sor_sweep(long n, double w, double *A, double *s_canon) {
     return (0.0 + s) + 0.0;
 }
 
+/* One sweep with the residual terms summed per (i, j) column in k order, the
+ * partial sums the hyperplane handler (workloads/sor3d_gen_cuda.cu) keeps in
+ * its reduction slots: cols[(i-1)*(n-2) + (j-1)], starting from the identity
+ * -0.0.  The array is the sequential sweep's. */
+void orc_sor_sweep_cols(long n, double w, double *A, double *cols) {
+    const long nn = n * n, m = n - 2;
+    for (long i = 1; i <= n - 2; i++)
+        for (long j = 1; j <= n - 2; j++) {
+            double cs = -0.0;
+            for (long k = 1; k <= n - 2; k++) {
+                const long c = (i * n + j) * n + k;
+                const double old = A[c];
+                const double nv = (1.0 - w) * old + w / 6.0 * (A[c - nn] + A[c + nn] + A[c - n] + A[c + n] +
+                                                               A[c - 1] + A[c + 1]);
+                A[c] = nv;
+                cs = cs + (nv - old) * (nv - old);
+            }
+            cols[(i - 1) * m + (j - 1)] = cs;
+        }
+}
+
 /* ------------------------------------------------------------ batched heat */
 
 long orc_heat_side(uint64_t seed, long k, long lo, long hi) {

@@ -58,6 +58,44 @@ def test_sor_golden(g, golden, mode, variant):
         assert close_sum(res, unhex(c["s"]), (n - 2) ** 3), name
 
 
+@pytest.mark.parametrize("tfm", [1, 0])
+@pytest.mark.parametrize("mode", MODES)
+def test_sor_generated_hyperplane_handler(g, golden, mode, tfm):
+    """The same program through cdvmh's generated shape for three dependences
+    (workloads/sor3d_gen_cuda.cu: one launch per hyperplane, a SUM slot per
+    column prepared with fill = 1 and accumulated across the launches), with
+    the runtime's transformed layout (the plane of the two fastest dependent
+    axes diagonalised) or natural: the array bit for bit against the
+    reference's goldens, the SUM bit for bit against the column-wise
+    restatement and within the error bound of the reference's value."""
+    import ctypes
+    g.set_mode(mode)
+    rt, w = g.runtime(), g.workloads()
+    rt.dvmhgb_set_autotransform(tfm)
+    w.wl_sor3d_use_generated.argtypes = [ctypes.c_int]
+    w.wl_sor3d_use_generated(1)
+    try:
+        for name, c in golden.items():
+            if c["prog"] != "sor3d":
+                continue
+            n, sw, omega, seed = c["params"]
+            g.reset_stats()
+            s = g.Sor(n, omega, seed)
+            res = s.run(sw)
+            A = s.fetch()
+            s.close()
+            st = g.stats()
+            assert sha(A) == c["A_sha256"], (name, mode, tfm)
+            cols, A_ref = orc.sor_run_columns(n, sw, omega, seed)
+            assert np.array_equal(res, cols), (name, mode, tfm, res, cols)
+            assert close_sum(res, unhex(c["s"]), (n - 2) ** 3), name
+            if not tfm:
+                assert st["relayouts"] == 0, st
+    finally:
+        w.wl_sor3d_use_generated(0)
+        rt.dvmhgb_set_autotransform(1)
+
+
 @pytest.mark.parametrize("variant", [0, 1, 2, 3])
 @pytest.mark.parametrize("n", [4, 9, 17, 66, 75, 131])
 def test_sor_sizes_vs_oracle(g, n, variant):

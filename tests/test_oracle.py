@@ -91,6 +91,20 @@ def test_sor_vs_reference(golden):
         assert np.allclose(can, seq, rtol=1e-12, atol=0), name
 
 
+def test_sor_columns_restatement(golden):
+    """The column-wise SUM restatement (the hyperplane handler's slots) sweeps
+    the same array as the reference and sums within its error bound."""
+    u = 2.0 ** -53
+    for name, c in golden.items():
+        if c["prog"] != "sor3d":
+            continue
+        n, sw, omega, seed = c["params"]
+        cols, A = orc.sor_run_columns(n, sw, omega, seed)
+        assert sha(A) == c["A_sha256"], name
+        ref = unhex(c["s"])
+        assert np.all(np.abs(cols - ref) <= 2 * (n - 2) ** 3 * u * ref), name
+
+
 def test_heat_vs_reference(golden):
     for name, c in golden.items():
         if c["prog"] != "heat":
