@@ -461,6 +461,32 @@ def extra_configs(g, stream):
         ms = e0.elapsed_time(e1) / sweeps
         s.close()
         res[mode] = {"value": (n - 2) ** 3 / (ms * 1e-3), "ms_per_sweep": ms}
+    # the same program through cdvmh's generated hyperplane handler (one launch per
+    # hyperplane, 3n - 8 per sweep): the reference's own GPU execution shape
+    import ctypes
+    w = g.workloads()
+    w.wl_sor3d_use_generated.argtypes = [ctypes.c_int]
+    w.wl_sor3d_use_generated(1)
+    try:
+        for mode in ("batched", "plain"):
+            g.set_mode(mode)
+            s = g.Sor(n, 1.5, SEED + 2)
+            s.run(2)
+            g.sync()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            k = 5
+            e0.record(stream)
+            s.run(k)
+            e1.record(stream)
+            g.sync()
+            torch.cuda.synchronize()
+            ms = e0.elapsed_time(e1) / k
+            s.close()
+            res["generated_hyperplane_" + mode] = {"value": (n - 2) ** 3 / (ms * 1e-3), "ms_per_sweep": ms,
+                                                   "launches_per_sweep": 3 * (n - 2) - 2}
+    finally:
+        w.wl_sor3d_use_generated(0)
+        g.set_mode("batched")
     peak, _ = peaks()
     for r in res.values():
         r["hbm_frac"] = r["value"] * 16 / 1e9 / peak
