@@ -517,6 +517,7 @@ def extra_configs(g, stream):
     out["heat_batched_256"] = {"unit": "cell-updates/s", "bytes_per_cell": 16, "cells": cells, **res}
     g.set_mode("batched")
     out["gsd2d_layouts_2048"] = gsd2d_layouts(g, stream, 2048, 2)
+    out["jacobi3d_512_generated_handlers"] = jacobi3d_generated(g, stream, 512, 20)
     out["jacobi2d_1024"] = jacobi2d(g, stream, 1024, 100)
     out["jacperf3d_fp32_384"] = jacperf(g, 3, 384, 5.058044, 1e-4)
     out["jacperf2d_fp32_8000"] = jacperf(g, 2, 8000, 58.37598, 1e-3)
@@ -565,6 +566,38 @@ def jacperf(g, rank, L, answer, tol):
     res["cpu_port"] = {"ms_per_iteration": 1e3 * (t10 - t1) / 9, "cores": L_.orc_max_threads()}
     res["cpu_port"]["value"] = (L - 2) ** rank / (res["cpu_port"]["ms_per_iteration"] * 1e-3)
     return {"unit": "cell-updates/s", "bytes_per_cell": 20, "dtype": "f32", "reference_check": [answer, tol], **res}
+
+
+def jacobi3d_generated(g, stream, n, steps):
+    """The headline program through cdvmh's generated one-point-per-thread
+    handlers (the reference's GPU kernel shape: one MAX slot per launched
+    thread, default 32 x 4 x 2 blocks) on this runtime, beside the library's
+    kernels in the headline line."""
+    import ctypes
+    import torch
+    w = g.workloads()
+    w.wl_jac3d_use_generated.argtypes = [ctypes.c_int]
+    w.wl_jac3d_use_generated(1)
+    res = {}
+    try:
+        for mode in ("batched", "plain"):
+            g.set_mode(mode)
+            j = g.Jacobi(3, n, SEED)
+            j.run(3)
+            g.sync()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            j.run(steps)
+            e1.record(stream)
+            g.sync()
+            torch.cuda.synchronize()
+            ms = e0.elapsed_time(e1) / steps
+            j.close()
+            res[mode] = {"ms_per_step": ms, "value": (n - 2) ** 3 / (ms * 1e-3)}
+    finally:
+        w.wl_jac3d_use_generated(0)
+        g.set_mode("batched")
+    return {"unit": "cell-updates/s", "bytes_per_cell": 32, **res}
 
 
 def jacobi2d(g, stream, n, iters):

@@ -40,7 +40,17 @@ static wl_jacobi_params P;
 #ifndef WL_NO_CUDA
 void loop_jac3d_upd_cuda(DvmType *pLoopRef, DvmType A_hdr[], DvmType B_hdr[], double *eps_ptr);
 void loop_jac3d_stn_cuda(DvmType *pLoopRef, DvmType A_hdr[], DvmType B_hdr[]);
+void loop_jac3d_upd_gen_cuda(DvmType *pLoopRef, DvmType A_hdr[], DvmType B_hdr[], double *eps_ptr);
+void loop_jac3d_stn_gen_cuda(DvmType *pLoopRef, DvmType A_hdr[], DvmType B_hdr[]);
 #endif
+static int useGenerated;
+
+/* the CUDA handlers the loops register: 0 = jac3d_cuda.cu (the library's
+ * kernels), 1 = cdvmh's generated one-point-per-thread shape (jacperf_cuda.cu) */
+int wl_jac3d_use_generated(int on) {
+    useGenerated = on;
+    return 0;
+}
 
 /* ---------------------------------------------------------------- host handlers */
 
@@ -147,7 +157,9 @@ double wl_jac3d_step(void) {
                                  dvmh_handler_func_C((DvmHandlerFunc)loop_jac3d_upd_host, 3, A, B, &eps));
 #ifndef WL_NO_CUDA
     dvmh_loop_register_handler_C(cur_loop, DEVICE_TYPE_CUDA, 0,
-                                 dvmh_handler_func_C((DvmHandlerFunc)loop_jac3d_upd_cuda, 3, A, B, &eps));
+                                 dvmh_handler_func_C((DvmHandlerFunc)(useGenerated ? loop_jac3d_upd_gen_cuda
+                                                                                   : loop_jac3d_upd_cuda),
+                                                     3, A, B, &eps));
 #endif
     dvmh_loop_perform_C(cur_loop);
 
@@ -160,7 +172,9 @@ double wl_jac3d_step(void) {
                                  dvmh_handler_func_C((DvmHandlerFunc)loop_jac3d_stn_host, 2, A, B));
 #ifndef WL_NO_CUDA
     dvmh_loop_register_handler_C(cur_loop, DEVICE_TYPE_CUDA, 0,
-                                 dvmh_handler_func_C((DvmHandlerFunc)loop_jac3d_stn_cuda, 2, A, B));
+                                 dvmh_handler_func_C((DvmHandlerFunc)(useGenerated ? loop_jac3d_stn_gen_cuda
+                                                                                   : loop_jac3d_stn_cuda),
+                                                     2, A, B));
 #endif
     dvmh_loop_perform_C(cur_loop);
     dvmh_region_end_C(cur_region);

@@ -1,5 +1,6 @@
-// CUDA handlers of jacperf.c (the reference's FP32 Jacobi benchmarks) in the
-// shape cdvmh generates for parallel loops (cdvmh/src/converter_main.cpp:
+// CUDA handlers of jacperf.c (the reference's FP32 Jacobi benchmarks), and
+// generated-shape handlers of jac3d.c's FP64 loops (wl_jac3d_use_generated),
+// in the shape cdvmh generates for parallel loops (cdvmh/src/converter_main.cpp:
 // 2132-2401 for the handler, :1861-2130 for the kernel), with no knowledge of
 // this runtime: natural bases and headers (dvmh_get_natural_base_C,
 // dvmh_fill_header_C), the index type from dvmh_loop_guess_index_type_C, the
@@ -60,15 +61,14 @@ __global__ void loop_jacperf_init_kernel(float *A, IndexT A_hdr1, IndexT A_hdr2,
     }
 }
 
-template <typename IndexT, int R>
-__global__ void loop_jacperf_upd_kernel(float *A, IndexT A_hdr1, IndexT A_hdr2, float *B, IndexT B_hdr1,
-                                        IndexT B_hdr2, Geo<IndexT, R> g, float eps, float eps_grid[],
-                                        IndexT blockOffset) {
+template <typename T, typename IndexT, int R>
+__global__ void loop_jacperf_upd_kernel(T *A, IndexT A_hdr1, IndexT A_hdr2, T *B, IndexT B_hdr1, IndexT B_hdr2,
+                                        Geo<IndexT, R> g, T eps, T eps_grid[], IndexT blockOffset) {
     IndexT x[R];
     if (pointOf<IndexT, R>((IndexT)blockIdx.x + blockOffset, g.lo, g.hi, g.blocksS, x)) {
         const IndexT qa = R == 3 ? x[0] * A_hdr1 + x[1] * A_hdr2 + x[R - 1] : x[0] * A_hdr1 + x[R - 1];
         const IndexT qb = R == 3 ? x[0] * B_hdr1 + x[1] * B_hdr2 + x[R - 1] : x[0] * B_hdr1 + x[R - 1];
-        float tmp = fabs(B[qb] - A[qa]);
+        T tmp = fabs(B[qb] - A[qa]);
         eps = Max(tmp, eps);
         A[qa] = B[qb];
     }
@@ -77,9 +77,9 @@ __global__ void loop_jacperf_upd_kernel(float *A, IndexT A_hdr1, IndexT A_hdr2, 
     eps_grid[slot] = eps;
 }
 
-template <typename IndexT, int R>
-__global__ void loop_jacperf_stn_kernel(float *A, IndexT A_hdr1, IndexT A_hdr2, float *B, IndexT B_hdr1,
-                                        IndexT B_hdr2, Geo<IndexT, R> g, IndexT blockOffset) {
+template <typename T, typename IndexT, int R>
+__global__ void loop_jacperf_stn_kernel(T *A, IndexT A_hdr1, IndexT A_hdr2, T *B, IndexT B_hdr1, IndexT B_hdr2,
+                                        Geo<IndexT, R> g, IndexT blockOffset) {
     IndexT x[R];
     if (!pointOf<IndexT, R>((IndexT)blockIdx.x + blockOffset, g.lo, g.hi, g.blocksS, x)) return;
     if (R == 3) {
@@ -88,12 +88,12 @@ __global__ void loop_jacperf_stn_kernel(float *A, IndexT A_hdr1, IndexT A_hdr2, 
             (A[(i - 1) * A_hdr1 + j * A_hdr2 + k] + A[i * A_hdr1 + (j - 1) * A_hdr2 + k] +
              A[i * A_hdr1 + j * A_hdr2 + (k - 1)] + A[i * A_hdr1 + j * A_hdr2 + (k + 1)] +
              A[i * A_hdr1 + (j + 1) * A_hdr2 + k] + A[(i + 1) * A_hdr1 + j * A_hdr2 + k]) /
-            6.0f;
+            (T)6;
     } else {
         const IndexT i = x[0], j = x[R - 1];
         B[i * B_hdr1 + j] = (A[(i - 1) * A_hdr1 + j] + A[i * A_hdr1 + (j - 1)] + A[i * A_hdr1 + (j + 1)] +
                              A[(i + 1) * A_hdr1 + j]) /
-                            4.0f;
+                            (T)4;
     }
 }
 
@@ -102,7 +102,7 @@ __global__ void loop_jacperf_stn_kernel(float *A, IndexT A_hdr1, IndexT A_hdr2, 
 // chunk of at most 65535 blocks.
 struct Prep {
     DvmType loop_ref, device_num;
-    float *A, *B;
+    void *A, *B;
     DvmType A_devHdr[8], B_devHdr[8];
     DvmType lo[3], hi[3], steps[3], blocksS[3];
     dim3 threads;
@@ -116,10 +116,10 @@ Prep prepare(DvmType *pLoopRef, DvmType A_hdr[], DvmType B_hdr[]) {
     DvmType tmpVar;
     p.loop_ref = *pLoopRef;
     p.device_num = dvmh_loop_get_device_num_C(p.loop_ref);
-    p.A = (float *)dvmh_get_natural_base_C(p.device_num, A_hdr);
+    p.A = dvmh_get_natural_base_C(p.device_num, A_hdr);
     tmpVar = dvmh_fill_header_C(p.device_num, p.A, A_hdr, p.A_devHdr, 0);
     assert(tmpVar == 0);
-    p.B = (float *)dvmh_get_natural_base_C(p.device_num, B_hdr);
+    p.B = dvmh_get_natural_base_C(p.device_num, B_hdr);
     tmpVar = dvmh_fill_header_C(p.device_num, p.B, B_hdr, p.B_devHdr, 0);
     assert(tmpVar == 0);
     (void)tmpVar;
@@ -167,43 +167,46 @@ void initHandler(DvmType *pLoopRef, DvmType A_hdr[], DvmType B_hdr[]) {
     chunks(p, [&](dim3 blocks, DvmType off) {
         if (p.indexT == rt_INT)
             loop_jacperf_init_kernel<int, R><<<blocks, p.threads, 0, p.stream>>>(
-                p.A, p.A_devHdr[1], p.A_devHdr[2], p.B, p.B_devHdr[1], p.B_devHdr[2], L, geo<int, R>(p), off);
+                (float *)p.A, p.A_devHdr[1], p.A_devHdr[2], (float *)p.B, p.B_devHdr[1], p.B_devHdr[2], L,
+                geo<int, R>(p), off);
         else
             loop_jacperf_init_kernel<long long, R><<<blocks, p.threads, 0, p.stream>>>(
-                p.A, p.A_devHdr[1], p.A_devHdr[2], p.B, p.B_devHdr[1], p.B_devHdr[2], L, geo<long long, R>(p), off);
+                (float *)p.A, p.A_devHdr[1], p.A_devHdr[2], (float *)p.B, p.B_devHdr[1], p.B_devHdr[2], L,
+                geo<long long, R>(p), off);
     });
 }
 
-template <int R>
+template <typename T, int R>
 void updHandler(DvmType *pLoopRef, DvmType A_hdr[], DvmType B_hdr[]) {
     Prep p = prepare<R>(pLoopRef, A_hdr, B_hdr);
-    float eps, *eps_grid;
+    T eps, *eps_grid;
     dvmh_loop_cuda_register_red_C(p.loop_ref, 1, (void **)&eps_grid, 0);
     dvmh_loop_red_init_C(p.loop_ref, 1, &eps, 0);
     dvmh_loop_cuda_red_prepare_C(p.loop_ref, 1, p.blocksS[0] * p.threads.x * p.threads.y * p.threads.z, 0);
     chunks(p, [&](dim3 blocks, DvmType off) {
         if (p.indexT == rt_INT)
-            loop_jacperf_upd_kernel<int, R><<<blocks, p.threads, 0, p.stream>>>(
-                p.A, p.A_devHdr[1], p.A_devHdr[2], p.B, p.B_devHdr[1], p.B_devHdr[2], geo<int, R>(p), eps, eps_grid,
-                off);
-        else
-            loop_jacperf_upd_kernel<long long, R><<<blocks, p.threads, 0, p.stream>>>(
-                p.A, p.A_devHdr[1], p.A_devHdr[2], p.B, p.B_devHdr[1], p.B_devHdr[2], geo<long long, R>(p), eps,
+            loop_jacperf_upd_kernel<T, int, R><<<blocks, p.threads, 0, p.stream>>>(
+                (T *)p.A, p.A_devHdr[1], p.A_devHdr[2], (T *)p.B, p.B_devHdr[1], p.B_devHdr[2], geo<int, R>(p), eps,
                 eps_grid, off);
+        else
+            loop_jacperf_upd_kernel<T, long long, R><<<blocks, p.threads, 0, p.stream>>>(
+                (T *)p.A, p.A_devHdr[1], p.A_devHdr[2], (T *)p.B, p.B_devHdr[1], p.B_devHdr[2], geo<long long, R>(p),
+                eps, eps_grid, off);
     });
     dvmh_loop_cuda_red_finish_C(p.loop_ref, 1);
 }
 
-template <int R>
+template <typename T, int R>
 void stnHandler(DvmType *pLoopRef, DvmType A_hdr[], DvmType B_hdr[]) {
     Prep p = prepare<R>(pLoopRef, A_hdr, B_hdr);
     chunks(p, [&](dim3 blocks, DvmType off) {
         if (p.indexT == rt_INT)
-            loop_jacperf_stn_kernel<int, R><<<blocks, p.threads, 0, p.stream>>>(
-                p.A, p.A_devHdr[1], p.A_devHdr[2], p.B, p.B_devHdr[1], p.B_devHdr[2], geo<int, R>(p), off);
+            loop_jacperf_stn_kernel<T, int, R><<<blocks, p.threads, 0, p.stream>>>(
+                (T *)p.A, p.A_devHdr[1], p.A_devHdr[2], (T *)p.B, p.B_devHdr[1], p.B_devHdr[2], geo<int, R>(p), off);
         else
-            loop_jacperf_stn_kernel<long long, R><<<blocks, p.threads, 0, p.stream>>>(
-                p.A, p.A_devHdr[1], p.A_devHdr[2], p.B, p.B_devHdr[1], p.B_devHdr[2], geo<long long, R>(p), off);
+            loop_jacperf_stn_kernel<T, long long, R><<<blocks, p.threads, 0, p.stream>>>(
+                (T *)p.A, p.A_devHdr[1], p.A_devHdr[2], (T *)p.B, p.B_devHdr[1], p.B_devHdr[2], geo<long long, R>(p),
+                off);
     });
 }
 
@@ -214,18 +217,28 @@ extern "C" void loop_jacperf2_init_cuda(DvmType *pLoopRef, DvmType A_hdr[], DvmT
 }
 extern "C" void loop_jacperf2_upd_cuda(DvmType *pLoopRef, DvmType A_hdr[], DvmType B_hdr[], float *eps_ptr) {
     (void)eps_ptr;
-    updHandler<2>(pLoopRef, A_hdr, B_hdr);
+    updHandler<float, 2>(pLoopRef, A_hdr, B_hdr);
 }
 extern "C" void loop_jacperf2_stn_cuda(DvmType *pLoopRef, DvmType A_hdr[], DvmType B_hdr[]) {
-    stnHandler<2>(pLoopRef, A_hdr, B_hdr);
+    stnHandler<float, 2>(pLoopRef, A_hdr, B_hdr);
 }
 extern "C" void loop_jacperf3_init_cuda(DvmType *pLoopRef, DvmType A_hdr[], DvmType B_hdr[]) {
     initHandler<3>(pLoopRef, A_hdr, B_hdr);
 }
 extern "C" void loop_jacperf3_upd_cuda(DvmType *pLoopRef, DvmType A_hdr[], DvmType B_hdr[], float *eps_ptr) {
     (void)eps_ptr;
-    updHandler<3>(pLoopRef, A_hdr, B_hdr);
+    updHandler<float, 3>(pLoopRef, A_hdr, B_hdr);
 }
 extern "C" void loop_jacperf3_stn_cuda(DvmType *pLoopRef, DvmType A_hdr[], DvmType B_hdr[]) {
-    stnHandler<3>(pLoopRef, A_hdr, B_hdr);
+    stnHandler<float, 3>(pLoopRef, A_hdr, B_hdr);
+}
+
+// jac3d.c's FP64 loops (examples/Performance/jac3d_perf.c:56-73 in FP64) through
+// the same generated shape, for comparison with the library's fused kernels
+extern "C" void loop_jac3d_upd_gen_cuda(DvmType *pLoopRef, DvmType A_hdr[], DvmType B_hdr[], double *eps_ptr) {
+    (void)eps_ptr;
+    updHandler<double, 3>(pLoopRef, A_hdr, B_hdr);
+}
+extern "C" void loop_jac3d_stn_gen_cuda(DvmType *pLoopRef, DvmType A_hdr[], DvmType B_hdr[]) {
+    stnHandler<double, 3>(pLoopRef, A_hdr, B_hdr);
 }

@@ -37,6 +37,31 @@ def test_jacobi_golden(g, golden, mode):
         assert sha(A) == c["A_sha256"] and sha(B) == c["B_sha256"], (name, mode)
 
 
+@pytest.mark.parametrize("mode", ["plain", "batched"])
+def test_jacobi3d_generated_handlers_golden(g, golden, mode):
+    """The FP64 Jacobi-3D program through cdvmh's generated one-point-per-thread
+    handlers (jacperf_cuda.cu: one MAX slot per launched thread) instead of the
+    library's kernels: the same golden outputs, bit for bit."""
+    import ctypes
+    g.set_mode(mode)
+    w = g.workloads()
+    w.wl_jac3d_use_generated.argtypes = [ctypes.c_int]
+    w.wl_jac3d_use_generated(1)
+    try:
+        for name, c in golden.items():
+            if c["prog"] != "jac3d" or c["params"][0] > 200:
+                continue
+            n, it, seed = c["params"]
+            j = g.Jacobi(3, n, seed)
+            eps = j.run(it)
+            A, B = j.fetch()
+            j.close()
+            assert np.array_equal(eps, unhex(c["eps"])), (name, mode)
+            assert sha(A) == c["A_sha256"] and sha(B) == c["B_sha256"], (name, mode)
+    finally:
+        w.wl_jac3d_use_generated(0)
+
+
 def test_jacobi2d_cpu_config_golden(g, golden):
     """The reference's CPU configuration (1024^2, 100 iterations) on the GPU path."""
     c = golden["jac2d_n1024_it100"]
