@@ -178,40 +178,56 @@ static void dropVar(Var *v) {
     delete v;
 }
 
+static bool inCurrentRegion(const Var *v) {
+    if (st.curRegion)
+        for (auto &rv : st.curRegion->vars)
+            if (rv.var == v) return true;
+    return false;
+}
+
+// Variables known from earlier regions and loops that overlap [lo, hi), other
+// than `keep`: the program's memory there now holds something else, so unless
+// the current region registered them they are forgotten, device copies and
+// cached graphs with them.
+static void dropOverlaps(const char *lo, const char *hi, const Var *keep) {
+    auto first = st.vars.upper_bound(lo);
+    if (first != st.vars.begin()) --first;
+    std::vector<Var *> stale;
+    for (auto it = first; it != st.vars.end() && it->first < hi; ++it)
+        if (it->second != keep && it->second->addr + it->second->size > lo) stale.push_back(it->second);
+    if (stale.empty()) return;
+    queueFlush();  // queued loops may still name them
+    for (Var *o : stale) {
+        GB_CHECK(!inCurrentRegion(o), "variable at %p overlaps the variable '%s' registered in this region",
+                 (const void *)lo, o->name.c_str());
+        dropVar(o);
+    }
+}
+
 Var *varGet(const void *addr, size_t size) {
-    auto it = st.vars.find((const char *)addr);
+    const char *lo = (const char *)addr, *hi = lo + size;
+    auto it = st.vars.find(lo);
     if (it != st.vars.end()) {
         Var *v = it->second;
-        if (size > v->size) {
-            GB_CHECK(!v->dev || v->hostActual, "variable at %p grows while its device copy is newer", addr);
+        // the same extent, or a smaller one inside what this region registered: the same variable
+        if (size == v->size || (size < v->size && inCurrentRegion(v))) return v;
+        GB_CHECK(!v->dev || v->hostActual, "variable at %p changes size (%zu -> %zu bytes) while its device copy is "
+                 "newer than the program's", addr, v->size, size);
+        if (size > v->size && inCurrentRegion(v)) {
+            // this region registers more of it: the device copy is made anew
+            dropOverlaps(v->addr + v->size, hi, v);
             if (v->dev) devFree(v->dev);
             v->dev = nullptr;
             v->size = size;
             v->devActual = false;
             v->hostActual = true;
+            return v;
         }
-        return v;
+        // a different extent at an address known from an earlier region: the program's
+        // memory holds a new variable there (an allocation reused), so the old one is
+        // forgotten with the others it overlaps; keeping it would copy its old size back
     }
-    // variables known from earlier regions and loops that overlap the new one: the
-    // program's memory there now holds something else -- unless the current
-    // region registered them, they are forgotten (their device copies with them)
-    const char *lo = (const char *)addr, *hi = lo + size;
-    auto first = st.vars.upper_bound(lo);
-    if (first != st.vars.begin()) --first;
-    std::vector<Var *> stale;
-    for (auto it = first; it != st.vars.end() && it->first < hi; ++it)
-        if (it->second->addr + it->second->size > lo) stale.push_back(it->second);
-    if (!stale.empty()) {
-        queueFlush();  // queued loops may still name them
-        for (Var *o : stale) {
-            bool inRegion = false;
-            if (st.curRegion)
-                for (auto &rv : st.curRegion->vars) inRegion = inRegion || rv.var == o;
-            GB_CHECK(!inRegion, "variable at %p overlaps the variable '%s' registered in this region", addr,
-                     o->name.c_str());
-            dropVar(o);
-        }
-    }
+    dropOverlaps(lo, hi, nullptr);
     Var *v = new Var();
     v->addr = (const char *)addr;
     v->size = size;

@@ -52,3 +52,26 @@ def test_overlapping_variables_from_earlier_regions(rt):
     before = buf.copy()
     rt.dvmh_get_actual_variable2_(ctypes.c_void_p(p))
     assert np.array_equal(buf, before)
+
+
+def test_smaller_variable_at_a_known_address(rt):
+    # a new, smaller variable where an earlier region registered a larger one (an
+    # allocation reused): reading it back copies only its own bytes, never the old size
+    buf = np.full(24, 1.0)
+    p = buf.ctypes.data
+    region_with(rt, p, 192, b"old")
+    rt.dvmh_get_actual_variable2_(ctypes.c_void_p(p))
+    buf[:] = 2.0
+    rt.dvmh_actual_variable2_(ctypes.c_void_p(p))
+    region_with(rt, p, 128, b"new")      # doubles 0..15; the device copy is newer afterwards
+    buf[16:] = 9.0                       # the program's memory beyond the new variable
+    rt.dvmh_get_actual_variable2_(ctypes.c_void_p(p))
+    assert np.array_equal(buf[:16], np.full(16, 2.0))
+    assert np.array_equal(buf[16:], np.full(8, 9.0))
+    # and growing again at the same address from a later region
+    buf[:] = 3.0
+    rt.dvmh_actual_variable2_(ctypes.c_void_p(p))
+    region_with(rt, p, 192, b"grown")
+    buf[:] = -1.0
+    rt.dvmh_get_actual_variable2_(ctypes.c_void_p(p))
+    assert np.array_equal(buf, np.full(24, 3.0))
