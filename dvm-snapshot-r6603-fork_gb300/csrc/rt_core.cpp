@@ -211,10 +211,10 @@ Var *varGet(const void *addr, size_t size) {
         Var *v = it->second;
         // the same extent, or a smaller one inside what this region registered: the same variable
         if (size == v->size || (size < v->size && inCurrentRegion(v))) return v;
-        GB_CHECK(!v->dev || v->hostActual, "variable at %p changes size (%zu -> %zu bytes) while its device copy is "
-                 "newer than the program's", addr, v->size, size);
         if (size > v->size && inCurrentRegion(v)) {
             // this region registers more of it: the device copy is made anew
+            GB_CHECK(!v->dev || v->hostActual, "variable at %p grows (%zu -> %zu bytes) while its device copy is "
+                     "newer than the program's", addr, v->size, size);
             dropOverlaps(v->addr + v->size, hi, v);
             if (v->dev) devFree(v->dev);
             v->dev = nullptr;
