@@ -54,5 +54,32 @@ def test_workload_handlers_exported():
     _, g = ge.package()
     w = ctypes.CDLL(g.WORKLOADS)
     for name in ["loop_jac3d_upd_cuda", "loop_jac3d_stn_cuda", "loop_sor3d_cuda", "loop_heat_cuda",
-                 "loop_heat_batch_cuda", "wl_jac3d_setup", "wl_sor3d_run", "wl_heat_step"]:
+                 "loop_heat_batch_cuda", "wl_jac3d_setup", "wl_sor3d_run", "wl_heat_step",
+                 # handlers in cdvmh's generated shapes
+                 "loop_gen3d_cuda", "loop_genred_cuda", "loop_gs2d_cuda", "loop_gsd2d_cuda", "loop_gsd3d_cuda",
+                 "loop_rec2d_cuda", "loop_sor3d_gen_cuda", "loop_jac3d_upd_gen_cuda", "loop_jac3d_stn_gen_cuda",
+                 "loop_jacperf3_upd_cuda", "loop_jacperf2_stn_cuda", "wl_jacperf_run", "wl_genred_run_data"]:
         assert hasattr(w, name), name
+
+
+@pytest.mark.parametrize("pattern", [0, 1, 2])
+def test_edge_value_patterns_match_the_oracle(pattern):
+    """The edge-value inputs of the reductions program (wl_genred_pattern,
+    host C in the workload library; the reference driver compiles the same
+    source to make the golden cases) are the ones the oracle's own copy
+    (orc_genred_pattern) builds when it checks those goldens."""
+    import numpy as np
+
+    import __graft_entry__ as ge
+    from oracle import orc
+    ge.build()
+    _, g = ge.package()
+    w = ctypes.CDLL(g.WORKLOADS)
+    D, I = ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_int)
+    w.wl_genred_pattern.argtypes = [ctypes.c_int, ctypes.c_long, D, I]
+    n = 10007
+    x = np.zeros(n)
+    v = np.zeros(n, dtype=np.int32)
+    assert w.wl_genred_pattern(pattern, n, x.ctypes.data_as(D), v.ctypes.data_as(I)) == 0
+    xo, vo = orc.genred_pattern(pattern, n)
+    assert x.tobytes() == xo.tobytes() and np.array_equal(v, vo)
