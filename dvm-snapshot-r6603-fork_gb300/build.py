@@ -43,7 +43,8 @@ def _newer(src_list, out):
 
 def _headers():
     return glob.glob(os.path.join(INC, "*.h")) + glob.glob(os.path.join(PKG, "csrc", "*.h")) + \
-        glob.glob(os.path.join(PKG, "csrc", "*.inc")) + glob.glob(os.path.join(PKG, "workloads", "*.h"))
+        glob.glob(os.path.join(PKG, "csrc", "*.inc")) + glob.glob(os.path.join(PKG, "csrc", "kernels", "*.cuh")) + \
+        glob.glob(os.path.join(PKG, "workloads", "*.h"))
 
 
 def _compile(src, extra=()):

@@ -38,6 +38,7 @@
 
 #include "../../../include/dvmh_gb.h"
 #include "../../../include/dvmh_gb_kernels.h"
+#include "devinfo.cuh"
 
 namespace {
 
@@ -321,16 +322,9 @@ int sweepT(double *A, const Geo &g, const double *wDev, double *items, void *scr
     if (g.na + g.nb + g.nc - 2 > MAX_PLANES || ntiles >= (1L << 30)) return -1;
     const size_t smem = T::SMEM + sizeof(int) * (MAX_PLANES + 1);  // one size for every launch (occupancy cached)
     if (cudaMemsetAsync(scratch, 0, (size_t)(ntiles + 64) * sizeof(int), s) != cudaSuccess) return -1;
-    static int occ = 0, sms = 0;
-    if (!occ) {
-        cudaFuncSetAttribute(kSorWave<TK>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kSorWave<TK>, NT, smem);
-        int dev = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        if (occ < 1) occ = 1;
-    }
-    long grid = (long)occ * sms;  // all CTAs resident at once: waits always resolve
+    static std::atomic<int> occCache[gbdev::MAX_DEVICES];
+    const int occ = gbdev::residentCtas(occCache, kSorWave<TK>, NT, smem);
+    long grid = (long)occ * gbdev::smCount();  // all CTAs resident at once: waits always resolve
     long gridCap = (ntiles + WPB - 1) / WPB;
     if (grid > gridCap) grid = gridCap;
     kSorWave<TK><<<(unsigned)grid, NT, smem, s>>>(A, g, wDev, done, counter, items, status);
@@ -548,15 +542,9 @@ int sweepStream(double *A, const Geo &g0, const double *wDev, double *items, voi
     unsigned *counter = (unsigned *)scratch;
     int *prog = (int *)scratch + 64;  // counter on its own 256-byte line
     if (cudaMemsetAsync(scratch, 0, (size_t)(ncols + 64) * sizeof(int), s) != cudaSuccess) return -1;
-    static int occ = 0, sms = 0;
-    if (!occ) {
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kSorStream, SNT, 0);
-        int dev = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        if (occ < 1) occ = 1;
-    }
-    long grid = (long)occ * sms;  // all CTAs resident at once: waits always resolve
+    static std::atomic<int> occCache[gbdev::MAX_DEVICES];
+    const int occ = gbdev::residentCtas(occCache, kSorStream, SNT, 0);
+    long grid = (long)occ * gbdev::smCount();  // all CTAs resident at once: waits always resolve
     const long gridCap = (ncols + SWPB - 1) / SWPB;
     if (grid > gridCap) grid = gridCap;
     kSorStream<<<(unsigned)grid, SNT, 0, s>>>(A, g, wDev, prog, counter, items, status);

@@ -25,6 +25,7 @@
 
 #include "../../../include/dvmh_gb.h"
 #include "../../../include/dvmh_gb_kernels.h"
+#include "devinfo.cuh"
 #include "softfp64.cuh"
 
 namespace {
@@ -159,16 +160,7 @@ __global__ void __launch_bounds__(HT) kHeatMany(const dvmhgb_heat_desc *__restri
     }
 }
 
-int smCount() {
-    static int n = 0;
-    if (!n) {
-        int dev = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
-        if (n <= 0) n = 152;
-    }
-    return n;
-}
+int smCount() { return gbdev::smCount(); }
 
 }  // namespace
 

@@ -368,6 +368,87 @@ SF_HD uint64_t q64(double x, bool &ok) {
     return in ? ((X & MANT) | HID) << (e - 1011u) : 0;
 }
 
+// ---------------------------------------------------------------- 61-bit fixed point (stencil sums)
+//
+// A double x = +0 or 2^-9 <= x < 1 is an integer multiple of 2^-61 below 2^61
+// (its last significand bit weighs at least 2^-9 * 2^-52), so q61(x) = x * 2^61
+// is exact in a uint64.  Sums of up to six such values stay below 6 * 2^61 <
+// 2^64.  In this form an FP64 addition of two q61-representable values is an
+// integer addition (exact) followed by a rounding of the sum to 53
+// significant bits, to nearest even: the bits below the sum's 53-bit
+// significand are at most 11 (the sum is below 2^64), so the rounding touches
+// the low 32-bit word and a carry.  RN(a + b) of the FP64 unit and
+// q61_add(q61(a), q61(b)) are the same number, and the rounded sum is again a
+// multiple of 2^-61, so chains of additions stay exact in this form.  The
+// division by 6 of the stencil rounds the q61 sum straight to a double.
+// (The rounding is the textbook round-to-nearest-even on a guard position:
+// Goldberg 1991; Muller et al., Handbook of Floating-Point Arithmetic, ch. 2.)
+
+SF_HD bool q61_ok(double x) {
+    uint32_t h = hi32(bits(x));
+    return (h >> 20) - 1014u <= 8u || bits(x) == 0;  // exponent field 1014..1022 and sign clear, or +0
+}
+
+// x * 2^61 for a q61_ok x (an arbitrary value for any other x)
+SF_HD uint64_t q61(double x) {
+    uint64_t X = bits(x);
+    uint32_t e = hi32(X) >> 20;
+    uint64_t m = ((X & MANT) | HID) << ((e - 1014u) & 63u);
+    return X == 0 ? 0 : m;
+}
+
+// the index of the most significant set bit of a 32-bit word, -1 for 0
+SF_HD int msb32(uint32_t x) {
+#ifdef __CUDA_ARCH__
+    int r;
+    asm("bfind.u32 %0, %1;" : "=r"(r) : "r"(x));
+    return r;
+#else
+    return x ? 31 - __builtin_clz(x) : -1;
+#endif
+}
+
+// RN(s + t) for q61 operands whose exact sum is below 2^64
+SF_HD uint64_t q61_add(uint64_t s, uint64_t t) {
+    uint64_t u = s + t;
+    int r = msb32((uint32_t)(u >> 32)) - 20;  // significant bits beyond 53 (msb index - 52)
+    r = r < 0 ? 0 : r;
+    const uint32_t lo = (uint32_t)u, m1 = 1u << r, mask = m1 - 1u;
+    // half - 1 + lsb: carries into the kept bits iff the dropped part is above
+    // half, or exactly half with an odd lsb; masked to 0 when nothing is dropped
+    const uint32_t inc = ((m1 >> 1) - 1u + ((lo >> r) & 1u)) & mask;
+    u += inc;
+    return u & ~(uint64_t)mask;
+}
+
+// RN((s * 2^-61) / 6) for a q61 value s with at most 53 significant bits
+SF_HD double q61_div6(uint64_t s) {
+    const int c = clz64(s | 1);  // s == 0 is handled at the end
+    const uint64_t n = s << c;   // leading one at bit 63
+    const uint64_t q = mulhi(n, 0xAAAAAAAAAAAAAAABull) >> 1;  // floor(n / 3), in [2^61, 2^63)
+    const uint64_t r = n - 3 * q;
+    const bool top = (q >> 62) != 0;
+    const int sh = top ? 10 : 9;
+    uint64_t m = q >> sh;
+    const uint64_t guard = (q >> (sh - 1)) & 1;
+    const uint64_t sticky = (q & ((1ull << (sh - 1)) - 1)) | r;
+    m += guard & (uint64_t)((sticky != 0) | (m & 1));
+    const uint64_t e = (uint64_t)((top ? 1023 : 1022) - c);  // exponent field of the quotient
+    // the significand's leading one adds 1 to the exponent field; a rounding
+    // carry to 2^53 adds 2, which is the next binade with a zero significand
+    const uint64_t res = ((e - 1) << 52) + m;
+    return from(s == 0 ? 0 : res);
+}
+
+// the double s * 2^-61 for a q61 value with at most 53 significant bits
+SF_HD double q61_to(uint64_t s) {
+    if (s == 0) return 0.0;
+    const int c = clz64(s);
+    const int p = 63 - c;  // msb index
+    const uint64_t m = p >= 52 ? s >> (p - 52) : s << (52 - p);
+    return from(((uint64_t)(p - 61 + 1023 - 1) << 52) + m);
+}
+
 // Max(|t|, m) on bit patterns: for non-negative doubles the IEEE order is the
 // unsigned integer order.  A NaN t leaves m unchanged, as (t > m ? t : m) does.
 SF_HD uint64_t absmax_bits(double t, uint64_t m) {

@@ -113,13 +113,14 @@ extern "C" void loop_jac3d_fused_cuda(DvmType refs[2], DvmType A_hdr[], DvmType 
     cudaStream_t stream;
     dvmh_loop_cuda_get_config_C(upd, 0, 0, &threads, &stream, 0);
     dvmh_loop_cuda_get_config_C(stn, 0, 0, &threads, &stream, 0);
-    const int variant = dvmhgb_loop_variant(upd, DVMHGB_JAC3D_VARIANTS + 2, DEF_FUSED);  // + the pair, unfused or overlapped
+    const int variant = dvmhgb_loop_variant(upd, DVMHGB_JAC3D_VARIANTS + 3, DEF_FUSED);  // + the pair: unfused, overlapped (2)
     double eps, *eps_grid = 0;
     dvmh_loop_cuda_register_red_C(upd, 1, (void **)&eps_grid, 0);
     dvmh_loop_red_init_C(upd, 1, &eps, 0);
     dvmh_loop_cuda_red_prepare_C(upd, 1, dvmhgb_jac3d_fused_items(lo, hi, variant), 0);
     // the fused kernel writes the next B into a second buffer; the unfused pair writes B itself
     double *Bnew = variant >= DVMHGB_JAC3D_UNFUSED ? B.base : (double *)dvmhgb_loop_alt_buffer(stn, B_hdr);
+    // (the update-then-fixed-point-stencil variants could also write B in place; they keep the one-pass shape)
     check(dvmhgb_jac3d_fused(A.base, B.base, Bnew, A.st, A.ext, lo, hi, eps_grid, variant, stream),
           "loop_jac3d_fused_cuda");
     dvmh_loop_cuda_red_finish_C(upd, 1);

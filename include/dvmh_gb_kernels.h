@@ -36,22 +36,28 @@ int dvmhgb_jac3d_update(double *A, const double *B, const long st[3], const long
  * + N, N = 0..5 additions of a cell on the FP64 unit (the others on the integer
  * pipe when the CTA's inputs are all +0 or positive normal, else all native);
  * v = 12, 13: all native, one row per thread, registers capped for 3 / 4 CTAs
- * per SM; -1 for v outside 0..DVMHGB_JAC3D_VARIANTS-1 */
-#define DVMHGB_JAC3D_VARIANTS 14
+ * per SM; v = 14, 15, 16: the sums in 61-bit fixed point on the integer pipe
+ * (planes whose neighbourhood holds a value outside +0 and [2^-9, 1) on the
+ * FP64 unit), registers capped for 4 / 3 / 2 CTAs per SM; -1 for v outside
+ * 0..DVMHGB_JAC3D_VARIANTS-1 */
+#define DVMHGB_JAC3D_VARIANTS 17
 int dvmhgb_jac3d_stencil(const double *A, double *B, const long st[3], const long ext[3], const long lo[3],
                          const long hi[3], int native, void *stream);
 /* loops 1+2 fused (same box): reads A, B; writes A = B and Bnew = stencil(A_new)
  * into Bnew (a second buffer of B's layout), B's values outside the box copied
  * into Bnew; MAX partials, one per CTA (the count depends on the variant).
- * Variants 0..DVMHGB_JAC3D_VARIANTS-1 as above, and DVMHGB_JAC3D_UNFUSED: the
- * update and the stencil kernels one after the other (Bnew may then be B
- * itself: the stencil reads only A; the fused variants reject Bnew == B) */
+ * Variants 0..13 as above (one pass), 14..16 the update kernel and then the
+ * fixed-point stencil of that variant, and DVMHGB_JAC3D_UNFUSED: the update
+ * and the stencil kernels (variant 13) one after the other (Bnew may then be B
+ * itself: the stencil reads only A; the one-pass variants reject Bnew == B) */
 #define DVMHGB_JAC3D_UNFUSED DVMHGB_JAC3D_VARIANTS
 /* DVMHGB_JAC3D_OVERLAP: the pair in 8 chunks of planes, the updates on
  * `stream`, the stencils on a second stream of the library (stencil chunk k
  * after update chunk k+1), joined back into `stream`, so that the HBM-bound
  * update runs beside the FP64-bound stencil; Bnew must be B */
 #define DVMHGB_JAC3D_OVERLAP (DVMHGB_JAC3D_VARIANTS + 1)
+/* DVMHGB_JAC3D_OVERLAP_Q: the same with the fixed-point stencil (variant 14) */
+#define DVMHGB_JAC3D_OVERLAP_Q (DVMHGB_JAC3D_VARIANTS + 2)
 long dvmhgb_jac3d_fused_items(const long lo[3], const long hi[3], int native);
 int dvmhgb_jac3d_fused(double *A, const double *B, double *Bnew, const long st[3], const long ext[3],
                        const long lo[3], const long hi[3], double *items, int native, void *stream);

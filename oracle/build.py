@@ -22,10 +22,20 @@ def build(force=False):
     return LIB
 
 
+def reference_source():
+    """The reference's dvm_sys source tree: $DVMH_REF_SRC, else a checkout named
+    reference/ beside this repository; None where neither exists (the GPU machine)."""
+    env = os.environ.get("DVMH_REF_SRC")
+    if env:
+        return env if os.path.isdir(env) else None
+    sibling = os.path.join(os.path.dirname(os.path.dirname(HERE)), "reference", "dvm_sys")
+    return sibling if os.path.isdir(sibling) else None
+
+
 def build_reference():
     """Build the reference runtime from its sources (only where they exist)."""
-    ref = os.environ.get("DVMH_REF_SRC", "/root/reference/dvm_sys")
-    if not os.path.isdir(ref):
+    ref = reference_source()
+    if ref is None:
         return None
     root = os.path.dirname(HERE)
     subprocess.check_call(["make", "-s", "-f", "oracle/ref.mk", "-j8", "REF=" + ref], cwd=root)

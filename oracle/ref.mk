@@ -3,7 +3,7 @@
 # infrastructure only: the result is the oracle that pins oracle/restate.c and
 # generates tests/golden/.  Nothing in the product links it.
 #
-# usage:  make -f oracle/ref.mk -j8 REF=/root/reference/dvm_sys
+# usage:  make -f oracle/ref.mk -j8 REF=<the reference checkout>/dvm_sys
 #
 # What is compiled (file lists follow rts/src/makefile.uni OBJ_C/OBJ_FTN and
 # rts/dvmh/makefile.uni OBJ, written out here; the reference makefiles are not run):
@@ -15,7 +15,9 @@
 # sources expect from the installer) and an empty dynamic_include.h (NVRTC hook).
 # Defines = the reference installer's single-process, MPI-stub configuration.
 
-REF     ?= /root/reference/dvm_sys
+ifndef REF
+$(error REF must name the reference dvm_sys source tree)
+endif
 OUT     ?= oracle/_ref
 GEN      = $(OUT)/gen
 OBJ_DIR  = $(OUT)/obj

@@ -18,7 +18,10 @@ import tempfile
 import numpy as np
 
 ROOT = os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
-REF = os.environ.get("DVMH_REF_SRC", "/root/reference/dvm_sys")
+sys.path.insert(0, ROOT)
+from oracle.build import reference_source  # noqa: E402
+
+REF = reference_source()
 DRIVER = os.path.join(ROOT, "oracle", "_ref", "ref_driver")
 
 # (name, program, params, keep full arrays)
@@ -98,6 +101,8 @@ def hx(a):
 
 
 def build():
+    if REF is None:
+        sys.exit("make_golden: the reference sources are needed (set DVMH_REF_SRC)")
     subprocess.check_call(["make", "-s", "-f", "oracle/ref.mk", "-j8", "REF=" + REF], cwd=ROOT)
 
 

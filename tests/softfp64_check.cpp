@@ -116,3 +116,42 @@ extern "C" long softfp64_check_scale(long n, uint64_t seed) {
     }
     return bad;
 }
+
+// q61 chains: ((((a + b) + c) + d) + e) + f, then / 6, for q61_ok operands
+// (exponent fields 1014..1022 or +0, mantissas with random, sparse or
+// all-ones low bits so that ties and carries into the next binade occur)
+static double q61Operand(uint64_t r, uint64_t q) {
+    if ((q & 15) == 0) return 0.0;
+    uint64_t e = 1014 + (q >> 4) % 9, m = r & sf::MANT;
+    switch ((q >> 12) & 3) {
+        case 0: m &= ~((1ull << ((q >> 16) % 53)) - 1); break;  // few significant low bits
+        case 1: m |= (1ull << ((q >> 16) % 52)) - 1; break;     // runs of ones
+        default: break;
+    }
+    return sf::from((e << 52) | m);
+}
+
+extern "C" long softfp64_check_q61(long n, uint64_t seed) {
+    volatile double six = 6.0;
+    long bad = 0;
+    for (long i = 0; i < n; i++) {
+        double v[6];
+        for (int k = 0; k < 6; k++) v[k] = q61Operand(mix(seed + 12 * i + 2 * k), mix(seed + 12 * i + 2 * k + 1));
+        double t = v[0];
+        uint64_t s = sf::q61(v[0]);
+        for (int k = 0; k < 6; k++) {
+            if (!sf::q61_ok(v[k]) || sf::q61_to(sf::q61(v[k])) != v[k]) bad++;
+            if (k == 0) continue;
+            t = t + v[k];
+            s = sf::q61_add(s, sf::q61(v[k]));
+            bad += !same(sf::q61_to(s), t);
+        }
+        bad += !same(sf::q61_div6(s), t / six);
+    }
+    // the range test refuses everything outside [2^-9, 1) and +0
+    const double outside[] = {-0.0, -0.5, 1.0, 1.5, 0x1p-10, 0x1.fffffffffffffp-10, 5e-324, 1e300};
+    for (double x : outside) bad += sf::q61_ok(x);
+    const double inside[] = {0.0, 0x1p-9, 0x1.fffffffffffffp-1, 0.5, 0.1};
+    for (double x : inside) bad += !sf::q61_ok(x);
+    return bad;
+}

@@ -130,11 +130,12 @@ def test_plain_mode_no_fusion(g):
     assert s["fused_pairs"] == 0 and s["graphs_captured"] == 0 and s["handler_calls"] == 6
 
 
-@pytest.mark.parametrize("variant", list(range(16)))
+@pytest.mark.parametrize("variant", list(range(20)))
 def test_jacobi3d_variants_vs_oracle(g, variant):
     """Every kernel variant of the 3-D loops (rows per thread x additions on the
-    FP64 unit, the rest on the integer pipe) through the program, plain
-    (separate update and stencil loops) and batched (the fused loop)."""
+    FP64 unit, the rest on the integer pipe; the fixed-point stencils; the
+    unfused and overlapped pairs) through the program, plain (separate update
+    and stencil loops) and batched (the fused loop)."""
     try:
         g.force_variant(variant)
         for n, iters in ((19, 4), (66, 3), (131, 2)):
@@ -163,7 +164,7 @@ def _stencil_ref(A):
     return t / 6.0, c
 
 
-@pytest.mark.parametrize("variant", list(range(14)))
+@pytest.mark.parametrize("variant", list(range(17)))
 def test_jacobi3d_kernels_signs_and_tiny_values(g, variant):
     """The kernels directly through the C ABI on values that take every path:
     negative values (no integer-pipe additions for that CTA), values below
@@ -280,3 +281,40 @@ def test_subarray_actuality(g, mode):
     j.close()
     assert np.array_equal(Ag, A) and np.array_equal(Bg, B), mode
     assert eps[0] == e_ref, mode
+
+
+@pytest.mark.parametrize("variant", [14, 15, 16])
+def test_jacobi3d_fixed_point_stencil_range_edges(g, variant):
+    """The fixed-point stencil computes a plane on the FP64 unit when any value
+    its cells read lies outside +0 and [2^-9, 1).  Values on both sides of
+    those limits are planted where each kind of load reads them: a CTA's own
+    rows, the j-halo rows above and below it, the k-edge columns left and right
+    of its 64-element chunk, the i-planes before and after a chunk of planes,
+    and the array's first and last planes.  Bit-exact against float64 on the CPU."""
+    import ctypes
+    import torch
+    L = g.runtime()
+    n0, n1, n2 = 70, 41, 200  # row pitch 200: 16-byte aligned rows
+    LA = ctypes.c_long * 3
+    st, ext, lo, hi = LA(n1 * n2, n2, 1), LA(n0, n1, n2), LA(1, 1, 1), LA(n0 - 2, n1 - 2, n2 - 2)
+    gen = torch.Generator().manual_seed(100 + variant)
+    A = 0.5 + 0.5 * torch.rand(n0, n1, n2, dtype=torch.float64, generator=gen)
+    inside = [2.0 ** -9, 0.9999999999999999, 0.0, 2.0 ** -9 * 1.5]
+    outside = [2.0 ** -9 * 0.9999999999999999, 1.0, -0.25, 5e-324, -0.0, 2.0 ** -60, 1.5]
+    rng = np.random.default_rng(variant)
+    spots = [(1, 1, 1), (n0 - 2, n1 - 2, n2 - 2), (0, 5, 7), (n0 - 1, 9, 70)]
+    spots += [(int(i), int(j), int(k)) for i, j, k in zip(rng.integers(0, n0, 40), rng.integers(0, n1, 40),
+                                                            rng.integers(0, n2, 40))]
+    spots += [(20, 8, 63), (21, 7, 64), (30, 16, 127), (31, 15, 128), (44, 24, 0), (45, 40, 199), (8, 0, 90)]
+    for q, (i, j, k) in enumerate(spots):
+        A[i, j, k] = (outside if q % 3 else inside)[q % 4 if q % 3 == 0 else q % 7]
+    Ad = A.cuda()
+    Bs = torch.full_like(Ad, 7.0)
+    vp = lambda t: ctypes.c_void_p(t.data_ptr())
+    sp = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    assert L.dvmhgb_jac3d_stencil(vp(Ad), vp(Bs), st, ext, lo, hi, variant, sp) == 0
+    torch.cuda.synchronize()
+    s_ref, _ = _stencil_ref(A)
+    got = Bs.cpu()
+    assert torch.equal(got[1:-1, 1:-1, 1:-1].view(torch.int64), s_ref.view(torch.int64)), variant
+    assert torch.equal(got[0], torch.full_like(got[0], 7.0))  # outside the box: untouched

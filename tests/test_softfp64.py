@@ -51,3 +51,11 @@ def test_softfp64_matches_gb300_fp64_unit():
     bad = (ctypes.c_long * 4)()
     assert g.runtime().dvmhgb_selftest_softfp64(ctypes.c_long(1 << 30), ctypes.c_ulonglong(7), bad) == 0
     assert list(bad) == [0, 0, 0, 0], "mismatches add/sub/mul/div6: %s" % list(bad)
+
+
+@pytest.mark.parametrize("seed", [5, 20261205])
+def test_q61_chain_matches_host_fpu(hostlib, seed):
+    """The fixed-point form of the Jacobi stencil: five additions and the division by 6."""
+    hostlib.softfp64_check_q61.restype = ctypes.c_long
+    hostlib.softfp64_check_q61.argtypes = [ctypes.c_long, ctypes.c_uint64]
+    assert hostlib.softfp64_check_q61(2_000_000, seed) == 0
