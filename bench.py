@@ -521,7 +521,24 @@ def extra_configs(g, stream):
     out["jacobi2d_1024"] = jacobi2d(g, stream, 1024, 100)
     out["jacperf3d_fp32_384"] = jacperf(g, 3, 384, 5.058044, 1e-4)
     out["jacperf2d_fp32_8000"] = jacperf(g, 2, 8000, 58.37598, 1e-3)
+    out["tune"] = tune_configs(g)
     return out
+
+
+def tune_configs(g):
+    """The learned tuner on the configurations' own loops (J2 1024^2, J3 512^3,
+    SOR 384^3, heat 256 arrays): exhaustive variant tuning at smaller sizes
+    trains the variant model; at the configuration's size, exhaustive tuning
+    and model-guided tuning are run and compared (tune.configs_eval)."""
+    import importlib.util
+    spec = importlib.util.spec_from_file_location("dvmhgb_tune", os.path.join(ROOT, "dvm-snapshot-r6603-fork_gb300",
+                                                                              "tune.py"))
+    tune = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(tune)
+    try:
+        return tune.configs_eval(g, seed=SEED, log=lambda *a: None)
+    finally:
+        g.set_mode("batched")
 
 
 def jacperf(g, rank, L, answer, tol):

@@ -72,6 +72,7 @@ def build(verbose=False):
     rt_src = sorted(glob.glob(os.path.join(PKG, "csrc", "*.cpp")) + glob.glob(os.path.join(PKG, "csrc", "*.cu")) +
                     glob.glob(os.path.join(PKG, "csrc", "kernels", "*.cu")))
     wl_src = sorted(glob.glob(os.path.join(PKG, "workloads", "*.c")) +
+                    glob.glob(os.path.join(PKG, "workloads", "*.cpp")) +
                     glob.glob(os.path.join(PKG, "workloads", "*.cu")))
     jobs = max(2, min(16, os.cpu_count() or 4))
     with cf.ThreadPoolExecutor(jobs) as ex:

@@ -58,7 +58,15 @@ struct Tile {
     static constexpr int RPL = 32 / TK;          // rows per warp load
     static constexpr int LOG = TK == 32 ? 5 : (TK == 16 ? 4 : 3);
 };
-constexpr long SPIN_LIMIT = 1L << 24;    // ~1-4 s of polling before giving up
+constexpr long SPIN_LIMIT = 1L << 24;    // default polls before giving up: ~1-4 s
+
+// How long a wavefront launch waits: every wait for a predecessor polls at
+// most pollLimit times; the hand-out of tiles (columns) starts at firstIndex
+// (0 in every sweep the runtime runs; tests start later so that a wait expires)
+struct Bound {
+    long pollLimit;
+    unsigned firstIndex;
+};
 constexpr int ERR_SOR_TIMEOUT = 0x50520001;
 constexpr int MAX_PLANES = 1536;         // a + b + c planes of the tile grid
 
@@ -186,7 +194,7 @@ __device__ __forceinline__ void stageFaces(double *box, const double *A, const G
 
 template <int TK>
 __global__ void __launch_bounds__(NT) kSorWave(double *A, Geo g, const double *wPtr, int *done, unsigned *counter,
-                                               double *items, int *status) {
+                                               double *items, int *status, Bound bound) {
     using T = Tile<TK>;
     constexpr int SK = T::SK;
     extern __shared__ double sm[];  // per warp: box [SI][SJ][SK] + olds [32][OSTR]; then pre[np + 1]
@@ -203,7 +211,7 @@ __global__ void __launch_bounds__(NT) kSorWave(double *A, Geo g, const double *w
     const long nck = g.nc;
     while (true) {
         long idx = 0;
-        if (lane == 0) idx = (long)atomicAdd(counter, 1u);  // >= 2^31 once a warp has failed
+        if (lane == 0) idx = (long)atomicAdd(counter, 1u) + bound.firstIndex;  // >= 2^31 once a warp has failed
         idx = __shfl_sync(0xffffffffu, idx, 0);
         if (idx >= ntiles) break;
         long a, b, c;
@@ -219,7 +227,7 @@ __global__ void __launch_bounds__(NT) kSorWave(double *A, Geo g, const double *w
                 const int *f = done + tileLinear(g, pa, pb, pc);
                 long n = 0;
                 while (ldAcquire(f) == 0) {
-                    if (++n > SPIN_LIMIT) {
+                    if (++n > bound.pollLimit) {
                         atomicExch(status, ERR_SOR_TIMEOUT);
                         atomicOr(counter, 0x80000000u);  // no warp takes another tile
                         fail = 1;
@@ -314,7 +322,8 @@ bool geo(const long st[3], const long ext[3], const long lo[3], const long hi[3]
 int tkOf(int variant) { return variant == 0 ? 32 : (variant == 1 ? 16 : (variant == 2 ? 8 : (variant == 3 ? 64 : 0))); }
 
 template <int TK>
-int sweepT(double *A, const Geo &g, const double *wDev, double *items, void *scratch, int *status, cudaStream_t s) {
+int sweepT(double *A, const Geo &g, const double *wDev, double *items, void *scratch, int *status, Bound bound,
+           cudaStream_t s) {
     using T = Tile<TK>;
     const long ntiles = g.na * g.nb * g.nc;
     unsigned *counter = (unsigned *)scratch;
@@ -327,7 +336,7 @@ int sweepT(double *A, const Geo &g, const double *wDev, double *items, void *scr
     long grid = (long)occ * gbdev::smCount();  // all CTAs resident at once: waits always resolve
     long gridCap = (ntiles + WPB - 1) / WPB;
     if (grid > gridCap) grid = gridCap;
-    kSorWave<TK><<<(unsigned)grid, NT, smem, s>>>(A, g, wDev, done, counter, items, status);
+    kSorWave<TK><<<(unsigned)grid, NT, smem, s>>>(A, g, wDev, done, counter, items, status, bound);
     dvmhgb_count_launches(1);
     return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }
@@ -390,10 +399,10 @@ __device__ __forceinline__ double ldAt(const double *A, const SGeo &g, long i, l
 }
 
 // bounded wait until *f >= want; false (status written, counter stopped) when it runs out
-__device__ __forceinline__ bool waitProgress(const int *f, int want, int *status, unsigned *counter) {
+__device__ __forceinline__ bool waitProgress(const int *f, int want, int *status, unsigned *counter, long limit) {
     long n = 0;
     while (ldAcquire(f) < want) {
-        if (++n > SPIN_LIMIT) {
+        if (++n > limit) {
             atomicExch(status, ERR_SOR_TIMEOUT);
             atomicOr(counter, 0x80000000u);
             return false;
@@ -404,7 +413,7 @@ __device__ __forceinline__ bool waitProgress(const int *f, int want, int *status
 }
 
 __global__ void __launch_bounds__(SNT) kSorStream(double *A, SGeo g, const double *wPtr, int *prog, unsigned *counter,
-                                                  double *items, int *status) {
+                                                  double *items, int *status, Bound bound) {
     __shared__ double sqs[SWPB][32][SQR + 1];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, li = lane / TJ, lj = lane % TJ, sk = li + lj;
     double *sq = sqs[warp][lane];
@@ -414,7 +423,7 @@ __global__ void __launch_bounds__(SNT) kSorStream(double *A, SGeo g, const doubl
     const int nk = (int)g.nk;
     while (true) {
         long idx = 0;
-        if (lane == 0) idx = (long)atomicAdd(counter, 1u);  // >= 2^31 once a warp has failed
+        if (lane == 0) idx = (long)atomicAdd(counter, 1u) + bound.firstIndex;  // >= 2^31 once a warp has failed
         idx = __shfl_sync(0xffffffffu, idx, 0);
         if (idx >= ncols) break;
         long a, b;
@@ -437,8 +446,8 @@ __global__ void __launch_bounds__(SNT) kSorStream(double *A, SGeo g, const doubl
             // 1. the predecessors' rows up to the group's last position (lane (0, 0) reaches gr*SC + SC - 1)
             const int want = min(nk, gr * SC + SC);
             int fail = 0;
-            if (lane == 0 && predI && !waitProgress(predI, want, status, counter)) fail = 1;
-            if (lane == 1 && predJ && !waitProgress(predJ, want, status, counter)) fail = 1;
+            if (lane == 0 && predI && !waitProgress(predI, want, status, counter, bound.pollLimit)) fail = 1;
+            if (lane == 1 && predJ && !waitProgress(predJ, want, status, counter, bound.pollLimit)) fail = 1;
             if (__any_sync(0xffffffffu, fail)) return;
             __syncwarp();  // orders the acquiring lanes' loads before every lane's face loads
             // 2. the group's values: own row positions p0 .. p0 + SC (one ahead), the faces p0 .. p0 + SC - 1
@@ -518,7 +527,7 @@ __global__ void __launch_bounds__(SNT) kSorStream(double *A, SGeo g, const doubl
 }
 
 int sweepStream(double *A, const Geo &g0, const double *wDev, double *items, void *scratch, int *status,
-                cudaStream_t s) {
+                Bound bound, cudaStream_t s) {
     SGeo g;
     g.s0 = g0.s0;
     g.s1 = g0.s1;
@@ -547,7 +556,7 @@ int sweepStream(double *A, const Geo &g0, const double *wDev, double *items, voi
     long grid = (long)occ * gbdev::smCount();  // all CTAs resident at once: waits always resolve
     const long gridCap = (ncols + SWPB - 1) / SWPB;
     if (grid > gridCap) grid = gridCap;
-    kSorStream<<<(unsigned)grid, SNT, 0, s>>>(A, g, wDev, prog, counter, items, status);
+    kSorStream<<<(unsigned)grid, SNT, 0, s>>>(A, g, wDev, prog, counter, items, status, bound);
     dvmhgb_count_launches(1);
     return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }
@@ -569,18 +578,27 @@ long dvmhgb_sor3d_scratch_bytes(const long lo[3], const long hi[3], int variant)
     return (ntiles + 64) * (long)sizeof(int);
 }
 
-int dvmhgb_sor3d_sweep(double *A, const long st[3], const long ext[3], const long lo[3], const long hi[3],
-                       const double *wDev, double *items, void *scratch, int *status, int variant, void *stream) {
+int dvmhgb_sor3d_sweep_bounded(double *A, const long st[3], const long ext[3], const long lo[3], const long hi[3],
+                               const double *wDev, double *items, void *scratch, int *status, int variant,
+                               void *stream, long pollLimit, long firstIndex) {
     const int tk = tkOf(variant);
     Geo g;
     if (!tk || !A || !wDev || !items || !scratch || !status || !geo(st, ext, lo, hi, 64 / tk, g)) return -1;
+    if (pollLimit < 1 || firstIndex < 0 || firstIndex >= (1L << 30)) return -1;
+    const Bound bound{pollLimit, (unsigned)firstIndex};
     cudaStream_t s = (cudaStream_t)stream;
     switch (tk) {
-        case 64: return sweepStream(A, g, wDev, items, scratch, status, s);
-        case 32: return sweepT<32>(A, g, wDev, items, scratch, status, s);
-        case 16: return sweepT<16>(A, g, wDev, items, scratch, status, s);
-        default: return sweepT<8>(A, g, wDev, items, scratch, status, s);
+        case 64: return sweepStream(A, g, wDev, items, scratch, status, bound, s);
+        case 32: return sweepT<32>(A, g, wDev, items, scratch, status, bound, s);
+        case 16: return sweepT<16>(A, g, wDev, items, scratch, status, bound, s);
+        default: return sweepT<8>(A, g, wDev, items, scratch, status, bound, s);
     }
+}
+
+int dvmhgb_sor3d_sweep(double *A, const long st[3], const long ext[3], const long lo[3], const long hi[3],
+                       const double *wDev, double *items, void *scratch, int *status, int variant, void *stream) {
+    return dvmhgb_sor3d_sweep_bounded(A, st, ext, lo, hi, wDev, items, scratch, status, variant, stream, SPIN_LIMIT,
+                                      0);
 }
 
 }  // extern "C"

@@ -208,13 +208,24 @@ int dvmhgb_heat(const dvmhgb_heat_desc *d, void *stream) {
     return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }
 
-int dvmhgb_heat_many(const dvmhgb_heat_desc *dDev, int n, long totalStrips, void *stream) {
-    if (!dDev || n < 1 || totalStrips < 1) return -1;
+int dvmhgb_heat_desc_rows(dvmhgb_heat_desc *d, long sr) {
+    if (!d || sr < 1) return -1;
+    d->sr = sr;
+    d->strips = d->nck * ((d->hi0 - d->lo0 + sr) / sr);
+    return d->strips < (1L << 31) ? 0 : -1;
+}
+
+int dvmhgb_heat_many_grid(const dvmhgb_heat_desc *dDev, int n, long totalStrips, int ctasPerSm, void *stream) {
+    if (!dDev || n < 1 || totalStrips < 1 || ctasPerSm < 1 || ctasPerSm > 8) return -1;
     long blocks = (totalStrips + HT / 32 - 1) / (HT / 32);
-    if (blocks > (long)smCount() * 8) blocks = (long)smCount() * 8;
+    if (blocks > (long)smCount() * ctasPerSm) blocks = (long)smCount() * ctasPerSm;
     kHeatMany<<<(unsigned)blocks, HT, 0, (cudaStream_t)stream>>>(dDev, n, totalStrips);
     dvmhgb_count_launches(1);
     return cudaGetLastError() == cudaSuccess ? 0 : -1;
+}
+
+int dvmhgb_heat_many(const dvmhgb_heat_desc *dDev, int n, long totalStrips, void *stream) {
+    return dvmhgb_heat_many_grid(dDev, n, totalStrips, 8, stream);
 }
 
 }  // extern "C"

@@ -24,6 +24,7 @@
 // shared memory (2.5-D blocking): every A element comes from HBM once.
 #include <cuda_runtime.h>
 
+#include <atomic>
 #include <cstdint>
 #include <cstdio>
 
@@ -446,29 +447,35 @@ __global__ void __launch_bounds__(TX *TY, MINB) kStencil3(double *A, const doubl
 // addition plus a round-to-nearest-even of the sum to 53 significant bits,
 // and the division by 6 rounds the sum straight to the double quotient.  Bit
 // for bit the FP64 unit's results, on the integer pipe, which a GB300 SM runs
-// about 60 times faster than its FP64 unit (2 FP64 thread-operations per
-// clock): measured on GB300, 1.7e11 cells/s against 7.1e10 for the five
-// native additions.
+// far faster than its FP64 unit (2 FP64 thread-operations per clock):
+// measured on GB300, 1.7e11 cells/s of the cell arithmetic alone against
+// 7.1e10 for the five native additions.
+//
+// The integer pipe then bounds this kernel while the FP64 unit idles, so a
+// fraction of the CTAs (nat of every den, by block index) computes its cells
+// the native way -- five FP64 additions, the division on the integer pipe --
+// and both pipes of an SM work at once.  Both forms give the same bits.
 //
 // Layout of the work as in kStencil3 with one row per thread: a CTA of TY
 // warps covers 64 elements of k and TY rows of j and streams the planes i of
 // its chunk; a thread keeps planes i-1, i, i+1 of its element pair in
-// registers as q61 values, plane i+2 in flight as doubles (converted one
-// plane later, so the loads have a plane of work to arrive), and plane i's
-// rows in double-buffered shared memory for the j neighbours; k neighbours
-// come by shuffles, the chunk's edge columns by lanes 0 / 31.
+// registers (q61 values, or the doubles' bits in a native CTA), plane i+2 in
+// flight as doubles (converted one plane later, so the loads have a plane of
+// work to arrive), and plane i's rows in double-buffered shared memory for
+// the j neighbours; k neighbours come by shuffles, the chunk's edge columns
+// by lanes 0 / 31.
 //
-// Range: every value the cells of a plane read must be q61_ok.  Each thread
-// flags the values it converts; the flags of the CTA are OR-ed once per plane
-// (the barrier the shared-memory rows need anyway) and kept for the last
-// three planes.  A plane whose neighbourhood holds any other value (a
-// negative value, one below 2^-9 or at least 1, a subnormal, an infinity or a
-// NaN) is computed by the whole CTA on the FP64 unit from global memory (the
-// arithmetic of stencil7<5>), so every input gives the FP64 unit's result.
-template <int MINB>
-__global__ void __launch_bounds__(TX *TY, MINB) kStencil3Q(const double *__restrict__ A, double *Out, Box3 b,
-                                                             long p0, int ichunk) {
-    __shared__ ulonglong2 sm[2][TY + 2][TX];
+// Range (fixed-point CTAs): every value the cells of a plane read must be
+// q61_ok.  Each thread flags the values it converts; the flags of the CTA are
+// OR-ed once per plane (the barrier the shared-memory rows need anyway) and
+// kept for the last three planes.  A plane whose neighbourhood holds any
+// other value (a negative value, one below 2^-9 or at least 1, a subnormal,
+// an infinity or a NaN) is computed by the whole CTA on the FP64 unit from
+// global memory (the arithmetic of stencil7<5>), so every input gives the
+// FP64 unit's result.
+template <bool Q>
+__device__ __forceinline__ void planes3(const double *__restrict__ A, double *Out, const Box3 &b, long p0, int ichunk,
+                                        ulonglong2 (*sm)[TY + 2][TX]) {
     const int lane = threadIdx.x, ty = threadIdx.y;
     const long kb = 2 * (p0 + (long)blockIdx.x * TX);
     const long jb = b.lo1 + (long)blockIdx.y * TY;
@@ -500,9 +507,17 @@ __global__ void __launch_bounds__(TX *TY, MINB) kStencil3Q(const double *__restr
     auto ldE = [&](long ii, long joff, bool ja) -> double {
         return (ja && hcA && ii >= 0 && ii < b.e0) ? A[ii * b.s0 + joff + hc] : 0.0;
     };
+    // a loaded value in the CTA's representation (q61, or the double's bits)
     auto cv = [](double x, bool &bad) -> uint64_t {
+        if (!Q) return sf::bits(x);
         bad |= !sf::q61_ok(x);
         return sf::q61(x);
+    };
+    // (((((a + b) + c) + d) + e) + f) / 6 in the CTA's representation
+    auto cell = [](uint64_t a, uint64_t b2, uint64_t c, uint64_t d, uint64_t e, uint64_t f) -> double {
+        if (Q) return sf::q61_div6(sf::q61_add(sf::q61_add(sf::q61_add(sf::q61_add(sf::q61_add(a, b2), c), d), e), f));
+        return sf::div3p2(sf::nadd(sf::nadd(sf::nadd(sf::nadd(sf::nadd(sf::from(a), sf::from(b2)), sf::from(c)),
+                                                     sf::from(d)), sf::from(e)), sf::from(f)), 1);
     };
     // the cell (i, j, kk) on the FP64 unit, its neighbours from global memory (0 outside the array)
     auto nativeCell = [&](long i, long kk) -> double {
@@ -547,10 +562,8 @@ __global__ void __launch_bounds__(TX *TY, MINB) kStencil3Q(const double *__restr
             if (lane == 0) left = ec;
             if (lane == TX - 1) right = ec;
             // (((((A[i-1] + A[j-1]) + A[k-1]) + A[k+1]) + A[j+1]) + A[i+1]) / 6, left to right
-            v0 = sf::q61_div6(sf::q61_add(
-                sf::q61_add(sf::q61_add(sf::q61_add(sf::q61_add(pmx, up.x), left), pcy), dn.x), ppx));
-            v1 = sf::q61_div6(sf::q61_add(
-                sf::q61_add(sf::q61_add(sf::q61_add(sf::q61_add(pmy, up.y), pcx), right), dn.y), ppy));
+            v0 = cell(pmx, up.x, left, pcy, dn.x, ppx);
+            v1 = cell(pmy, up.y, pcx, right, dn.y, ppy);
         } else {  // rare: a value outside the fixed-point range near this plane
             v0 = (jI && kI0) ? nativeCell(i, k) : 0.0;
             v1 = (jI && kI1) ? nativeCell(i, k + 1) : 0.0;
@@ -572,7 +585,8 @@ __global__ void __launch_bounds__(TX *TY, MINB) kStencil3Q(const double *__restr
             sm[cur ^ 1][hrIdx][lane] = make_ulonglong2(hpx, hpy);
         }
         sm[cur ^ 1][1 + ty][lane] = make_ulonglong2(ppx, ppy);
-        flags = ((flags << 1) | (__syncthreads_or(bad) ? 1u : 0u)) & 7u;
+        if (Q) flags = ((flags << 1) | (__syncthreads_or(bad) ? 1u : 0u)) & 7u;
+        else __syncthreads();
         cur ^= 1;
         pmx = pcx, pmy = pcy;
         pcx = ppx, pcy = ppy;
@@ -580,6 +594,16 @@ __global__ void __launch_bounds__(TX *TY, MINB) kStencil3Q(const double *__restr
         ec = ep, ep = eq;
         hpx = hqx, hpy = hqy;
     }
+}
+
+// nat of every den CTAs (by linear block index) native, the others fixed point
+template <int MINB>
+__global__ void __launch_bounds__(TX *TY, MINB) kStencil3Q(const double *__restrict__ A, double *Out, Box3 b,
+                                                             long p0, int ichunk, int nat, int den) {
+    __shared__ ulonglong2 sm[2][TY + 2][TX];
+    const unsigned cta = blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z);
+    if ((int)(cta % (unsigned)den) < nat) planes3<false>(A, Out, b, p0, ichunk, sm);
+    else planes3<true>(A, Out, b, p0, ichunk, sm);
 }
 
 struct St3Geom {
@@ -803,11 +827,13 @@ __global__ void kCopyOutside(const double *__restrict__ src, double *__restrict_
 // 3-D variants (stencil and fused alike): v < 12: v = 6 * (JT - 1) + N, N =
 // additions of a cell on the FP64 unit (0..5, the others on the integer pipe),
 // JT = rows per thread, two CTAs per SM; v = 12, 13: all additions native, one
-// row per thread, registers capped for three / four CTAs per SM; v = 14, 15,
-// 16: the q61 fixed-point stencil (kStencil3Q), registers capped for four /
-// three / two CTAs per SM (the fused entry point runs the update and then this
-// stencil into the second buffer: there is no one-pass q61 form)
-constexpr int V3Q = 14, V3 = 17;
+// row per thread, registers capped for three / four CTAs per SM; v = 14..21:
+// the q61 fixed-point stencil (kStencil3Q) with (CTAs per SM, native CTAs of
+// every den): 14 (4, 0 of 1), 15 (3, 0 of 1), 16 (4, 1 of 2), 17 (4, 1 of 3),
+// 18 (4, 2 of 5), 19 (3, 1 of 2), 20 (4, 1 of 4), 21 (4, 3 of 5) (the fused
+// entry point runs the update and then this stencil into the second buffer:
+// there is no one-pass q61 form)
+constexpr int V3Q = 14, V3 = 22;
 int jtOf3(int v) { return (v >= 6 && v < 12) ? 2 : 1; }
 bool isQ3(int v) { return v >= V3Q && v < V3; }
 // the fused entry point's extra variants: the two loops as two kernels (the
@@ -832,9 +858,11 @@ void launch3(int variant, const St3Geom &g, double *A, const double *B, double *
 #undef C3
     case 12: kStencil3<FUSED, 5, 1, 3><<<g.grid, blk, 0, s>>>(A, B, Out, b, g.p0, g.ichunk, items); break;
     case 13: kStencil3<FUSED, 5, 1, 4><<<g.grid, blk, 0, s>>>(A, B, Out, b, g.p0, g.ichunk, items); break;
-    case 14: if (!FUSED) kStencil3Q<4><<<g.grid, blk, 0, s>>>(A, Out, b, g.p0, g.ichunk); break;
-    case 15: if (!FUSED) kStencil3Q<3><<<g.grid, blk, 0, s>>>(A, Out, b, g.p0, g.ichunk); break;
-    case 16: if (!FUSED) kStencil3Q<2><<<g.grid, blk, 0, s>>>(A, Out, b, g.p0, g.ichunk); break;
+#define CQ(V, M, N, D) \
+    case V: if (!FUSED) kStencil3Q<M><<<g.grid, blk, 0, s>>>(A, Out, b, g.p0, g.ichunk, N, D); break;
+        CQ(14, 4, 0, 1) CQ(15, 3, 0, 1) CQ(16, 4, 1, 2) CQ(17, 4, 1, 3) CQ(18, 4, 2, 5) CQ(19, 3, 1, 2)
+        CQ(20, 4, 1, 4) CQ(21, 4, 3, 5)
+#undef CQ
     }
 }
 
@@ -1049,9 +1077,9 @@ __global__ void __launch_bounds__(256) kMaxPartials(const double *partials, long
 }
 
 // device address of noallocPartials on each device, looked up once per device
+// (a lookup races harmlessly with another: both store the same address)
 constexpr int MAX_DEVICES = 64;
-double *noallocAddr[MAX_DEVICES];
-bool noallocReady[MAX_DEVICES];
+std::atomic<double *> noallocAddr[MAX_DEVICES];
 
 }  // namespace
 
@@ -1062,7 +1090,8 @@ int dvmhgb_jac3d_update_noalloc(double *A, const double *B, const long st[3], co
     if (!A || !B || !epsDev || !st || !lo || !hi || !rows16(st, 3) || !aligned16(A) || !aligned16(B)) return -1;
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= MAX_DEVICES) return -3;
-    if (!noallocReady[dev]) {
+    double *partials = noallocAddr[dev].load(std::memory_order_acquire);
+    if (!partials) {
         // first call on this device: take the array's address with the device current
         void *p = nullptr;
         cudaError_t e = cudaGetSymbolAddress(&p, noallocPartials);
@@ -1071,8 +1100,8 @@ int dvmhgb_jac3d_update_noalloc(double *A, const double *B, const long st[3], co
                     cudaGetErrorString(e));
             return -3;
         }
-        noallocAddr[dev] = (double *)p;
-        noallocReady[dev] = true;
+        partials = (double *)p;
+        noallocAddr[dev].store(partials, std::memory_order_release);
     }
     UpdGeom g = updGeom(hi[0] - lo[0] + 1, hi[1] - lo[1] + 1, lo[2], hi[2]);
     if (!g.ok) return -1;
@@ -1084,7 +1113,6 @@ int dvmhgb_jac3d_update_noalloc(double *A, const double *B, const long st[3], co
         return -2;
     }
     cudaStream_t s = (cudaStream_t)stream;
-    double *partials = noallocAddr[dev];
     kUpdate<<<(unsigned)g.blocks, UPD_THREADS, 0, s>>>(A, B, st[0], st[1], lo[0], lo[1], lo[2], hi[2], g.nj, g.units,
                                                        g.nseg, g.p0, g.p1, partials, 1);
     kMaxPartials<<<1, 256, 0, s>>>(partials, g.blocks, epsDev);

@@ -33,6 +33,7 @@
 namespace dvmhgb {
 
 constexpr int MAXR = 7;  // maximum array/loop rank (the reference's MAX_ARRAY_RANK)
+constexpr int TUNE_NF = 24;  // features per tuner record (DVMHGB_TUNE_NF)
 
 // ---------------------------------------------------------------- errors
 
@@ -97,6 +98,7 @@ enum ObjKind : uint32_t {
     K_REGION = 0x5245474eu,
     K_LOOP = 0x4c4f4f50u,
     K_SPEC = 0x53504543u,
+    K_DECL = 0x4445434cu,
 };
 
 struct Obj {
@@ -140,6 +142,11 @@ struct Array : Obj {
     AlignMap align;  // set by dvmh_distribute_C / dvmh_align_C
     bool hostActual = true, devActual = false;
     DvmType *desc = nullptr;
+    // a regular variable of the program seen as an array (dvmh_variable_gen_header_C):
+    // the host copy is the program's own memory (neither pinned nor freed here) and
+    // the header is the runtime's
+    bool extHost = false;
+    DvmType ownHdr[MAXR + 3] = {};
     std::string name;
     const void *regMark = nullptr;  // the region this array was last registered in
     size_t regIdx = 0;              // and its entry there
@@ -163,6 +170,16 @@ struct Var : Obj {
     char *dev = nullptr;
     bool hostActual = true, devActual = false;
     std::string name;
+    DvmType hdr[4] = {};  // its rank-0 header (dvmh_variable_gen_header_C with rank 0): hdr[0] = this
+};
+
+// An array declared without its size (dvmh_array_declare_C); dvmh_array_alloc_C
+// turns it into an Array once the program allocates it.
+struct Decl : Obj {
+    Decl() : Obj(K_DECL) {}
+    int rank = 0;
+    DvmType typeSize = 0;
+    long ext[MAXR] = {}, shLo[MAXR] = {}, shHi[MAXR] = {};
 };
 
 struct Region;
@@ -252,6 +269,10 @@ struct SpecLoop : Obj {
     int block[3] = {0, 0, 0};
     int variant = -1;  // tuner's kernel variant, -1 = handler default
     int layout = -1;   // tuner's layout choice for autotransform (1 transform, 0 natural), -1 none
+    void *handler = nullptr;  // the handler running this execution (single, fused or batch)
+    uint64_t tkey = 0;        // the tuner's key of this loop shape and handler (0: no variant asked)
+    bool exploring = false;   // the variant is one the tuner had not timed yet
+    float vf[TUNE_NF] = {};   // features of the loop and the chosen variant
     std::vector<CudaRed> reds;
     std::vector<void *> scratch;  // device allocations owned by this execution
     std::vector<void *> hostScratch;  // pinned host allocations owned by this execution
@@ -329,6 +350,25 @@ void varH2D(Var *v);
 void varD2H(Var *v);
 void varForgetStaging(const Var *v);  // the variable is dropped: its pinned staging buffer too
 void fillDesc(Array *a);
+size_t maxDeviceElems();  // the most device elements of any live array with a device copy
+bool isLive(Obj *o, uint32_t kind);
+void trackObj(Obj *o);
+void untrackObj(Obj *o);
+void varDrop(Var *v);     // forget a variable, its device copy and the graphs that name it
+// a new array on the caller's descriptor, or on its own header for desc == null
+// (sizes per axis, shadow widths); no storage yet
+Array *arrayNew(DvmType desc[], int rank, DvmType typeSize, const long ext[], const long shLo[], const long shHi[]);
+// host storage: `external` (the program's memory) or a pinned buffer of the runtime
+void arrayAttachHost(Array *a, char *external);
+void arrayRelease(Array *a);  // free the array's buffers and the object (its descriptor is cleared)
+void arrayRetarget(Array *a, DvmType desc[]);  // the array is known by another descriptor from now on
+
+// ---------------------------------------------------------------- regular variables (rt_regular.cpp)
+
+// Regular (non-distributed) variables entered into data regions
+// (dvmh_data_enter_C / dvmh_data_exit_C) and their runtime forms.
+bool regularActual(const void *addr, bool toHost);  // get_actual / actual of a regular array; false if unknown
+void regularRegionEnd();  // data exit of the variables a region (or a loop outside regions) entered implicitly
 
 // ---------------------------------------------------------------- loops / batching (rt_loop.cpp)
 
@@ -361,9 +401,13 @@ void alignCompose(AlignMap &out, const AlignMap &target, const int axis[], const
 // ---------------------------------------------------------------- tuner (rt_tuner.cpp)
 
 bool tunerWants(const Loop *l);  // record timings of this loop shape
-int tunerVariant(const Loop *l, int nvariants, int dflt, bool bestOnly);
+// the variant for this execution; sets s->tkey, s->exploring and s->vf
+int tunerVariant(SpecLoop *s, int nvariants, int dflt, const float *desc, int ndesc, bool bestOnly);
 void tunerPick(Loop *l, int block[3], int *variant);
-void tunerRecord(const Loop *l, const int block[3], int variant, double seconds);
+// a timed execution of a variant-choosing handler
+void tunerRecord(uint64_t key, int variant, bool exploring, const float *vf, double seconds);
+bool tunerExploring();  // a flush must run without capture: some loop shape still tries variants
+void tunerFlushed();    // an uncaptured flush ran
 int tunerLayout(const Loop *l, bool explore);  // 1: the reference's transform, 0: natural
 void tunerRecordLayout(const Loop *l, int choice, double seconds);
 

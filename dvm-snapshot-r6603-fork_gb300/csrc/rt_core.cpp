@@ -136,6 +136,8 @@ static void loadSettings() {
 static void track(Obj *o) { liveObjs.insert(o); }
 static void untrack(Obj *o) { liveObjs.erase(o); }
 bool isLive(Obj *o, uint32_t kind) { return o && liveObjs.count(o) && o->kind == kind; }
+void trackObj(Obj *o) { track(o); }
+void untrackObj(Obj *o) { untrack(o); }
 
 Array *arrayOf(const DvmType desc[], const char *what) {
     GB_CHECK(desc, "NULL descriptor passed to %s", what);
@@ -178,6 +180,20 @@ static void dropVar(Var *v) {
     delete v;
 }
 
+void varDrop(Var *v) { dropVar(v); }
+
+// A variable known from an earlier region is forgotten because the program
+// registers other memory over it.  Its device copy may not hold the only
+// current value: the program must have read it back (get_actual) or ended its
+// data region first.  The reference reports a changed or overlapping regular
+// variable as an error too (rts/dvmh/dvmh2.cpp:1794-1830).
+static void checkForgettable(const Var *v, const char *what, const void *addr) {
+    GB_CHECK(!v->dev || v->hostActual,
+             "%s at %p: the variable '%s' registered there by an earlier region (%zu bytes at %p) has its only "
+             "current value on the device; read it back (get_actual) before registering other memory over it",
+             what, addr, v->name.c_str(), v->size, (const void *)v->addr);
+}
+
 static bool inCurrentRegion(const Var *v) {
     if (st.curRegion)
         for (auto &rv : st.curRegion->vars)
@@ -200,6 +216,7 @@ static void dropOverlaps(const char *lo, const char *hi, const Var *keep) {
     for (Var *o : stale) {
         GB_CHECK(!inCurrentRegion(o), "variable at %p overlaps the variable '%s' registered in this region",
                  (const void *)lo, o->name.c_str());
+        checkForgettable(o, "a variable overlapping it is registered", lo);
         dropVar(o);
     }
 }
@@ -226,6 +243,7 @@ Var *varGet(const void *addr, size_t size) {
         // a different extent at an address known from an earlier region: the program's
         // memory holds a new variable there (an allocation reused), so the old one is
         // forgotten with the others it overlaps; keeping it would copy its old size back
+        checkForgettable(v, "a variable of another size is registered", addr);
     }
     dropOverlaps(lo, hi, nullptr);
     Var *v = new Var();
@@ -278,18 +296,25 @@ static void layout(Array *a) {
     a->delems = (size_t)c;
 }
 
-static void allocateHost(Array *a) {
+void arrayAttachHost(Array *a, char *external) {
     if (a->host)
         return;
     layout(a);
-    size_t bytes = std::max<size_t>(a->hostBytes(), 16);
-    a->host = (char *)hostAlloc(bytes);
-    memset(a->host, 0, bytes);
+    if (external) {
+        a->host = external;
+        a->extHost = true;
+    } else {
+        size_t bytes = std::max<size_t>(a->hostBytes(), 16);
+        a->host = (char *)hostAlloc(bytes);
+        memset(a->host, 0, bytes);
+    }
     a->distributed = true;
     a->hostActual = true;
     a->devActual = false;
     fillDesc(a);
 }
+
+static void allocateHost(Array *a) { arrayAttachHost(a, nullptr); }
 
 void ensureDevBuffer(Array *a) {
     GB_CHECK(a->distributed, "array '%s' is used before it is distributed or aligned", a->name.c_str());
@@ -316,6 +341,13 @@ void ensureHostActual(Array *a) {
         copyD2H(a);
         a->hostActual = true;
     }
+}
+
+size_t maxDeviceElems() {
+    size_t m = 0;
+    for (Obj *o : liveObjs)
+        if (o->kind == K_ARRAY && ((Array *)o)->dev) m = std::max(m, ((Array *)o)->delems);
+    return m;
 }
 
 // ---------------------------------------------------------------- helpers
@@ -373,11 +405,13 @@ void dvmh_init_C(DvmType flags, int *pArgc, char ***pArgv) {
     deviceInit();
     st.inited = true;
     logmsg(LOG_INFO, "initialised on %s (%d SMs), mode %d", gpu.prop.name, gpu.smCount, settings.mode);
+    DvmhModuleInitializer::executeInit();  // data enter of the translation units' global variables
 }
 
 void dvmh_exit_C(DvmType exitCode) {
     if (st.inited) {
         queueFlush();
+        DvmhModuleInitializer::executeFinish();  // data exit of the global variables
         streamSync();
         loopsAtExit();
     }
@@ -400,13 +434,16 @@ void dvmh_barrier(void) {
 
 // ---------------------------------------------------------------- arrays, templates, distribution
 
-void dvmh_array_create_C(DvmType dvmDesc[], DvmType rank, DvmType typeSize, ...) {
-    GB_CHECK(st.inited, "LibDVMH is not initialized");
-    GB_CHECK(!st.curRegion && !st.curLoop, "dvmh_array_create is not allowed in a region or a parallel loop");
-    GB_CHECK(dvmDesc, "NULL descriptor passed to dvmh_array_create");
-    GB_CHECK(rank > 0 && rank <= MAXR, "array rank must be in 1..%d (got %ld)", MAXR, (long)rank);
+}  // extern "C"
+
+namespace dvmhgb {
+
+Array *arrayNew(DvmType dvmDesc[], int rank, DvmType typeSize, const long ext[], const long shLo[],
+                const long shHi[]) {
+    GB_CHECK(rank > 0 && rank <= MAXR, "array rank must be in 1..%d (got %d)", MAXR, rank);
     Array *a = new Array();
-    a->rank = (int)rank;
+    if (!dvmDesc) dvmDesc = a->ownHdr;  // the runtime's own header (a regular variable's array form)
+    a->rank = rank;
     if (typeSize <= 0) {
         a->dtype = (int)-typeSize;
         a->esize = dvmhgb::typeSize(a->dtype);
@@ -414,20 +451,60 @@ void dvmh_array_create_C(DvmType dvmDesc[], DvmType rank, DvmType typeSize, ...)
     } else {
         a->esize = (size_t)typeSize;
     }
-    va_list ap;
-    va_start(ap, typeSize);
-    for (int i = 0; i < a->rank; i++) {
-        a->ext[i] = (long)va_arg(ap, DvmType);
-        a->shLo[i] = (long)va_arg(ap, DvmType);
-        a->shHi[i] = (long)va_arg(ap, DvmType);
+    for (int i = 0; i < rank; i++) {
+        a->ext[i] = ext[i];
+        a->shLo[i] = shLo[i];
+        a->shHi[i] = shHi[i];
         GB_CHECK(a->ext[i] > 0, "non-positive size %ld of array on axis %d", a->ext[i], i + 1);
         GB_CHECK(a->shLo[i] >= 0 && a->shHi[i] >= 0, "negative shadow width on axis %d", i + 1);
     }
-    va_end(ap);
     a->desc = dvmDesc;
     dvmDesc[0] = (DvmType)a;
     track(a);
     arrayDescs[dvmDesc]++;
+    return a;
+}
+
+void arrayRelease(Array *a) {
+    queueFlush();
+    streamSync();
+    graphsForget(a);
+    if (a->dev) devFree(a->dev);
+    if (a->devAlt) devFree(a->devAlt);
+    if (a->host && !a->extHost) hostFree(a->host);
+    untrack(a);
+    if (--arrayDescs[a->desc] <= 0) arrayDescs.erase(a->desc);
+    a->desc[0] = 0;
+    delete a;
+}
+
+void arrayRetarget(Array *a, DvmType desc[]) {
+    if (--arrayDescs[a->desc] <= 0) arrayDescs.erase(a->desc);
+    a->desc = desc;
+    arrayDescs[desc]++;
+    if (a->host) fillDesc(a);
+    else desc[0] = (DvmType)a;
+}
+
+}  // namespace dvmhgb
+
+extern "C" {
+
+void dvmh_array_create_C(DvmType dvmDesc[], DvmType rank, DvmType typeSize, ...) {
+    GB_CHECK(st.inited, "LibDVMH is not initialized");
+    GB_CHECK(!st.curRegion && !st.curLoop, "dvmh_array_create is not allowed in a region or a parallel loop");
+    GB_CHECK(dvmDesc, "NULL descriptor passed to dvmh_array_create");
+    GB_CHECK(rank > 0 && rank <= MAXR, "array rank must be in 1..%d (got %ld)", MAXR, (long)rank);
+    long ext[MAXR], shLo[MAXR], shHi[MAXR];
+    va_list ap;
+    va_start(ap, typeSize);
+    for (int i = 0; i < rank; i++) {
+        ext[i] = (long)va_arg(ap, DvmType);
+        shLo[i] = (long)va_arg(ap, DvmType);
+        shHi[i] = (long)va_arg(ap, DvmType);
+    }
+    va_end(ap);
+    arrayNew(dvmDesc, (int)rank, typeSize, ext, shLo, shHi);
 }
 
 void dvmh_template_create_C(DvmType dvmDesc[], DvmType rank, ...) {
@@ -500,16 +577,10 @@ void dvmh_align_C(DvmType dvmDesc[], const DvmType templDesc[], DvmType templRan
 void dvmh_array_free_C(DvmType dvmDesc[]) {
     Array *a = arrayOf(dvmDesc, "dvmh_array_free");
     GB_CHECK(!st.curRegion, "dvmh_array_free inside a region");
-    queueFlush();
-    streamSync();
-    graphsForget(a);
-    if (a->dev) devFree(a->dev);
-    if (a->devAlt) devFree(a->devAlt);
-    if (a->host) hostFree(a->host);
-    untrack(a);
-    if (--arrayDescs[a->desc] <= 0) arrayDescs.erase(a->desc);
+    GB_CHECK(!a->extHost, "dvmh_array_free: '%s' is a regular variable of the program (it leaves the runtime at "
+             "dvmh_data_exit)", a->name.c_str());
+    arrayRelease(a);
     dvmDesc[0] = 0;
-    delete a;
 }
 
 void dvmh_delete_object_(DvmType dvmDesc[]) {
@@ -616,7 +687,10 @@ void dvmh_get_actual_variable2_(void *addr) {
     GB_PROF("dvmh_get_actual_variable2_");
     if (!st.inited) return;
     auto it = st.vars.find((const char *)addr);
-    if (it == st.vars.end()) return;  // unknown variables are always current on the host
+    if (it == st.vars.end()) {
+        regularActual(addr, true);  // a regular array; other unknown variables are current on the host
+        return;
+    }
     Var *v = it->second;
     if (!v->hostActual) {
         varD2H(v);
@@ -628,7 +702,10 @@ void dvmh_actual_variable2_(const void *addr) {
     GB_PROF("dvmh_actual_variable2_");
     if (!st.inited) return;
     auto it = st.vars.find((const char *)addr);
-    if (it == st.vars.end()) return;
+    if (it == st.vars.end()) {
+        regularActual(addr, false);
+        return;
+    }
     Var *v = it->second;
     v->hostActual = true;
     v->devActual = false;
@@ -738,11 +815,26 @@ static Region *regionOf(DvmType ref, const char *what) {
     return r;
 }
 
+static void regionAddVar(Region *r, Var *v, long intent, const char *varName) {
+    if (varName && v->name.empty()) v->name = varName;
+    for (auto &rv : r->vars)
+        if (rv.var == v) {
+            rv.intent |= intent;
+            return;
+        }
+    r->vars.push_back({v, intent});
+}
+
 void dvmh_region_register_array_C(DvmType curRegion, DvmType intent, const DvmType dvmDesc[], const char varName[]) {
     GB_PROF("dvmh_region_register_array_C");
     Region *r = regionOf(curRegion, "dvmh_region_register_array");
+    GB_CHECK(dvmDesc, "NULL header passed to dvmh_region_register_array");
     Obj *o = (Obj *)dvmDesc[0];
     if (isLive(o, K_TEMPLATE)) return;
+    if (isLive(o, K_VAR)) {  // a scalar regular variable (its rank-0 header)
+        regionAddVar(r, (Var *)o, (long)intent, varName);
+        return;
+    }
     Array *a = arrayOf(dvmDesc, "dvmh_region_register_array");
     if (varName && a->name.empty()) a->name = varName;
     if (a->regMark == r && a->regIdx < r->arrays.size() && r->arrays[a->regIdx].arr == a) {
@@ -767,14 +859,7 @@ void dvmh_region_register_scalar_C(DvmType curRegion, DvmType intent, const void
     GB_PROF("dvmh_region_register_scalar_C");
     Region *r = regionOf(curRegion, "dvmh_region_register_scalar");
     GB_CHECK(addr && typeSize > 0, "invalid scalar registration");
-    Var *v = varGet(addr, (size_t)typeSize);
-    if (varName && v->name.empty()) v->name = varName;
-    for (auto &rv : r->vars)
-        if (rv.var == v) {
-            rv.intent |= (long)intent;
-            return;
-        }
-    r->vars.push_back({v, (long)intent});
+    regionAddVar(r, varGet(addr, (size_t)typeSize), (long)intent, varName);
 }
 
 void dvmh_region_execute_on_targets_C(DvmType curRegion, DvmType deviceTypes) {
@@ -814,6 +899,7 @@ void dvmh_region_end_C(DvmType curRegion) {
     untrack(r);
     st.curRegion = nullptr;
     delete r;
+    regularRegionEnd();
 }
 
 // ---------------------------------------------------------------- extension API

@@ -27,7 +27,6 @@
 namespace dvmhgb {
 
 extern dvmhgb_stats_t stats;
-bool isLive(Obj *o, uint32_t kind);
 bool isArrayDesc(const void *p);
 
 // ---------------------------------------------------------------- rules
@@ -55,6 +54,9 @@ struct TimedExec {
     int variant;
     int layout;    // the tuner's layout choice in this execution, -1 none
     bool inGraph;  // owned by a cached graph (reused on every replay)
+    uint64_t tkey;   // the tuner's key when the handler chose a variant, else 0
+    bool exploring;  // that variant had not been timed before
+    float vf[TUNE_NF];
 };
 struct TimingTotal {
     double ms = 0;
@@ -77,7 +79,7 @@ void collectTimings() {  // called after a stream synchronisation
             TimingTotal &tt = timingTotals[t.func];
             tt.ms += ms;
             tt.count++;
-            if (t.loopCopy) tunerRecord(t.loopCopy, t.block, t.variant, ms * 1e-3);
+            if (t.tkey) tunerRecord(t.tkey, t.variant, t.exploring, t.vf, ms * 1e-3);
             if (t.loopCopy && t.layout >= 0) tunerRecordLayout(t.loopCopy, t.layout, ms * 1e-3);
         }
         if (!t.inGraph) {
@@ -122,7 +124,6 @@ static std::list<CachedGraph> graphCache;  // most recently used first
 bool queueBusy() { return !queue.empty(); }
 
 static void deleteLoop(Loop *l) {
-    extern void untrackObj(Obj *);
     untrackObj(l);
     delete l;
 }
@@ -146,12 +147,16 @@ static SpecLoop *specOf(DvmType ref, const char *what) {
     return s;
 }
 
+// the reference's default block for `rank` free block dimensions (loop.cpp:1464-1485)
 static void defaultBlock(int rank, int b[3]) {
     b[0] = b[1] = b[2] = 1;
     if (rank >= 3) { b[0] = 32; b[1] = 4; b[2] = 2; }
     else if (rank == 2) { b[0] = 32; b[1] = 8; }
     else if (rank == 1) { b[0] = 256; }
 }
+
+// block dimensions a loop may use: one fewer with dependences (loop.h:257, loop.cpp:2136)
+static int freeBlockDims(int loopRank, bool hasDeps) { return loopRank - (hasDeps ? 1 : 0); }
 
 // arrays a loop's handler can touch: its array-descriptor parameters
 static void loopArrays(const Loop *l, std::vector<const void *> &out) {
@@ -198,7 +203,6 @@ static bool deferFolds = false;
 static std::vector<FoldJob> deferred;
 
 static SpecLoop *newSpec(Loop *l) {
-    extern void trackObj(Obj *);
     SpecLoop *s = new SpecLoop();
     s->loop = l;
     s->device = 1;
@@ -208,7 +212,6 @@ static SpecLoop *newSpec(Loop *l) {
 }
 
 static void finishSpec(SpecLoop *s) {
-    extern void untrackObj(Obj *);
     Loop *l = s->loop;
     for (size_t i = 0; i < l->reds.size(); i++) {
         bool done = false;
@@ -246,11 +249,22 @@ static void timeBegin(TimedExec &t, void *func) {
     t.variant = -1;
     t.layout = -1;
     t.inGraph = ctx.capturing;
+    t.tkey = 0;
+    t.exploring = false;
     if (ctx.capturing) return;
     t.e0 = newEvent();
     t.e1 = newEvent();
     GB_CUDA(cudaEventRecord(t.e0, gpu.stream));
 }
+// the tuner's choice made in this execution (graph replays are not recorded)
+static void timeTuned(TimedExec &t, const SpecLoop *s) {
+    if (!s->tkey || ctx.capturing) return;
+    t.tkey = s->tkey;
+    t.variant = s->variant;
+    t.exploring = s->exploring;
+    memcpy(t.vf, s->vf, sizeof t.vf);
+}
+
 static void timeEnd(TimedExec &t) {
     if (ctx.capturing) {
         if (ctx.times) ctx.times->push_back(t);
@@ -287,6 +301,7 @@ static void launchGraph(CachedGraph &g) {
 
 static void runSingle(Loop *l) {
     SpecLoop *s = newSpec(l);
+    s->handler = (void *)l->cuda.func;
     DvmType ref = (DvmType)s;
     stats.handler_calls++;
     TimedExec t;
@@ -299,7 +314,8 @@ static void runSingle(Loop *l) {
         memcpy(t.block, s->block, sizeof t.block);
         t.variant = s->variant;
         t.layout = s->layout;
-        t.loopCopy = tunerWants(l) ? new Loop(*l) : nullptr;
+        t.loopCopy = (tunerWants(l) && s->layout >= 0) ? new Loop(*l) : nullptr;
+        timeTuned(t, s);
         timeEnd(t);
     }
     finishSpec(s);
@@ -307,6 +323,7 @@ static void runSingle(Loop *l) {
 
 static void runFused(DvmHandlerFunc fused, Loop *a, Loop *b) {
     SpecLoop *sa = newSpec(a), *sb = newSpec(b);
+    sa->handler = sb->handler = (void *)fused;
     DvmType refs[2] = {(DvmType)sa, (DvmType)sb};
     void *params[80];
     int n = 0;
@@ -320,7 +337,10 @@ static void runFused(DvmHandlerFunc fused, Loop *a, Loop *b) {
         CallScope call;
         callWithParams(fused, refs, n, params);
     }
-    if (timingOn) timeEnd(t);
+    if (timingOn) {
+        timeTuned(t, sa->tkey ? sa : sb);
+        timeEnd(t);
+    }
     finishSpec(sa);
     finishSpec(sb);
 }
@@ -330,6 +350,7 @@ static void runBatch(DvmHandlerFunc batched, const std::vector<Loop *> &group) {
     std::vector<SpecLoop *> specs;
     for (Loop *l : group) {
         specs.push_back(newSpec(l));
+        specs.back()->handler = (void *)batched;
         refs.push_back((DvmType)specs.back());
     }
     stats.handler_calls++;
@@ -345,7 +366,10 @@ static void runBatch(DvmHandlerFunc batched, const std::vector<Loop *> &group) {
     deferFolds = false;
     if (!deferred.empty()) launchRedFoldBatch(deferred, gpu.stream, specs[0]->scratch, specs[0]->hostScratch);
     deferred.clear();
-    if (timingOn) timeEnd(t);
+    if (timingOn) {
+        timeTuned(t, specs[0]);
+        timeEnd(t);
+    }
     for (SpecLoop *s : specs) finishSpec(s);
 }
 
@@ -476,6 +500,14 @@ void queueFlush() {
     std::vector<Loop *> q;
     q.swap(queue);
     stats.flushes++;
+    if (settings.tuneMode && tunerExploring()) {
+        // variants are still being tried: run the queue as it is, each handler timed on its own
+        runQueued(q);
+        tunerFlushed();
+        for (Loop *l : q) deleteLoop(l);
+        if (settings.syncEachLoop) streamSync();
+        return;
+    }
     std::vector<uint64_t> sig = signature(q);
     uint64_t key = hashSig(sig);
     for (auto it = graphCache.begin(); it != graphCache.end(); ++it) {
@@ -564,9 +596,6 @@ static void afterReductions(Loop *l, bool toHost) {
 using namespace dvmhgb;
 
 namespace dvmhgb {
-extern std::unordered_set<Obj *> liveObjs;
-void trackObj(Obj *o) { liveObjs.insert(o); }
-void untrackObj(Obj *o) { liveObjs.erase(o); }
 }  // namespace dvmhgb
 
 extern "C" {
@@ -849,33 +878,54 @@ void dvmh_loop_fill_local_part_C(DvmType curLoop, const DvmType dvmDesc[], DvmTy
 
 DvmType dvmh_loop_guess_index_type_C(DvmType curLoop) {
     Loop *l = specOf(curLoop, "dvmh_loop_guess_index_type")->loop;
-    // int when every element of every region array is addressable with int
+    // int when every element of the arrays the loop can reach is addressable
+    // with int: the region's arrays, or (a loop outside regions) every array
+    // with a device copy (dvmh2.cpp:4110-4137)
     size_t maxElems = 0;
     if (l->region)
         for (auto &ra : l->region->arrays) maxElems = std::max(maxElems, ra.arr->delems);
+    else
+        maxElems = maxDeviceElems();
     return maxElems < (size_t)2147483647 ? rt_INT : rt_LLONG;
 }
+
+static const char *const pickBlockErrors[] = {
+    "",
+    "Setting CUDA block with more dimensions than the parallel loop has (minus 1 in case of dependency) is prohibited",
+    "Block size on an axis is bigger than the device can handle",
+    "Block size is bigger than the device can handle",
+    "Shared memory amount is insufficient for the CUDA block",
+    "Register count is insufficient for the CUDA block",
+};
 
 void dvmh_loop_cuda_get_config_C(DvmType curLoop, DvmType sharedPerThread, DvmType regsPerThread, void *inOutThreads,
                                  void *outStream, DvmType *outSharedPerBlock) {
     SpecLoop *s = specOf(curLoop, "dvmh_loop_cuda_get_config");
     Loop *l = s->loop;
-    (void)regsPerThread;
     dim3 *t = (dim3 *)inOutThreads;
-    int b[3];
-    if (l->userBlock) {
-        b[0] = l->cudaBlock[0];
-        b[1] = l->cudaBlock[1];
-        b[2] = l->cudaBlock[2];
-    } else if (t && t->x >= 1 && t->y >= 1 && t->z >= 1) {
+    int b[3] = {0, 0, 0};
+    if (t && t->x >= 1 && t->y >= 1 && t->z >= 1) {  // the handler's own default
         b[0] = (int)t->x;
         b[1] = (int)t->y;
         b[2] = (int)t->z;
-    } else {
-        defaultBlock(l->rank, b);
     }
-    if (!l->userBlock && settings.tuneMode) tunerPick(l, b, &s->variant);
+    if (l->userBlock) memcpy(b, l->cudaBlock, sizeof b);
+    if (!l->userBlock && settings.tuneMode) {
+        if (b[0] < 1) defaultBlock(std::min(3, freeBlockDims(l->rank, l->depMask != 0)), b);
+        tunerPick(l, b, &s->variant);
+    }
     if (sharedPerThread < 0) sharedPerThread = 0;
+    dvmhgb_cuda_limits_t lim;
+    for (int i = 0; i < 3; i++) lim.maxBlockSize[i] = gpu.prop.maxThreadsDim[i];
+    lim.maxThreadsPerBlock = gpu.prop.maxThreadsPerBlock;
+    lim.sharedPerBlock = (long)gpu.prop.sharedMemPerBlock;
+    lim.regsPerBlock = (long)gpu.prop.regsPerBlock;
+    lim.warpSize = gpu.prop.warpSize;
+    lim.maxRegsPerThread = 255;
+    const int err = dvmhgb_pick_block(l->rank, l->depMask != 0, l->userBlock, b, (long)sharedPerThread,
+                                      (long)regsPerThread, &lim);
+    GB_CHECK(err == 0, "%s: block (%d, %d, %d), %ld bytes of shared memory and %ld registers per thread",
+             pickBlockErrors[err], b[0], b[1], b[2], (long)sharedPerThread, (long)regsPerThread);
     memcpy(s->block, b, sizeof b);
     if (t) {
         t->x = (unsigned)b[0];
@@ -884,6 +934,38 @@ void dvmh_loop_cuda_get_config_C(DvmType curLoop, DvmType sharedPerThread, DvmTy
     }
     if (outStream) *(cudaStream_t *)outStream = s->stream;
     if (outSharedPerBlock) *outSharedPerBlock = (DvmType)b[0] * b[1] * b[2] * sharedPerThread;
+}
+
+int dvmhgb_pick_block(int loopRank, int hasDeps, int userBlock, int block[3], long sharedPerThread,
+                      long regsPerThread, const dvmhgb_cuda_limits_t *lim) {
+    GB_CHECK(block && lim, "NULL argument to dvmhgb_pick_block");
+    const int maxBlockRank = freeBlockDims(loopRank, hasDeps != 0);
+    if (!(block[0] >= 1 && block[1] >= 1 && block[2] >= 1)) defaultBlock(std::min(3, maxBlockRank), block);
+    int blockRank = 3;
+    while (blockRank > 0 && block[blockRank - 1] == 1) blockRank--;
+    if (blockRank > maxBlockRank) return 1;
+    for (int i = 0; i < 3; i++)
+        if (block[i] > lim->maxBlockSize[i]) return 2;
+    if ((long)block[0] * block[1] * block[2] > lim->maxThreadsPerBlock) return 3;
+    // a block that needs more per-block resources than a block can have: one
+    // dimension of at most 256 threads, a multiple of the warp size
+    auto shrink = [&](long have, long perThread) {
+        long n = std::min(256L, have / perThread);
+        n = n / lim->warpSize * lim->warpSize;
+        block[0] = maxBlockRank >= 1 ? (int)std::max(1L, n) : 1;
+        block[1] = block[2] = 1;
+    };
+    if (sharedPerThread < 0) sharedPerThread = 0;
+    if (sharedPerThread > 0 && (long)block[0] * block[1] * block[2] * sharedPerThread > lim->sharedPerBlock) {
+        if (userBlock) return 4;
+        shrink(lim->sharedPerBlock, sharedPerThread);
+    }
+    if (regsPerThread <= 0) regsPerThread = lim->maxRegsPerThread;
+    if ((long)block[0] * block[1] * block[2] * regsPerThread > lim->regsPerBlock) {
+        if (userBlock) return 5;
+        shrink(lim->regsPerBlock, regsPerThread);
+    }
+    return 0;
 }
 
 // ---------------------------------------------------------------- reductions inside handlers
@@ -1072,18 +1154,22 @@ void dvmhgb_register_batch(DvmHandlerFunc single, DvmHandlerFunc batched) {
 
 void dvmhgb_force_variant(int v) { forcedVariant = v < 0 ? -1 : v; }
 
-int dvmhgb_loop_variant(DvmType loopRef, int nvariants, int dflt) {
+int dvmhgb_loop_variant_desc(DvmType loopRef, int nvariants, int dflt, const float *desc, int ndesc) {
     SpecLoop *s = specOf(loopRef, "dvmhgb_loop_variant");
     GB_CHECK(nvariants >= 1 && dflt >= 0 && dflt < nvariants, "invalid variant request");
+    GB_CHECK(ndesc >= 0 && ndesc <= DVMHGB_VARIANT_NDESC && (ndesc == 0 || desc), "invalid variant description");
     const int forced = forcedVariant;
     int v = s->variant >= 0 ? s->variant : dflt;
     // online tuning explores only in immediate execution (a captured graph keeps its choice)
-    if (settings.tuneMode && !ctx.capturing) v = tunerVariant(s->loop, nvariants, dflt, false);
-    else if (settings.tuneMode) v = tunerVariant(s->loop, nvariants, dflt, true);
+    if (settings.tuneMode && forced < 0) v = tunerVariant(s, nvariants, dflt, desc, ndesc, ctx.capturing);
     if (forced >= 0) v = forced;
     v = v < nvariants ? v : nvariants - 1;
     s->variant = v;
     return v;
+}
+
+int dvmhgb_loop_variant(DvmType loopRef, int nvariants, int dflt) {
+    return dvmhgb_loop_variant_desc(loopRef, nvariants, dflt, nullptr, 0);
 }
 
 void *dvmhgb_loop_scratch(DvmType loopRef, DvmType bytes) {

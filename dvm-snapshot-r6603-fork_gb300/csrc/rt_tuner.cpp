@@ -17,6 +17,7 @@
 //     many FP64 operations run on the FP64 unit), chosen online per loop.
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <map>
 #include <unordered_map>
@@ -28,6 +29,7 @@
 namespace dvmhgb {
 
 extern dvmhgb_stats_t stats;
+static float lg(double v) { return (float)std::log2(v > 1 ? v : 1); }
 
 // ---------------------------------------------------------------- timing database
 
@@ -41,18 +43,61 @@ static std::vector<Record> db;
 
 // ---------------------------------------------------------------- online variant tuning of ABI loops
 
+static bool variantModelReady();
+static void rankByVariantModel(const std::vector<std::vector<float>> &feats, std::vector<int> &order);
+
+//
+// Per loop shape and handler (the tuner's key): the fastest seconds seen for
+// each variant.  Exhaustive tuning hands out every untried variant in turn;
+// model-guided tuning ranks the variants by the variant model (features of
+// the loop and of each variant's description) and hands out only the first
+// floor(frac x nvariants) of that order (none: the first is kept untried).
+// Afterwards the fastest variant timed is kept; before anything is timed, the
+// default (exhaustive) or the model's first choice.
+
 struct VariantState {
     std::map<int, double> best;  // variant -> best seconds seen
     int nvariants = 0;
-    int pending = -1;
+    int chosen = -1;
+    std::vector<int> order;      // model-guided: variants fastest first by the model
+    int explore = -1;            // variants to try (-1: all)
+    int explored = 0;            // executions that tried an untried variant
+    double exploreSeconds = 0;   // their summed time
+    void *handler = nullptr;
 };
 static std::unordered_map<uint64_t, VariantState> vstate;
+static std::vector<uint64_t> vorder;  // keys in the order first seen
+static long uncapturedFlushes = 0;    // flushes run eagerly since tuning was reset
+static std::vector<Record> vdb;       // the variant database
 
-static uint64_t loopKey(const Loop *l) {
-    uint64_t h = (uint64_t)l->cuda.func * 0x9E3779B97F4A7C15ull;
+static double tuneFrac() {
+    static double f = -1;
+    if (f < 0) {
+        const char *e = getenv("DVMH_GB_TUNE_FRAC");
+        f = e ? atof(e) : 0.1;
+        if (f < 0) f = 0;
+    }
+    return f;
+}
+
+static uint64_t loopKey(const void *handler, const Loop *l) {
+    uint64_t h = (uint64_t)handler * 0x9E3779B97F4A7C15ull;
     for (int i = 0; i < l->rank; i++) h = (h ^ (uint64_t)(l->hi[i] - l->lo[i] + 1)) * 1099511628211ull;
     h ^= (uint64_t)l->depMask;
-    return h;
+    return h ? h : 1;
+}
+
+// features of a loop and one variant's description
+static void variantFeatures(const Loop *l, const float *desc, int ndesc, float *f) {
+    memset(f, 0, sizeof(float) * TUNE_NF);
+    double total = 1;
+    for (int a = 0; a < l->rank; a++) total *= (double)(l->hi[a] - l->lo[a] + 1);
+    f[0] = (float)l->rank;
+    for (int a = 0; a < 4 && a < l->rank; a++) f[1 + a] = lg((double)(l->hi[a] - l->lo[a] + 1));
+    f[5] = lg(total);
+    f[6] = (float)(l->depMask != 0);
+    f[7] = (float)l->reds.size();
+    for (int d = 0; d < ndesc && 8 + d < TUNE_NF; d++) f[8 + d] = desc[d];
 }
 
 bool tunerWants(const Loop *l) { return settings.tuneMode != 0 && l->hasCuda; }
@@ -63,30 +108,91 @@ void tunerPick(Loop *l, int block[3], int *variant) {
     (void)variant;  // the variant is chosen when the handler asks (dvmhgb_loop_variant)
 }
 
-int tunerVariant(const Loop *l, int nvariants, int dflt, bool bestOnly) {
-    if (settings.tuneMode == 0) return dflt;
-    VariantState &vs = vstate[loopKey(l)];
-    vs.nvariants = nvariants;
-    if (!bestOnly)
-        for (int v = 0; v < nvariants; v++)
-            if (!vs.best.count(v)) return v;  // exhaustive: untried variants first
-    if (vs.best.empty()) return dflt;
-    int bestV = dflt;
-    double bestT = 1e300;
-    for (auto &kv : vs.best)
-        if (kv.second < bestT) {
-            bestT = kv.second;
-            bestV = kv.first;
-        }
-    return bestV;
+static bool explorationDone(const VariantState &vs) {
+    if (vs.explore >= 0) {
+        for (int i = 0; i < vs.explore; i++)
+            if (!vs.best.count(vs.order[i])) return false;
+        return true;
+    }
+    return (int)vs.best.size() >= vs.nvariants;
 }
 
-void tunerRecord(const Loop *l, const int block[3], int variant, double seconds) {
-    (void)block;
+int tunerVariant(SpecLoop *s, int nvariants, int dflt, const float *desc, int ndesc, bool bestOnly) {
+    const Loop *l = s->loop;
+    const uint64_t key = loopKey(s->handler ? s->handler : (void *)l->cuda.func, l);
+    auto found = vstate.find(key);
+    if (found == vstate.end()) vorder.push_back(key);
+    VariantState &vs = vstate[key];
+    vs.handler = s->handler;
+    if (vs.nvariants != nvariants) {
+        vs = VariantState();
+        vs.handler = s->handler;
+        vs.nvariants = nvariants;
+        if (settings.tuneMode == 2 && ndesc > 0 && variantModelReady()) {
+            std::vector<std::vector<float>> feats(nvariants, std::vector<float>(TUNE_NF));
+            for (int v = 0; v < nvariants; v++) variantFeatures(l, desc + (size_t)v * ndesc, ndesc, feats[v].data());
+            rankByVariantModel(feats, vs.order);
+            vs.explore = (int)std::floor(tuneFrac() * nvariants);
+        }
+    }
+    int v = -1;
+    bool exploring = false;
+    if (!bestOnly && !explorationDone(vs)) {
+        if (vs.explore >= 0) {
+            for (int i = 0; i < vs.explore && v < 0; i++)
+                if (!vs.best.count(vs.order[i])) v = vs.order[i];
+        } else {
+            for (int c = 0; c < nvariants && v < 0; c++)
+                if (!vs.best.count(c)) v = c;
+        }
+        exploring = v >= 0;
+    }
+    if (v < 0) {
+        double bestT = 1e300;
+        for (auto &kv : vs.best)
+            if (kv.second < bestT) {
+                bestT = kv.second;
+                v = kv.first;
+            }
+        if (v < 0) v = vs.explore >= 0 ? vs.order[0] : dflt;
+    }
+    vs.chosen = v;
+    s->tkey = key;
+    s->exploring = exploring;
+    variantFeatures(l, desc ? desc + (size_t)v * ndesc : nullptr, desc ? ndesc : 0, s->vf);
+    s->vf[TUNE_NF - 1] = desc ? s->vf[TUNE_NF - 1] : (float)v;  // no description: the variant number itself
+    return v;
+}
+
+void tunerRecord(uint64_t key, int variant, bool exploring, const float *vf, double seconds) {
     if (variant < 0) return;
-    VariantState &vs = vstate[loopKey(l)];
-    auto it = vs.best.find(variant);
-    if (it == vs.best.end() || seconds < it->second) vs.best[variant] = seconds;
+    auto it = vstate.find(key);
+    if (it == vstate.end()) return;
+    VariantState &vs = it->second;
+    auto b = vs.best.find(variant);
+    if (b == vs.best.end() || seconds < b->second) vs.best[variant] = seconds;
+    if (exploring) {
+        vs.explored++;
+        vs.exploreSeconds += seconds;
+    }
+    Record rec;
+    memcpy(rec.f, vf, sizeof rec.f);
+    rec.loopId = (long)key;
+    rec.cand = variant;
+    rec.seconds = seconds;
+    vdb.push_back(rec);
+}
+
+bool tunerExploring() {
+    if (uncapturedFlushes == 0) return true;  // the loops' handlers have not asked yet
+    for (auto &kv : vstate)
+        if (!explorationDone(kv.second)) return true;
+    return false;
+}
+
+void tunerFlushed() {
+    uncapturedFlushes++;
+    streamSync();  // the timings of this flush reach the tuner before the next decision
 }
 
 // ---------------------------------------------------------------- online layout tuning of ACROSS loops
@@ -105,8 +211,8 @@ static std::unordered_map<uint64_t, LayoutTune> lstate;
 static std::unordered_map<void *, uint64_t> lastLayoutKey;  // handler -> its most recent loop shape
 
 int tunerLayout(const Loop *l, bool explore) {
-    LayoutTune &t = lstate[loopKey(l)];
-    lastLayoutKey[(void *)l->cuda.func] = loopKey(l);
+    LayoutTune &t = lstate[loopKey((void *)l->cuda.func, l)];
+    lastLayoutKey[(void *)l->cuda.func] = loopKey((void *)l->cuda.func, l);
     if (explore) {
         if (t.runs[1] < 2) return 1;
         if (t.runs[0] < 2) return 0;
@@ -117,7 +223,7 @@ int tunerLayout(const Loop *l, bool explore) {
 
 void tunerRecordLayout(const Loop *l, int choice, double seconds) {
     if (choice < 0 || choice > 1) return;
-    LayoutTune &t = lstate[loopKey(l)];
+    LayoutTune &t = lstate[loopKey((void *)l->cuda.func, l)];
     t.runs[choice]++;
     if (seconds < t.best[choice]) t.best[choice] = seconds;
 }
@@ -173,7 +279,6 @@ static int candidates(const dvmhgb_synth_loop *L, dvmhgb_synth_cand *out, int ma
     return maxOut;
 }
 
-static float lg(double v) { return (float)std::log2(v > 1 ? v : 1); }
 
 static void features(const dvmhgb_synth_loop *L, const dvmhgb_synth_cand *C, float *f) {
     memset(f, 0, sizeof(float) * DVMHGB_TUNE_NF);
@@ -206,24 +311,30 @@ static void features(const dvmhgb_synth_loop *L, const dvmhgb_synth_cand *C, flo
 
 // ---------------------------------------------------------------- learned model
 
-static std::vector<float> model;  // packed MLP parameters (host copy)
-static std::vector<float> fmean, fstd;
-static float *modelDev = nullptr;
+// the cost model of synthetic candidates, and the variant model of
+// variant-choosing handlers: packed MLP parameters (host copy), the
+// per-feature normalisation used in training, the parameters on the device
+struct Mlp {
+    std::vector<float> params, mean, stdv;
+    float *dev = nullptr;
+    bool empty() const { return params.empty(); }
+};
+static Mlp model, vmodelStore;
 
-static void rankByModel(const std::vector<std::vector<float>> &feats, std::vector<int> &order) {
+static void rankBy(const Mlp &m, const std::vector<std::vector<float>> &feats, std::vector<int> &order) {
     int n = (int)feats.size();
     order.resize(n);
     for (int i = 0; i < n; i++) order[i] = i;
-    if (model.empty() || n == 0) return;
+    if (m.empty() || n == 0) return;
     std::vector<float> X((size_t)n * DVMHGB_TUNE_NF);
     for (int i = 0; i < n; i++)
         for (int j = 0; j < DVMHGB_TUNE_NF; j++)
-            X[(size_t)i * DVMHGB_TUNE_NF + j] = (feats[i][j] - fmean[j]) / fstd[j];
+            X[(size_t)i * DVMHGB_TUNE_NF + j] = (feats[i][j] - m.mean[j]) / m.stdv[j];
     float *dX = (float *)devAlloc(X.size() * sizeof(float));
     float *dY = (float *)devAlloc(n * sizeof(float));
     float *work = (float *)devAlloc(dvmhgb_mlp_work_floats(n) * sizeof(float));
     GB_CUDA(cudaMemcpyAsync(dX, X.data(), X.size() * sizeof(float), cudaMemcpyHostToDevice, gpu.stream));
-    GB_CHECK(dvmhgb_mlp_forward(modelDev, dX, n, dY, work, gpu.stream) == 0, "cost model forward failed");
+    GB_CHECK(dvmhgb_mlp_forward(m.dev, dX, n, dY, work, gpu.stream) == 0, "cost model forward failed");
     std::vector<float> y(n);
     GB_CUDA(cudaMemcpyAsync(y.data(), dY, n * sizeof(float), cudaMemcpyDeviceToHost, gpu.stream));
     streamSync();
@@ -231,6 +342,26 @@ static void rankByModel(const std::vector<std::vector<float>> &feats, std::vecto
     devFree(dY);
     devFree(work);
     std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return y[a] < y[b]; });
+}
+
+static void rankByModel(const std::vector<std::vector<float>> &feats, std::vector<int> &order) {
+    rankBy(model, feats, order);
+}
+static void rankByVariantModel(const std::vector<std::vector<float>> &feats, std::vector<int> &order) {
+    rankBy(vmodelStore, feats, order);
+}
+static bool variantModelReady() { return !vmodelStore.empty(); }
+
+static void install(Mlp &m, const float *params, const float *mean, const float *stdv) {
+    long np = dvmhgb_mlp_nparams();
+    m.params.assign(params, params + np);
+    m.mean.assign(mean, mean + DVMHGB_TUNE_NF);
+    m.stdv.assign(stdv, stdv + DVMHGB_TUNE_NF);
+    for (auto &x : m.stdv)
+        if (x <= 0) x = 1;
+    if (m.dev) devFree(m.dev);
+    m.dev = (float *)devAlloc(np * sizeof(float));
+    GB_CUDA(cudaMemcpy(m.dev, m.params.data(), np * sizeof(float), cudaMemcpyHostToDevice));
 }
 
 }  // namespace dvmhgb
@@ -379,15 +510,69 @@ void dvmhgb_tuner_db_clear(void) { db.clear(); }
 // Installs the cost model: packed MLP parameters (dvmhgb_mlp_nparams floats)
 // and the per-feature normalisation used in training.
 int dvmhgb_tuner_set_model(const float *params, const float *mean, const float *stdv) {
-    long np = dvmhgb_mlp_nparams();
-    model.assign(params, params + np);
-    fmean.assign(mean, mean + DVMHGB_TUNE_NF);
-    fstd.assign(stdv, stdv + DVMHGB_TUNE_NF);
-    for (auto &s : fstd)
-        if (s <= 0) s = 1;
-    if (modelDev) devFree(modelDev);
-    modelDev = (float *)devAlloc(np * sizeof(float));
-    GB_CUDA(cudaMemcpy(modelDev, model.data(), np * sizeof(float), cudaMemcpyHostToDevice));
+    install(model, params, mean, stdv);
+    return 0;
+}
+
+int dvmhgb_tuner_set_variant_model(const float *params, const float *mean, const float *stdv) {
+    install(vmodelStore, params, mean, stdv);
+    return 0;
+}
+
+long dvmhgb_tuner_vdb_size(void) { return (long)vdb.size(); }
+
+long dvmhgb_tuner_vdb_export(float *X, double *seconds, unsigned long long *keys, int *variants, long maxRows) {
+    long n = std::min(maxRows, (long)vdb.size());
+    for (long i = 0; i < n; i++) {
+        if (X) memcpy(X + i * DVMHGB_TUNE_NF, vdb[i].f, sizeof(float) * DVMHGB_TUNE_NF);
+        if (seconds) seconds[i] = vdb[i].seconds;
+        if (keys) keys[i] = (unsigned long long)vdb[i].loopId;
+        if (variants) variants[i] = vdb[i].cand;
+    }
+    return n;
+}
+
+void dvmhgb_tuner_vdb_clear(void) { vdb.clear(); }
+
+void dvmhgb_tuner_reset(void) {
+    queueFlush();
+    streamSync();
+    vstate.clear();
+    vorder.clear();
+    lstate.clear();
+    lastLayoutKey.clear();
+    uncapturedFlushes = 0;
+}
+
+long dvmhgb_tuner_variant_count(void) { return (long)vorder.size(); }
+
+int dvmhgb_tuner_exploring(void) {
+    streamSync();  // the timings so far reach the tuner
+    return settings.tuneMode && tunerExploring() ? 1 : 0;
+}
+
+int dvmhgb_tuner_variant_info(long index, DvmHandlerFunc *handler, int *nvariants, int *chosen, double *best,
+                              int maxBest, int *explored, double *exploreSeconds) {
+    streamSync();
+    if (index < 0 || index >= (long)vorder.size()) return -1;
+    const VariantState &vs = vstate[vorder[index]];
+    if (handler) *handler = (DvmHandlerFunc)vs.handler;
+    if (nvariants) *nvariants = vs.nvariants;
+    if (chosen) {
+        // the variant kept now: the fastest timed, else the default / the model's first
+        int v = vs.chosen;
+        double bt = 1e300;
+        for (auto &kv : vs.best)
+            if (kv.second < bt) bt = kv.second, v = kv.first;
+        *chosen = v;
+    }
+    if (best)
+        for (int v = 0; v < maxBest && v < vs.nvariants; v++) {
+            auto it = vs.best.find(v);
+            best[v] = it == vs.best.end() ? -1.0 : it->second;
+        }
+    if (explored) *explored = vs.explored;
+    if (exploreSeconds) *exploreSeconds = vs.exploreSeconds;
     return 0;
 }
 

@@ -200,6 +200,138 @@ def run(rt, n_loops=2000, n_test=200, seed=20261207, reps=2, epochs=200, frac=0.
     return out
 
 
+# ---------------------------------------------------------------- the configurations' own loops
+#
+# The hand-written handlers of the workload programs choose among kernel
+# variants through dvmhgb_loop_variant_desc, describing each variant to the
+# runtime.  Every timed execution goes into the runtime's variant database.
+# Protocol, per program:
+#   1. exhaustive tuning (mode 1) at a few training sizes: the runtime tries
+#      every variant once, in successive steps, and records each;
+#   2. the variant model (same MLP, same kernels) is trained on those records,
+#      log-times centred per loop shape, and installed in the runtime;
+#   3. at the configuration's own size (never seen in training): exhaustive
+#      tuning again (the reference point: every variant's time, their sum the
+#      exhaustive tuning time), then model-guided tuning (mode 2): the runtime
+#      ranks the variants by the model, tries only the first floor(0.1 n)
+#      (none: it keeps the model's first choice), and keeps the fastest tried.
+# Reported: the kept variant's time over the exhaustive best, the model's
+# tuning time over the exhaustive one, both variants.
+
+def _programs(g, seed):
+    """name -> (training sizes, configuration size, maker(size) -> object with run/close)."""
+    return {
+        "jacobi2d_1024": ([258, 514, 2050], 1024, lambda n: g.Jacobi(2, n, seed)),
+        "jacobi3d_512": ([130, 194, 258, 322], 512, lambda n: g.Jacobi(3, n, seed)),
+        "sor3d_384": ([66, 130, 194], 384, lambda n: g.Sor(n, 1.5, seed + 2)),
+        "heat_256x2048": ([(64, 512), (128, 1024)], (256, 2048), lambda p: g.Heat(p[0], 64, p[1], 0.2, seed + 3)),
+    }
+
+
+def _variant_runs(g, rt, mode, maker, size, steps_cap=64):
+    """Tunes one program at one size in `mode`; returns the variant record of
+    the handler with the most variants (the program's main loop)."""
+    rt.dvmhgb_tuner_reset()
+    rt.dvmhgb_set_tuning(mode)
+    w = maker(size)
+    try:
+        steps = 0
+        while steps < steps_cap:
+            w.run(1)
+            steps += 1
+            g.sync()
+            if not rt.dvmhgb_tuner_exploring():
+                break
+        w.run(2)  # the kept variant, as it then runs
+        g.sync()
+        info = _variant_info(rt)
+    finally:
+        rt.dvmhgb_set_tuning(0)
+        w.close()
+    return info
+
+
+def _variant_info(rt):
+    H = ctypes.c_void_p()
+    nv, ch, ex = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+    es = ctypes.c_double()
+    best = (ctypes.c_double * 64)()
+    out = None
+    for i in range(int(rt.dvmhgb_tuner_variant_count())):
+        rt.dvmhgb_tuner_variant_info(ctypes.c_long(i), ctypes.byref(H), ctypes.byref(nv), ctypes.byref(ch), best, 64,
+                                     ctypes.byref(ex), ctypes.byref(es))
+        rec = {"nvariants": nv.value, "chosen": ch.value, "best": [best[v] for v in range(nv.value)],
+               "explored": ex.value, "explore_seconds": es.value}
+        if out is None or rec["nvariants"] > out["nvariants"]:
+            out = rec
+    return out
+
+
+def configs_eval(g, seed=20261203, epochs=300, log=print):
+    """The learned tuner on the configurations' own loops (the bench's configs.tune)."""
+    rt = g.runtime()
+    rt.dvmhgb_tuner_vdb_size.restype = ctypes.c_long
+    rt.dvmhgb_tuner_vdb_export.restype = ctypes.c_long
+    rt.dvmhgb_tuner_variant_count.restype = ctypes.c_long
+    rt.dvmhgb_mlp_nparams.restype = ctypes.c_long
+    g.set_mode("batched")
+    progs = _programs(g, seed)
+    rt.dvmhgb_tuner_vdb_clear()
+    t0 = time.time()
+    for name, (train, _, maker) in progs.items():
+        for size in train:
+            _variant_runs(g, rt, 1, maker, size)
+    rows = int(rt.dvmhgb_tuner_vdb_size())
+    X = np.zeros((rows, 24), dtype=np.float32)
+    sec = np.zeros(rows)
+    keys = np.zeros(rows, dtype=np.uint64)
+    var = np.zeros(rows, dtype=np.int32)
+    fp = ctypes.POINTER(ctypes.c_float)
+    rt.dvmhgb_tuner_vdb_export(X.ctypes.data_as(fp), sec.ctypes.data_as(ctypes.POINTER(ctypes.c_double)),
+                               keys.ctypes.data_as(ctypes.POINTER(ctypes.c_ulonglong)),
+                               var.ctypes.data_as(ctypes.POINTER(ctypes.c_int)), ctypes.c_long(rows))
+    # one row per (loop shape, variant): its fastest time; log-time centred per loop shape
+    best = {}
+    for i in range(rows):
+        k = (int(keys[i]), int(var[i]))
+        if k not in best or sec[i] < sec[best[k]]:
+            best[k] = i
+    idx = np.array(sorted(best.values()))
+    Xt, lt = X[idx], np.log(np.maximum(sec[idx], 1e-9))
+    kt = keys[idx]
+    y = lt.copy()
+    for k in np.unique(kt):
+        m = kt == k
+        y[m] = lt[m] - lt[m].mean()
+    mean, std = Xt.mean(0), Xt.std(0) + 1e-6
+    tu = Tuner(rt)
+    params, losses = tu.train((Xt - mean) / std, y, epochs=epochs, batch=min(4096, len(y)), lr=2e-3)
+    rt.dvmhgb_tuner_set_variant_model(np.ascontiguousarray(params, np.float32).ctypes.data_as(fp),
+                                      np.ascontiguousarray(mean, np.float32).ctypes.data_as(fp),
+                                      np.ascontiguousarray(std, np.float32).ctypes.data_as(fp))
+    t_train = time.time() - t0
+    out = {"protocol": "exhaustive at training sizes -> variant model -> at the configuration size: exhaustive "
+                       "vs model-guided (top floor(0.1 n) tried)", "train_rows": int(len(y)),
+           "loss_first_last": [float(losses[0]), float(losses[-1])], "train_seconds": t_train}
+    for name, (train, size, maker) in progs.items():
+        ex = _variant_runs(g, rt, 1, maker, size)
+        md = _variant_runs(g, rt, 2, maker, size)
+        bests = np.array(ex["best"])
+        vbest = int(np.argmin(np.where(bests >= 0, bests, np.inf)))
+        pick = md["chosen"]
+        out[name] = {"size": size if not isinstance(size, tuple) else list(size), "train_sizes": train,
+                     "variants": ex["nvariants"], "exhaustive_best_variant": vbest,
+                     "model_variant": pick, "model_tried": md["explored"],
+                     "model_over_exhaustive_time": float(bests[pick] / bests[vbest]) if bests[pick] > 0 else None,
+                     "tuning_time_frac": float(md["explore_seconds"] / ex["explore_seconds"])
+                     if ex["explore_seconds"] > 0 else None,
+                     "exhaustive_ms": {str(v): round(1e3 * b, 4) for v, b in enumerate(bests)},
+                     "exhaustive_tuning_s": ex["explore_seconds"], "model_tuning_s": md["explore_seconds"]}
+        log(name, out[name])
+    rt.dvmhgb_tuner_reset()
+    return out
+
+
 if __name__ == "__main__":
     import argparse
     import json
@@ -210,6 +342,7 @@ if __name__ == "__main__":
     ap.add_argument("--test", type=int, default=200)
     ap.add_argument("--reps", type=int, default=2)
     ap.add_argument("--out", default=None)
+    ap.add_argument("--configs", action="store_true", help="the configurations' own loops (variants) only")
     a = ap.parse_args()
     sys.path.insert(0, os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
     import __graft_entry__ as ge
@@ -217,7 +350,10 @@ if __name__ == "__main__":
     _, g = ge.package()
     g.init()
     t0 = time.time()
-    res = run(g.runtime(), n_loops=a.loops, n_test=a.test, reps=a.reps)
+    if a.configs:
+        res = configs_eval(g)
+    else:
+        res = run(g.runtime(), n_loops=a.loops, n_test=a.test, reps=a.reps)
     res["wall_seconds"] = time.time() - t0
     text = json.dumps(res, indent=1)
     if a.out:

@@ -9,6 +9,7 @@
 // the runtime folds all their reductions in one more launch.
 #include <cuda_runtime.h>
 
+#include <cmath>
 #include <cstdio>
 #include <cstdlib>
 
@@ -17,6 +18,22 @@
 #include "dvmh_gb_kernels.h"
 
 namespace {
+
+// the variants as the tuner's variant model sees them: family 4 (this program),
+// log2 rows per strip, CTAs per SM, then the batch: log2 of its loops and of
+// its cells, log2 of the largest loop's rows
+constexpr int HEAT_NDESC = 6;
+void heatVariantDesc(float *d, long loops, long cells, long maxRows) {
+    for (int v = 0; v < DVMHGB_HEAT_VARIANTS; v++) {
+        float *e = d + v * HEAT_NDESC;
+        e[0] = 4;
+        e[1] = (float)(4 + v % 5);
+        e[2] = (float)DVMHGB_HEAT_CTAS(v);
+        e[3] = (float)log2((double)loops);
+        e[4] = (float)log2((double)(cells > 1 ? cells : 1));
+        e[5] = (float)log2((double)(maxRows > 1 ? maxRows : 1));
+    }
+}
 
 // everything a heat loop needs on the device, its reduction buffers prepared
 void prepare(DvmType loop_ref, DvmType S_hdr[], DvmType D_hdr[], double *c_ptr, dvmhgb_heat_desc *d,
@@ -66,16 +83,27 @@ extern "C" void loop_heat_cuda(DvmType *pLoopRef, DvmType S_hdr[], DvmType D_hdr
     dvmh_loop_cuda_red_finish_C(loop_ref, 2);
 }
 
-// refs: `count` loops whose CUDA handler is loop_heat_cuda, over distinct arrays
+// refs: `count` loops whose CUDA handler is loop_heat_cuda, over distinct arrays.
+// The strip geometry (rows per strip, CTAs per SM) is the tuner's variant.
 extern "C" void loop_heat_batch_cuda(DvmType *refs, DvmType count) {
     dvmhgb_heat_desc *table =
         (dvmhgb_heat_desc *)dvmhgb_loop_host_scratch(refs[0], (DvmType)(sizeof(dvmhgb_heat_desc) * count));
     cudaStream_t stream = 0;
-    long total = 0, units = 0;
+    long cells = 0, maxRows = 1;
     for (DvmType q = 0; q < count; q++) {
         DvmType ref = refs[q];
         prepare(ref, (DvmType *)dvmhgb_loop_param(ref, 0), (DvmType *)dvmhgb_loop_param(ref, 1),
                 (double *)dvmhgb_loop_param(ref, 5), &table[q], &stream);
+        const long rows = table[q].hi0 - table[q].lo0 + 1;
+        cells += rows * (table[q].hi1 - table[q].lo1 + 1);
+        if (rows > maxRows) maxRows = rows;
+    }
+    float desc[DVMHGB_HEAT_VARIANTS * HEAT_NDESC];
+    heatVariantDesc(desc, (long)count, cells, maxRows);
+    const int v = dvmhgb_loop_variant_desc(refs[0], DVMHGB_HEAT_VARIANTS, DVMHGB_HEAT_DEFAULT, desc, HEAT_NDESC);
+    long total = 0, units = 0;
+    for (DvmType q = 0; q < count; q++) {
+        dvmhgb_heat_desc_rows(&table[q], DVMHGB_HEAT_ROWS(v));
         table[q].unitBase = units;
         table[q].stripBase = total;
         units += table[q].units;
@@ -84,7 +112,7 @@ extern "C" void loop_heat_batch_cuda(DvmType *refs, DvmType count) {
     dvmhgb_heat_desc *dev =
         (dvmhgb_heat_desc *)dvmhgb_loop_scratch(refs[0], (DvmType)(sizeof(dvmhgb_heat_desc) * count));
     if (cudaMemcpyAsync(dev, table, sizeof(dvmhgb_heat_desc) * count, cudaMemcpyHostToDevice, stream) != cudaSuccess ||
-        dvmhgb_heat_many(dev, (int)count, total, stream) != 0) {
+        dvmhgb_heat_many_grid(dev, (int)count, total, DVMHGB_HEAT_CTAS(v), stream) != 0) {
         fprintf(stderr, "loop_heat_batch_cuda: launch failed\n");
         exit(1);
     }

@@ -24,6 +24,22 @@
 
 namespace {
 
+// the variants as the tuner's variant model sees them: family 2 (this program),
+// the handler (1 update, 2 stencil, 3 the fused pair), its variant number
+constexpr int NDESC = 3;
+const float *variantDesc(int handler) {
+    static float d[3][(NOPS_STN + 2) * NDESC];
+    static bool ready = false;
+    if (!ready) {
+        for (int h = 1; h <= 3; h++)
+            for (int v = 0; v < NOPS_STN + 2; v++) {
+                d[h - 1][v * NDESC] = 2, d[h - 1][v * NDESC + 1] = (float)h, d[h - 1][v * NDESC + 2] = (float)v;
+            }
+        ready = true;
+    }
+    return d[handler - 1];
+}
+
 struct ArrDev {
     double *base;
     long st[R];
@@ -75,7 +91,7 @@ extern "C" void loop_jac2d_upd_cuda(DvmType *pLoopRef, DvmType A_hdr[], DvmType 
     dvmh_loop_cuda_register_red_C(loop_ref, 1, (void **)&eps_grid, 0);
     dvmh_loop_red_init_C(loop_ref, 1, &eps, 0);
     dvmh_loop_cuda_red_prepare_C(loop_ref, 1, dvmhgb_jac2d_update_items(lo, hi), 0);
-    check(dvmhgb_jac2d_update(A.base, B.base, A.st, lo, hi, eps_grid, dvmhgb_loop_variant(loop_ref, 3, 2), stream), "loop_jac2d_upd_cuda");
+    check(dvmhgb_jac2d_update(A.base, B.base, A.st, lo, hi, eps_grid, dvmhgb_loop_variant_desc(loop_ref, 3, 2, variantDesc(1), NDESC), stream), "loop_jac2d_upd_cuda");
     dvmh_loop_cuda_red_finish_C(loop_ref, 1);
 }
 
@@ -88,7 +104,7 @@ extern "C" void loop_jac2d_stn_cuda(DvmType *pLoopRef, DvmType A_hdr[], DvmType 
     dim3 threads(0, 0, 0);
     cudaStream_t stream;
     dvmh_loop_cuda_get_config_C(loop_ref, 0, 0, &threads, &stream, 0);
-    check(dvmhgb_jac2d_stencil(A.base, B.base, A.st, A.ext, lo, hi, dvmhgb_loop_variant(loop_ref, NOPS_STN + 1, DEF_STN), stream), "loop_jac2d_stn_cuda");
+    check(dvmhgb_jac2d_stencil(A.base, B.base, A.st, A.ext, lo, hi, dvmhgb_loop_variant_desc(loop_ref, NOPS_STN + 1, DEF_STN, variantDesc(2), NDESC), stream), "loop_jac2d_stn_cuda");
 }
 
 // refs[0]: the update loop (A_hdr, B_hdr, eps_ptr), refs[1]: the stencil loop (A2_hdr, B2_hdr)
@@ -117,7 +133,8 @@ extern "C" void loop_jac2d_fused_cuda(DvmType refs[2], DvmType A_hdr[], DvmType 
     dvmh_loop_cuda_red_prepare_C(upd, 1, dvmhgb_jac2d_fused_items(lo, hi), 0);
     double *Bnew = (double *)dvmhgb_loop_alt_buffer(stn, B_hdr);
     check(dvmhgb_jac2d_fused(A.base, B.base, Bnew, A.st, A.ext, lo, hi, eps_grid,
-                             dvmhgb_loop_variant(upd, NOPS_STN + 2, DEF_FUSED), stream), "loop_jac2d_fused_cuda");
+                             dvmhgb_loop_variant_desc(upd, NOPS_STN + 2, DEF_FUSED, variantDesc(3), NDESC), stream),
+          "loop_jac2d_fused_cuda");
     dvmh_loop_cuda_red_finish_C(upd, 1);
 }
 

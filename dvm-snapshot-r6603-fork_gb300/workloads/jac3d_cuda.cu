@@ -26,6 +26,46 @@
 
 namespace {
 
+// The variants as the tuner's variant model sees them (dvmhgb_loop_variant_desc):
+// family 1 (this program), the handler (1 update, 2 stencil, 3 the fused pair),
+// then for stencils: fixed-point sums, FP64-unit additions per cell, rows per
+// thread, CTAs per SM, share of CTAs on the FP64 unit, and for the pair how it
+// runs (0 one pass, 1 update then stencil, 2 the two overlapped in chunks).
+constexpr int NDESC = 8;
+void stencilDesc(int v, float *d) {
+    static const int q[8][3] = {{4, 0, 1}, {3, 0, 1}, {4, 1, 2}, {4, 1, 3}, {4, 2, 5}, {3, 1, 2}, {4, 1, 4}, {4, 3, 5}};
+    if (v < 12) {
+        d[2] = 0, d[3] = (float)(v % 6), d[4] = (float)(1 + v / 6), d[5] = 2, d[6] = 1;
+    } else if (v < DVMHGB_JAC3D_VARIANTS - 8) {
+        d[2] = 0, d[3] = 5, d[4] = 1, d[5] = v == 12 ? 3.0f : 4.0f, d[6] = 1;
+    } else {
+        const int *c = q[v - (DVMHGB_JAC3D_VARIANTS - 8)];
+        d[2] = 1, d[3] = 5, d[4] = 1, d[5] = (float)c[0], d[6] = (float)c[1] / (float)c[2];
+    }
+}
+const float *variantDesc(int handler) {
+    static float upd[3 * NDESC], stn[DVMHGB_JAC3D_VARIANTS * NDESC], fus[(DVMHGB_JAC3D_VARIANTS + 3) * NDESC];
+    static bool ready = false;
+    if (!ready) {
+        for (int v = 0; v < 3; v++) upd[v * NDESC] = 1, upd[v * NDESC + 1] = 1, upd[v * NDESC + 2] = (float)v;
+        for (int v = 0; v < DVMHGB_JAC3D_VARIANTS; v++) {
+            float *d = stn + v * NDESC;
+            d[0] = 1, d[1] = 2;
+            stencilDesc(v, d);
+        }
+        for (int v = 0; v < DVMHGB_JAC3D_VARIANTS + 3; v++) {
+            float *d = fus + v * NDESC;
+            d[0] = 1, d[1] = 3;
+            const int sv = v < DVMHGB_JAC3D_VARIANTS ? v
+                                                     : (v == DVMHGB_JAC3D_OVERLAP_Q ? DVMHGB_JAC3D_VARIANTS - 8 : 13);
+            stencilDesc(sv, d);
+            d[7] = v < DVMHGB_JAC3D_VARIANTS - 8 ? 0.0f : (v < DVMHGB_JAC3D_OVERLAP ? 1.0f : 2.0f);
+        }
+        ready = true;
+    }
+    return handler == 1 ? upd : (handler == 2 ? stn : fus);
+}
+
 struct ArrDev {
     double *base;
     long st[R];
@@ -77,7 +117,7 @@ extern "C" void loop_jac3d_upd_cuda(DvmType *pLoopRef, DvmType A_hdr[], DvmType 
     dvmh_loop_cuda_register_red_C(loop_ref, 1, (void **)&eps_grid, 0);
     dvmh_loop_red_init_C(loop_ref, 1, &eps, 0);
     dvmh_loop_cuda_red_prepare_C(loop_ref, 1, dvmhgb_jac3d_update_items(lo, hi), 0);
-    check(dvmhgb_jac3d_update(A.base, B.base, A.st, lo, hi, eps_grid, dvmhgb_loop_variant(loop_ref, 3, 2), stream), "loop_jac3d_upd_cuda");
+    check(dvmhgb_jac3d_update(A.base, B.base, A.st, lo, hi, eps_grid, dvmhgb_loop_variant_desc(loop_ref, 3, 2, variantDesc(1), NDESC), stream), "loop_jac3d_upd_cuda");
     dvmh_loop_cuda_red_finish_C(loop_ref, 1);
 }
 
@@ -90,7 +130,7 @@ extern "C" void loop_jac3d_stn_cuda(DvmType *pLoopRef, DvmType A_hdr[], DvmType 
     dim3 threads(0, 0, 0);
     cudaStream_t stream;
     dvmh_loop_cuda_get_config_C(loop_ref, 0, 0, &threads, &stream, 0);
-    check(dvmhgb_jac3d_stencil(A.base, B.base, A.st, A.ext, lo, hi, dvmhgb_loop_variant(loop_ref, DVMHGB_JAC3D_VARIANTS, DEF_STN), stream), "loop_jac3d_stn_cuda");
+    check(dvmhgb_jac3d_stencil(A.base, B.base, A.st, A.ext, lo, hi, dvmhgb_loop_variant_desc(loop_ref, DVMHGB_JAC3D_VARIANTS, DEF_STN, variantDesc(2), NDESC), stream), "loop_jac3d_stn_cuda");
 }
 
 // refs[0]: the update loop (A_hdr, B_hdr, eps_ptr), refs[1]: the stencil loop (A2_hdr, B2_hdr)
@@ -113,7 +153,8 @@ extern "C" void loop_jac3d_fused_cuda(DvmType refs[2], DvmType A_hdr[], DvmType 
     cudaStream_t stream;
     dvmh_loop_cuda_get_config_C(upd, 0, 0, &threads, &stream, 0);
     dvmh_loop_cuda_get_config_C(stn, 0, 0, &threads, &stream, 0);
-    const int variant = dvmhgb_loop_variant(upd, DVMHGB_JAC3D_VARIANTS + 3, DEF_FUSED);  // + the pair: unfused, overlapped (2)
+    // + the pair: unfused, overlapped (two stencils)
+    const int variant = dvmhgb_loop_variant_desc(upd, DVMHGB_JAC3D_VARIANTS + 3, DEF_FUSED, variantDesc(3), NDESC);
     double eps, *eps_grid = 0;
     dvmh_loop_cuda_register_red_C(upd, 1, (void **)&eps_grid, 0);
     dvmh_loop_red_init_C(upd, 1, &eps, 0);

@@ -67,6 +67,18 @@ int dvmhgb_loop_variant(DvmType loopRef, int nvariants, int dflt);
 /* Force every later dvmhgb_loop_variant() to return v (clamped to the loop's
  * variant count); v < 0 restores tuning / defaults.  Overrides DVMH_GB_VARIANT. */
 void dvmhgb_force_variant(int v);
+/* dvmhgb_loop_variant with a description of each variant: desc[v * ndesc + d]
+ * (ndesc <= DVMHGB_VARIANT_NDESC numbers per variant, the first one naming the
+ * kernel family).  With model-guided tuning the runtime ranks the variants by
+ * the variant model's predicted time for this loop and tries only the first
+ * floor(0.1 x nvariants) of them (none: the model's first choice is taken as
+ * it is); every timed execution is recorded with its features in the
+ * runtime's variant database.  Exhaustive tuning tries every variant, as
+ * dvmhgb_loop_variant does.  In batched mode, flushes run without graph
+ * capture while a loop's variants are being tried, then are captured with
+ * the chosen one. */
+#define DVMHGB_VARIANT_NDESC 16
+int dvmhgb_loop_variant_desc(DvmType loopRef, int nvariants, int dflt, const float *desc, int ndesc);
 
 /* Device layouts for ACROSS loops.  On (default; environment
  * DVMH_GB_AUTOTFM=0 turns it off), dvmh_loop_autotransform_C stores a loop's
@@ -91,6 +103,19 @@ void dvmhgb_set_reduce_dependences(int on);
 /* Online tuning of CUDA blocks, variants and layouts: 0 off, 1 exhaustive,
  * 2 model-guided (the same as DVMH_OPT_PARAMS at start-up). */
 void dvmhgb_set_tuning(int mode);
+/* Forget what the tuner learnt about variants and layouts (not its databases
+ * or models). */
+void dvmhgb_tuner_reset(void);
+/* The variant tuning of each loop shape seen (index 0 .. count-1): the handler
+ * that asked, its variant count, the variant kept (or about to be),
+ * per-variant fastest seconds (-1 = never timed; best[] holds nvariants
+ * entries, may be null), how many executions tried an untried variant and
+ * their summed seconds (the tuning time).  0, or -1 for a bad index. */
+long dvmhgb_tuner_variant_count(void);
+/* 1 while some loop shape is still trying variants (its flushes run uncaptured) */
+int dvmhgb_tuner_exploring(void);
+int dvmhgb_tuner_variant_info(long index, DvmHandlerFunc *handler, int *nvariants, int *chosen, double *best,
+                              int maxBest, int *explored, double *exploreSeconds);
 
 /* Self-test of the integer-pipe FP64 operations against the FP64 unit on n
  * random operand pairs: mismatches[0..3] = add, sub, mul, division by 6. */
@@ -134,6 +159,31 @@ void dvmhgb_hostprof_reset(void);
 
 /* Stream the runtime launches on (a cudaStream_t). */
 void *dvmhgb_stream(void);
+
+/* The CUDA block that dvmh_loop_cuda_get_config_C hands a handler, as a pure
+ * function of the loop and the device's limits (the reference's
+ * DvmhLoopCuda::pickBlock, rts/dvmh/loop.cpp:2134-2199, and its default
+ * blocks, loop.cpp:1464-1485): the user's block (userBlock != 0) or the given
+ * one (block[] >= 1) or the default for min(3, rank - (hasDeps != 0)) block
+ * dimensions; then a block needing more shared memory (sharedPerThread per
+ * thread) or registers (regsPerThread, 0 = the device's maximum per thread)
+ * than one block can have is shrunk to one dimension of
+ * max(1, roundDown(min(256, have / perThread), warpSize)) threads (1 for a
+ * loop with no free block dimension).  Returns 0 with block[] set, or a user
+ * error the reference reports: 1 more block dimensions than the loop has (one
+ * fewer with dependences), 2 an axis above the device's limit, 3 more threads
+ * than a block can have, 4 / 5 shared memory / registers insufficient for a
+ * block the user fixed. */
+typedef struct {
+    int maxBlockSize[3];
+    int maxThreadsPerBlock;
+    long sharedPerBlock;   /* cudaDeviceProp::sharedMemPerBlock */
+    long regsPerBlock;     /* cudaDeviceProp::regsPerBlock */
+    int warpSize;
+    int maxRegsPerThread;  /* 255 */
+} dvmhgb_cuda_limits_t;
+int dvmhgb_pick_block(int loopRank, int hasDeps, int userBlock, int block[3], long sharedPerThread,
+                      long regsPerThread, const dvmhgb_cuda_limits_t *limits);
 
 #ifdef __cplusplus
 }

@@ -36,17 +36,20 @@ int dvmhgb_jac3d_update(double *A, const double *B, const long st[3], const long
  * + N, N = 0..5 additions of a cell on the FP64 unit (the others on the integer
  * pipe when the CTA's inputs are all +0 or positive normal, else all native);
  * v = 12, 13: all native, one row per thread, registers capped for 3 / 4 CTAs
- * per SM; v = 14, 15, 16: the sums in 61-bit fixed point on the integer pipe
+ * per SM; v = 14..21: the sums in 61-bit fixed point on the integer pipe
  * (planes whose neighbourhood holds a value outside +0 and [2^-9, 1) on the
- * FP64 unit), registers capped for 4 / 3 / 2 CTAs per SM; -1 for v outside
+ * FP64 unit), with a share of the CTAs computing natively so that the FP64
+ * unit works beside the integer pipe -- (CTAs per SM, native CTAs of every
+ * den): 14 (4, 0/1), 15 (3, 0/1), 16 (4, 1/2), 17 (4, 1/3), 18 (4, 2/5),
+ * 19 (3, 1/2), 20 (4, 1/4), 21 (4, 3/5); -1 for v outside
  * 0..DVMHGB_JAC3D_VARIANTS-1 */
-#define DVMHGB_JAC3D_VARIANTS 17
+#define DVMHGB_JAC3D_VARIANTS 22
 int dvmhgb_jac3d_stencil(const double *A, double *B, const long st[3], const long ext[3], const long lo[3],
                          const long hi[3], int native, void *stream);
 /* loops 1+2 fused (same box): reads A, B; writes A = B and Bnew = stencil(A_new)
  * into Bnew (a second buffer of B's layout), B's values outside the box copied
  * into Bnew; MAX partials, one per CTA (the count depends on the variant).
- * Variants 0..13 as above (one pass), 14..16 the update kernel and then the
+ * Variants 0..13 as above (one pass), 14..21 the update kernel and then the
  * fixed-point stencil of that variant, and DVMHGB_JAC3D_UNFUSED: the update
  * and the stencil kernels (variant 13) one after the other (Bnew may then be B
  * itself: the stencil reads only A; the one-pass variants reject Bnew == B) */
@@ -85,6 +88,19 @@ long dvmhgb_sor3d_items(const long lo[3], const long hi[3], int variant);
 long dvmhgb_sor3d_scratch_bytes(const long lo[3], const long hi[3], int variant);
 int dvmhgb_sor3d_sweep(double *A, const long st[3], const long ext[3], const long lo[3], const long hi[3],
                        const double *wDev, double *items, void *scratch, int *status, int variant, void *stream);
+/* The same sweep with its bounded waits made explicit.  Every wait for a
+ * predecessor tile (column, variant 3) polls at most pollLimit times
+ * (dvmhgb_sor3d_sweep: 2^24, about 1-4 s) before the kernel writes its timeout
+ * code 0x50520001 to *status, sets the top bit of the hand-out counter (the
+ * first word of scratch) so that no warp takes another tile, and returns; the
+ * runtime reports a non-zero status word at its next synchronisation (exit
+ * status 1).  firstIndex > 0 starts the hand-out at that tile: the tiles
+ * before it are left to nobody, so their successors' waits run out -- how the
+ * tests make a wait expire without a fault.  -1 for pollLimit < 1 or a
+ * negative firstIndex. */
+int dvmhgb_sor3d_sweep_bounded(double *A, const long st[3], const long ext[3], const long lo[3], const long hi[3],
+                               const double *wDev, double *items, void *scratch, int *status, int variant,
+                               void *stream, long pollLimit, long firstIndex);
 
 /* ---- explicit 2-D heat step, FP64 (workloads/heat.c), with SUM and MINLOC:
  * per (row, 64-wide chunk) unit one SUM item (canonical pairwise tree), one
@@ -110,6 +126,17 @@ int dvmhgb_heat(const dvmhgb_heat_desc *d, void *stream);
 /* dDev: device array of n descriptors with unitBase / stripBase = prefix sums of
  * units / strips; totalStrips = the sum of strips */
 int dvmhgb_heat_many(const dvmhgb_heat_desc *dDev, int n, long totalStrips, void *stream);
+/* The strip geometry of the batched step, a tuner choice (results do not depend
+ * on it: a strip's SUM and MINLOC items are per (row, chunk) whatever the
+ * strip): variant v walks strips of DVMHGB_HEAT_ROWS(v) rows with a persistent
+ * grid of DVMHGB_HEAT_CTAS(v) CTAs of 8 warps per SM.  dvmhgb_heat_desc_rows
+ * sets a descriptor's rows per strip (and its strip count); -1 for sr < 1. */
+#define DVMHGB_HEAT_VARIANTS 10
+#define DVMHGB_HEAT_DEFAULT 2
+#define DVMHGB_HEAT_ROWS(v) (16L << ((v) % 5))
+#define DVMHGB_HEAT_CTAS(v) ((v) < 5 ? 8 : 4)
+int dvmhgb_heat_desc_rows(dvmhgb_heat_desc *d, long sr);
+int dvmhgb_heat_many_grid(const dvmhgb_heat_desc *dDev, int n, long totalStrips, int ctasPerSm, void *stream);
 
 /* ---- no counterpart in the reference: the Jacobi-3D update loop for callers
  * that cannot allocate device memory (inside a stream capture in global mode,
@@ -121,8 +148,11 @@ int dvmhgb_heat_many(const dvmhgb_heat_desc *dDev, int n, long totalStrips, void
  * process exits), not to a caller buffer: nothing is allocated and no
  * allocating library routine is called.  The first call on a device looks up
  * the array's device address (cudaGetSymbolAddress) with that device current;
- * make that first call before any stream capture.  All calls share the array:
- * calls whose GPU work overlaps in time race.  Returns 0; -1 invalid
+ * make that first call before any stream capture.  The address is kept for
+ * the life of the process: after cudaDeviceReset the array lives at a new
+ * address, so a process that resets a device must not call this entry point
+ * on that device again.  All calls share the array: calls whose GPU work
+ * overlaps in time race.  Returns 0; -1 invalid
  * arguments; -2 the launch would need more than 4096 partial slots (message
  * on stderr); -3 CUDA error. ---- */
 int dvmhgb_jac3d_update_noalloc(double *A, const double *B, const long st[3], const long lo[3], const long hi[3],
@@ -173,6 +203,14 @@ long dvmhgb_tuner_db_export(float *X, double *seconds, long *loopIds, int *cands
 void dvmhgb_tuner_db_clear(void);
 int dvmhgb_tuner_set_model(const float *params, const float *mean, const float *stdv);
 int dvmhgb_tuner_rank(const dvmhgb_synth_loop *L, const dvmhgb_synth_cand *cands, int n, int *order);
+/* The variant database (timed executions of variant-choosing handlers:
+ * features of loop and variant, the loop shape's key, the variant, seconds),
+ * and the variant model that ranks them (dvmhgb_loop_variant_desc); the model
+ * has the cost model's shape and normalisation. */
+long dvmhgb_tuner_vdb_size(void);
+long dvmhgb_tuner_vdb_export(float *X, double *seconds, unsigned long long *keys, int *variants, long maxRows);
+void dvmhgb_tuner_vdb_clear(void);
+int dvmhgb_tuner_set_variant_model(const float *params, const float *mean, const float *stdv);
 
 /* copy src -> dst for every element of the array outside the box (both arrays share st/ext) */
 int dvmhgb_copy_outside_box(int rank, const double *src, double *dst, const long *st, const long *ext,

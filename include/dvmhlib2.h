@@ -102,6 +102,9 @@ extern "C" {
 void dvmh_line_C(DvmType lineNumber, const char fileName[]);                 /* :19 */
 void dvmh_init_C(DvmType flags, int *pArgc, char ***pArgv);                  /* :22 */
 void dvmh_exit_C(DvmType exitCode);                                          /* :26 */
+/* a translation unit other than main's: initialises once, later calls are ignored */
+void dvmh_init_lib_C(DvmType flags);                                         /* :24 */
+void dvmh_init_lib_(const DvmType *pFlags);                                  /* :25 */
 
 /* ---- distributed arrays and templates ---- */
 /* varargs: {axisSize, shadowLow, shadowHigh} x rank; typeSize < 0 means -rt_TYPE */
@@ -119,6 +122,25 @@ DvmType dvmh_alignment_linear_C(DvmType axis, DvmType multiplier, DvmType summan
 void dvmh_align_C(DvmType dvmDesc[], const DvmType templDesc[], DvmType templRank, ...);   /* :67 */
 void dvmh_array_free_C(DvmType dvmDesc[]);                                                 /* :77 */
 void dvmh_delete_object_(DvmType dvmDesc[]);                                               /* :78 */
+/* dynamic arrays: declared with the first size unknown (0), then allocated with
+ * byteCount bytes (the first size = byteCount / (element size x other sizes)) */
+void dvmh_array_declare_C(DvmType dvmDesc[], DvmType rank, DvmType typeSize, ...);         /* :29 */
+void dvmh_array_alloc_C(DvmType dvmDesc[], DvmType byteCount);                             /* :35 */
+void dvmh_forget_header_(DvmType dvmDesc[]);                                               /* :79 */
+
+/* ---- regular (non-distributed) variables: data regions and their headers ---- */
+/* varargs: rank axis sizes (the first may be 0 for an incomplete array) */
+DvmType *dvmh_variable_gen_header_C(const void *addr, DvmType rank, DvmType typeSize, ...); /* :81 */
+DvmType *dvmh_variable_get_header_C(const void *addr);                                     /* :86 */
+void dvmh_data_enter_C(const void *addr, DvmType size);                                    /* :87 */
+void dvmh_data_enter_(const void *addr, const DvmType *pSize);                             /* :88 */
+void dvmh_data_exit_C(const void *addr, DvmType saveFlag);                                 /* :89 */
+void dvmh_data_exit_(const void *addr, const DvmType *pSaveFlag);                          /* :90 */
+void *dvmh_malloc_C(size_t size);                                                          /* :91 */
+void *dvmh_calloc_C(size_t nmemb, size_t size);                                            /* :92 */
+void *dvmh_realloc_C(void *ptr, size_t size);                                              /* :93 */
+char *dvmh_strdup_C(const char *s);                                                        /* :94 */
+void dvmh_free_C(void *ptr);                                                               /* :95 */
 
 /* ---- addresses and headers ---- */
 void *dvmh_get_natural_base_C(DvmType deviceNum, const DvmType dvmDesc[]);                 /* :103 */
@@ -128,6 +150,8 @@ DvmType dvmh_fill_header_C(DvmType deviceNum, const void *baseAddr, const DvmTyp
 /* varargs: rank global indexes */
 DvmType dvmh_calc_linear_C(const DvmType dvmDesc[], DvmType rank, ...);                    /* :137 */
 void *dvmh_get_element_addr_C(const DvmType dvmDesc[], DvmType rank, ...);                 /* :140 */
+/* the element's address if this process owns it, else NULL (one process owns all) */
+void *dvmh_get_own_element_addr_C(const DvmType dvmDesc[], DvmType rank, ...);             /* :139 */
 
 /* ---- actuality ---- */
 void dvmh_get_actual_variable2_(void *addr);                                               /* :111 */
@@ -206,6 +230,23 @@ double dvmh_wtime(void);
 
 #ifdef __cplusplus
 }
+
+/* The module initialiser cdvmh emits for a translation unit with global
+ * regular variables (cdvmh/src/c_dvmh.cpp:204-222): its init function (data
+ * enter of the globals) runs when the runtime initialises, or at once if it
+ * already has; its finish function at dvmh_exit_C.  Same class layout and
+ * member signatures as the reference's, so generated code links unchanged.  (:236-247) */
+class DvmhModuleInitializer {
+public:
+    explicit DvmhModuleInitializer(void (*fInit)(), void (*fFinish)() = 0);
+    static void executeInit();
+    static void executeFinish();
+protected:
+    static DvmhModuleInitializer *head;
+    DvmhModuleInitializer *next;
+    void (*funcInit)();
+    void (*funcFinish)();
+};
 #endif
 #pragma GCC visibility pop
 

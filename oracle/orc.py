@@ -59,6 +59,7 @@ def lib():
         L.orc_jacperf.restype = ctypes.c_long
         L.orc_jacperf.argtypes = [ctypes.c_int, ctypes.c_long, ctypes.c_long, _fp, _fp, _fp]
         L.orc_max_threads.restype = ctypes.c_int
+        L.orc_cdvh2d.argtypes = [ctypes.c_long, ctypes.c_long, ctypes.c_uint64, _dp, _dp]
         _L = L
     return _L
 
@@ -79,6 +80,13 @@ def jacobi_run(rank, n, iters, seed, threads=1):
     A, B = jacobi_init(rank, n, seed)
     eps = [lib().orc_jacobi_step(rank, n, P(A), P(B), threads) for _ in range(iters)]
     return np.array(eps), A, B
+
+
+def cdvh2d_run(n, iters, seed):
+    """The weighted Jacobi 2-D program of workloads/cdvh2d.c: (eps per iteration, B)."""
+    eps, B = np.zeros(iters), np.zeros(n * n)
+    lib().orc_cdvh2d(n, iters, seed, P(eps), P(B))
+    return eps, B
 
 
 def sor_run(n, sweeps, omega, seed):

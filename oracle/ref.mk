@@ -46,7 +46,7 @@ all: $(OUT)/libdvm.a $(OUT)/libdvmh.a $(OUT)/pstub.o $(OUT)/ref_driver
 # The workload programs (same sources the GPU build uses, without CUDA handlers)
 # linked against the reference runtime: the order-exact oracle with DVMH_NUM_THREADS=1.
 WL      ?= dvm-snapshot-r6603-fork_gb300/workloads
-WL_SRC   = $(WL)/jac2d.c $(WL)/jac3d.c $(WL)/sor3d.c $(WL)/heat.c $(WL)/gsd2d.c $(WL)/genred.c $(WL)/rec2d.c $(WL)/gsd3d.c $(WL)/gs2d.c $(WL)/gen3d.c $(WL)/jacperf.c oracle/ref_driver.c
+WL_SRC   = $(WL)/jac2d.c $(WL)/jac3d.c $(WL)/sor3d.c $(WL)/heat.c $(WL)/gsd2d.c $(WL)/genred.c $(WL)/rec2d.c $(WL)/gsd3d.c $(WL)/gs2d.c $(WL)/gen3d.c $(WL)/jacperf.c $(WL)/cdvh2d.c $(WL)/cdvh2d_init.cpp oracle/ref_driver.c
 WL_CFLAGS = -O2 -fopenmp -ffp-contract=off -fno-fast-math -DWL_NO_CUDA -I$(REF)/rts/dvmh/include -I$(WL)
 
 $(OUT)/ref_driver: $(WL_SRC) $(WL)/wl_common.h $(OUT)/libdvm.a $(OUT)/libdvmh.a $(OUT)/pstub.o

@@ -23,6 +23,7 @@
  *   gsd2d        n0 n1 sweeps seed dir0 dir1 mirror
  *                -> m[sweeps] (read after every sweep), A[n0*n1], then B[n0*n1]
  *                   when mirror
+ *   cdvh2d       n iters seed           -> eps[iters], B[n*n]
  * Run with DVMH_NUM_THREADS=1 for the sequential (order-exact) oracle.
  */
 #include <stdio.h>
@@ -57,6 +58,7 @@ int wl_gsd3d_run(long n0, long n1, long n2, long sweeps, uint64_t seed, double *
 int wl_gs2d_run(long n, long sweeps, uint64_t seed, double *s_out, double *a_out);
 int wl_gsd2d_run(long n0, long n1, long sweeps, uint64_t seed, int dir0, int dir1, int readEach, int mirror,
                  double *m_out, double *a_out, double *b_out);
+int wl_cdvh2d_run(long n, long iters, unsigned long long seed, double *eps_out, double *b_out);
 
 static void put(FILE *f, const void *p, size_t bytes) {
     if (fwrite(p, 1, bytes, f) != bytes) {
@@ -215,6 +217,13 @@ int main(int argc, char **argv) {
         put(f, a, sizeof(double) * n0 * n1);
         if (mirror)
             put(f, b, sizeof(double) * n0 * n1);
+    } else if (!strcmp(argv[1], "cdvh2d")) {
+        long n = atol(argv[3]), iters = atol(argv[4]);
+        uint64_t seed = strtoull(argv[5], 0, 10);
+        double *e = malloc(sizeof(double) * iters), *b = malloc(sizeof(double) * n * n);
+        wl_cdvh2d_run(n, iters, seed, e, b);
+        put(f, e, sizeof(double) * iters);
+        put(f, b, sizeof(double) * n * n);
     } else {
         fprintf(stderr, "unknown program %s\n", argv[1]);
         return 2;

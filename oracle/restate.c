@@ -185,6 +185,39 @@ double orc_jacobi_step(int rank, long n, double *A, double *B, int nthreads) {
     return Max(eps, 0.0);
 }
 
+/*
+ * The weighted Jacobi 2-D program in cdvmh's converted form
+ * (dvm-snapshot-r6603-fork_gb300/workloads/cdvh2d.c): row weights w[i] =
+ * 0.5 + u(seed, 2, i) / 2, weights coef = {0.25, 0.125, 0.375, 0.25}; each
+ * iteration eps = Max(|B - A|, eps), A = B over the interior, then
+ * B = w[i] * (coef0 A[i-1][j] + coef1 A[i][j-1] + coef2 A[i][j+1] + coef3 A[i+1][j]),
+ * every operation in the source order.  eps_out[iters], B[n*n].
+ */
+void orc_cdvh2d(long n, long iters, uint64_t seed, double *eps_out, double *B) {
+    const double coef[4] = {0.25, 0.125, 0.375, 0.25};
+    double *A = (double *)malloc(sizeof(double) * n * n), *w = (double *)malloc(sizeof(double) * n);
+    long i, j, it;
+    orc_jacobi_init(2, n, seed, A, B);
+    for (i = 0; i < n; i++) w[i] = 0.5 + orc_u01(seed, 2, (uint64_t)i) / 2.0;
+    for (it = 0; it < iters; it++) {
+        double eps = 0.0;
+        for (i = 1; i <= n - 2; i++)
+            for (j = 1; j <= n - 2; j++) {
+                long c = i * n + j;
+                eps = Max(fabs(B[c] - A[c]), eps);
+                A[c] = B[c];
+            }
+        for (i = 1; i <= n - 2; i++)
+            for (j = 1; j <= n - 2; j++) {
+                long c = i * n + j;
+                B[c] = w[i] * (coef[0] * A[c - n] + coef[1] * A[c - 1] + coef[2] * A[c + 1] + coef[3] * A[c + n]);
+            }
+        eps_out[it] = Max(eps, 0.0);
+    }
+    free(A);
+    free(w);
+}
+
 /* ------------------------------------------------------------ SOR (ACROSS) */
 
 void orc_sor_init(long n, uint64_t seed, double *A) {

@@ -85,6 +85,11 @@ CASES = [
     ("gsd2d_4x30_back", "gsd2d", [4, 30, 2, 34, -1, -1, 1], True),
     ("gsd2d_96x200_mixed", "gsd2d", [96, 200, 4, 20261207, -1, 1, 1], False),
     ("gsd2d_257x129_fwd", "gsd2d", [257, 129, 3, 20261208, 1, 1, 0], False),
+    # cdvh2d: n iters seed (the program in cdvmh's converted form: regular variables, dynamic arrays)
+    ("cdvh2d_n12_it3", "cdvh2d", [12, 3, 5], True),
+    ("cdvh2d_n3_it2", "cdvh2d", [3, 2, 6], True),
+    ("cdvh2d_n97_it5", "cdvh2d", [97, 5, 20261212], False),
+    ("cdvh2d_n300_it4", "cdvh2d", [300, 4, 20261213], False),
 ]
 
 
@@ -175,6 +180,14 @@ def case(name, prog, params, full):
         rec["A_sha256"] = sha(A)
         if full:
             rec["A"] = hx(A)
+    elif prog == "cdvh2d":
+        n, it = params[0], params[1]
+        d = np.frombuffer(raw, dtype="<f8")
+        rec["eps"] = hx(d[:it])
+        B = d[it:it + n * n]
+        rec["B_sha256"] = sha(B)
+        if full:
+            rec["B"] = hx(B)
     elif prog == "gsd2d":
         n0, n1, sw, mirror = params[0], params[1], params[2], params[6]
         d = np.frombuffer(raw, dtype="<f8")
@@ -212,10 +225,19 @@ def case(name, prog, params, full):
 
 
 def main():
+    """All cases, or (arguments given) only the cases whose names start with one
+    of the arguments, kept beside the others already in golden.json."""
     build()
-    out = {"generator": "tests/golden/make_golden.py", "runtime": "reference host handlers, DVMH_NUM_THREADS=1",
-           "cases": {}}
+    path = os.path.join(ROOT, "tests", "golden", "golden.json")
+    only = sys.argv[1:]
+    if only and os.path.exists(path):
+        out = json.load(open(path))
+    else:
+        out = {"generator": "tests/golden/make_golden.py", "runtime": "reference host handlers, DVMH_NUM_THREADS=1",
+               "cases": {}}
     for name, prog, params, full in CASES:
+        if only and not any(name.startswith(o) for o in only):
+            continue
         print("case", name, file=sys.stderr)
         out["cases"][name] = case(name, prog, params, full)
     path = os.path.join(ROOT, "tests", "golden", "golden.json")

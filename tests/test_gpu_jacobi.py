@@ -130,7 +130,7 @@ def test_plain_mode_no_fusion(g):
     assert s["fused_pairs"] == 0 and s["graphs_captured"] == 0 and s["handler_calls"] == 6
 
 
-@pytest.mark.parametrize("variant", list(range(20)))
+@pytest.mark.parametrize("variant", list(range(25)))
 def test_jacobi3d_variants_vs_oracle(g, variant):
     """Every kernel variant of the 3-D loops (rows per thread x additions on the
     FP64 unit, the rest on the integer pipe; the fixed-point stencils; the
@@ -164,7 +164,7 @@ def _stencil_ref(A):
     return t / 6.0, c
 
 
-@pytest.mark.parametrize("variant", list(range(17)))
+@pytest.mark.parametrize("variant", list(range(22)))
 def test_jacobi3d_kernels_signs_and_tiny_values(g, variant):
     """The kernels directly through the C ABI on values that take every path:
     negative values (no integer-pipe additions for that CTA), values below
@@ -283,7 +283,7 @@ def test_subarray_actuality(g, mode):
     assert eps[0] == e_ref, mode
 
 
-@pytest.mark.parametrize("variant", [14, 15, 16])
+@pytest.mark.parametrize("variant", list(range(14, 22)))
 def test_jacobi3d_fixed_point_stencil_range_edges(g, variant):
     """The fixed-point stencil computes a plane on the FP64 unit when any value
     its cells read lies outside +0 and [2^-9, 1).  Values on both sides of

@@ -25,7 +25,7 @@ def jac_cases(golden):
 def test_golden_present(golden):
     progs = {v["prog"] for v in golden.values()}
     assert progs == {"jac2d", "jac3d", "sor3d", "heat", "gsd2d", "genred", "genredx", "rec2d", "gsd3d", "gs2d",
-                     "gen3d", "jacperf"}
+                     "gen3d", "jacperf", "cdvh2d"}
 
 
 # the reference examples' own verification (examples/Performance/jac3d_perf.c:92, jac2d_perf.c:89)
@@ -196,6 +196,21 @@ def test_genred_edge_values_vs_reference(golden):
         assert list(r[3:7]) == c["i4"], name
         assert float(r[7]).hex() == c["f1"][0], name
         assert r[8] == c["lc"], name
+
+
+def test_cdvh2d_vs_reference(golden):
+    """The program in cdvmh's converted form (regular variables, dynamic arrays):
+    eps per iteration and B bit-exact against the reference runtime."""
+    cases = [k for k, v in golden.items() if v["prog"] == "cdvh2d"]
+    assert len(cases) >= 4
+    for k in cases:
+        c = golden[k]
+        n, it, seed = c["params"]
+        eps, B = orc.cdvh2d_run(n, it, seed)
+        assert [float(x).hex() for x in eps] == c["eps"], k
+        assert sha(B) == c["B_sha256"], k
+        if "B" in c:
+            assert np.array_equal(B, unhex(c["B"])), k
 
 
 def test_pairwise_tree_identity():

@@ -18,7 +18,11 @@ import pytest
 pytestmark = pytest.mark.gpu
 
 
-def test_update_noalloc_matches_allocating_entry_point():
+@pytest.mark.parametrize("k_lo,k_hi", [(1, 129), (57, 57), (100, 130)])
+def test_update_noalloc_matches_allocating_entry_point(k_lo, k_hi):
+    """The whole interior; one column at an odd k (the pair's second element
+    alone); a box ending on the row's last element, whose pair reaches into
+    the row padding."""
     import torch
 
     import __graft_entry__ as ge
@@ -29,7 +33,7 @@ def test_update_noalloc_matches_allocating_entry_point():
     n = 131  # odd extent: ragged 64-wide segments; rows padded to an even length (16-byte aligned rows)
     w = n + 1
     LA = ctypes.c_long * 3
-    st, lo, hi = LA(n * w, w, 1), LA(1, 1, 1), LA(n - 2, n - 2, n - 2)
+    st, lo, hi = LA(n * w, w, 1), LA(1, 1, k_lo), LA(n - 2, n - 2, k_hi)
     stream = torch.cuda.current_stream()
     sp = ctypes.c_void_p(stream.cuda_stream)
     vp = lambda t: ctypes.c_void_p(t.data_ptr())
@@ -46,9 +50,12 @@ def test_update_noalloc_matches_allocating_entry_point():
         torch.cuda.synchronize()
         assert torch.equal(A1, A2), call
         assert eps.item() == eps_ref.item(), (call, eps.item(), eps_ref.item())
-        # the loop ran: interior of A is B's, the boundary untouched
-        assert torch.equal(A2[1:-1, 1:-1, 1:n - 1], B[1:-1, 1:-1, 1:n - 1])
+        # the loop ran: A is B's inside the box, untouched outside it
+        assert torch.equal(A2[1:-1, 1:-1, k_lo:k_hi + 1], B[1:-1, 1:-1, k_lo:k_hi + 1])
+        assert torch.equal(A2[1:-1, 1:-1, :k_lo], A[1:-1, 1:-1, :k_lo])
+        assert torch.equal(A2[1:-1, 1:-1, k_hi + 1:], A[1:-1, 1:-1, k_hi + 1:])
         assert torch.equal(A2[0], A[0])
+        assert eps_ref.item() == (B - A)[1:-1, 1:-1, k_lo:k_hi + 1].abs().max().item()
 
 
 def test_update_noalloc_rejects_unaligned_rows():
