@@ -495,18 +495,20 @@ __device__ __forceinline__ void planes3(const double *__restrict__ A, double *Ou
     const bool hrA = haloWarp && hr >= 0 && hr < b.e1;
     const long hro = hr * b.s1;
     const int hrIdx = ty == 0 ? 0 : TY + 1;
+    // what this thread loads in every plane, and from where: its element pair,
+    // its edge column (lanes 0 and 31), its halo row (warps 0 and TY-1)
+    const bool ownOk = jA && kA, edgeOk = jA && hcA, haloOk = hrA && kA;
+    const double *own = A + jo + k, *edge = A + jo + hc, *halo = A + hro + k;
 
-    auto ldP = [&](long ii, long joff, bool ja) -> double2 {
+    auto ldPair = [&](const double *p, bool ok) -> double2 {
         double2 v = make_double2(0.0, 0.0);
-        if (ja && kA && ii >= 0 && ii < b.e0) {
-            v = ld2(A + ii * b.s0 + joff + k);
+        if (ok) {
+            v = ld2(p);
             if (!kA1) v.y = 0.0;
         }
         return v;
     };
-    auto ldE = [&](long ii, long joff, bool ja) -> double {
-        return (ja && hcA && ii >= 0 && ii < b.e0) ? A[ii * b.s0 + joff + hc] : 0.0;
-    };
+    auto planeOk = [&](long ii) { return ii >= 0 && ii < b.e0; };
     // a loaded value in the CTA's representation (q61, or the double's bits)
     auto cv = [](double x, bool &bad) -> uint64_t {
         if (!Q) return sf::bits(x);
@@ -528,18 +530,20 @@ __device__ __forceinline__ void planes3(const double *__restrict__ A, double *Ou
 
     // planes ib-1, ib, ib+1 (own pair), the edge column of ib and ib+1, the halo row of ib and ib+1
     bool bad = false;
-    double2 t = ldP(ib - 1, jo, jA);
+    const long s0 = b.s0;
+    double2 t = ldPair(own + (ib - 1) * s0, ownOk && planeOk(ib - 1));
     uint64_t pmx = cv(t.x, bad), pmy = cv(t.y, bad);
-    t = ldP(ib, jo, jA);
+    t = ldPair(own + ib * s0, ownOk && planeOk(ib));
     uint64_t pcx = cv(t.x, bad), pcy = cv(t.y, bad);
-    t = ldP(ib + 1, jo, jA);
+    t = ldPair(own + (ib + 1) * s0, ownOk && planeOk(ib + 1));
     uint64_t ppx = cv(t.x, bad), ppy = cv(t.y, bad);
-    uint64_t ec = cv(ldE(ib, jo, jA), bad), ep = cv(ldE(ib + 1, jo, jA), bad);
+    uint64_t ec = cv(edgeOk && planeOk(ib) ? edge[ib * s0] : 0.0, bad);
+    uint64_t ep = cv(edgeOk && planeOk(ib + 1) ? edge[(ib + 1) * s0] : 0.0, bad);
     uint64_t hpx = 0, hpy = 0;
     if (haloWarp) {
-        t = ldP(ib, hro, hrA);
+        t = ldPair(halo + ib * s0, haloOk && planeOk(ib));
         sm[0][hrIdx][lane] = make_ulonglong2(cv(t.x, bad), cv(t.y, bad));
-        t = ldP(ib + 1, hro, hrA);
+        t = ldPair(halo + (ib + 1) * s0, haloOk && planeOk(ib + 1));
         hpx = cv(t.x, bad);
         hpy = cv(t.y, bad);
     }
@@ -547,12 +551,23 @@ __device__ __forceinline__ void planes3(const double *__restrict__ A, double *Ou
     // flags of planes i-1, i, i+1 in bits 2, 1, 0 (the first three merged)
     unsigned flags = __syncthreads_or(bad) ? 7u : 0u;
     int cur = 0;
-    for (long i = ib; i <= ie; i++) {
+    // plane pointers of plane i+2 (loads) and plane i (stores), bumped by one plane per step;
+    // plane i+2 exists for the first `nload` steps
+    const int nplanes = (int)(ie - ib + 1);
+    const int nload = (int)(b.e0 - (ib + 2) < (long)nplanes ? b.e0 - (ib + 2) : (long)nplanes);
+    const double *qOwn = own + (ib + 2) * s0, *qEdge = edge + (ib + 2) * s0, *qHalo = halo + (ib + 2) * s0;
+    double *out = Out + ib * s0 + jo + k;
+    long i = ib;
+    for (int step = 0; step < nplanes; step++, i++) {
         // plane i+2 in flight
-        const double2 q = ldP(i + 2, jo, jA);
-        const double eqd = ldE(i + 2, jo, jA);
+        const bool more = step < nload;
+        const double2 q = ldPair(qOwn, ownOk && more);
+        const double eqd = (edgeOk && more) ? *qEdge : 0.0;
         double2 hq = make_double2(0.0, 0.0);
-        if (haloWarp) hq = ldP(i + 2, hro, hrA);
+        if (haloWarp) hq = ldPair(qHalo, haloOk && more);
+        qOwn += s0;
+        qEdge += s0;
+        qHalo += s0;
 
         // plane i
         double v0, v1;
@@ -569,11 +584,11 @@ __device__ __forceinline__ void planes3(const double *__restrict__ A, double *Ou
             v1 = (jI && kI1) ? nativeCell(i, k + 1) : 0.0;
         }
         if (jI) {
-            const long off = i * b.s0 + jo + k;
-            if (kI0 && kI1) st2cs(Out + off, make_double2(v0, v1));
-            else if (kI0) Out[off] = v0;
-            else if (kI1) Out[off + 1] = v1;
+            if (kI0 && kI1) st2cs(out, make_double2(v0, v1));
+            else if (kI0) out[0] = v0;
+            else if (kI1) out[1] = v1;
         }
+        out += s0;
 
         // plane i+2 converted; plane i+1 staged; one barrier; rotate
         bad = false;
@@ -596,13 +611,33 @@ __device__ __forceinline__ void planes3(const double *__restrict__ A, double *Ou
     }
 }
 
-// nat of every den CTAs (by linear block index) native, the others fixed point
-template <int MINB>
+// CTAs started on each SM (any starting value: only its residue matters); the
+// share of native CTAs is counted per SM, so that every SM runs both kinds at
+// once -- a split by block index alone can put all native CTAs on some SMs
+// (consecutive blocks of the same residue land on the same SM).  Launches that
+// run at the same time share the counters; that only shifts the pattern.
+__device__ unsigned ctaSlots[1024];
+
+// nat of every den CTAs started on an SM native, the others fixed point (MIX =
+// false: all fixed point, and only that path compiled)
+template <int MINB, bool MIX>
 __global__ void __launch_bounds__(TX *TY, MINB) kStencil3Q(const double *__restrict__ A, double *Out, Box3 b,
                                                              long p0, int ichunk, int nat, int den) {
     __shared__ ulonglong2 sm[2][TY + 2][TX];
-    const unsigned cta = blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z);
-    if ((int)(cta % (unsigned)den) < nat) planes3<false>(A, Out, b, p0, ichunk, sm);
+    if (!MIX) {
+        planes3<true>(A, Out, b, p0, ichunk, sm);
+        return;
+    }
+    __shared__ int native;
+    if (nat > 0) {
+        if (threadIdx.x == 0 && threadIdx.y == 0) {
+            unsigned smid;
+            asm volatile("mov.u32 %0, %%smid;" : "=r"(smid));
+            native = (int)(atomicAdd(&ctaSlots[smid & 1023u], 1u) % (unsigned)den) < nat;
+        }
+        __syncthreads();
+    }
+    if (nat > 0 && native) planes3<false>(A, Out, b, p0, ichunk, sm);
     else planes3<true>(A, Out, b, p0, ichunk, sm);
 }
 
@@ -859,7 +894,7 @@ void launch3(int variant, const St3Geom &g, double *A, const double *B, double *
     case 12: kStencil3<FUSED, 5, 1, 3><<<g.grid, blk, 0, s>>>(A, B, Out, b, g.p0, g.ichunk, items); break;
     case 13: kStencil3<FUSED, 5, 1, 4><<<g.grid, blk, 0, s>>>(A, B, Out, b, g.p0, g.ichunk, items); break;
 #define CQ(V, M, N, D) \
-    case V: if (!FUSED) kStencil3Q<M><<<g.grid, blk, 0, s>>>(A, Out, b, g.p0, g.ichunk, N, D); break;
+    case V: if (!FUSED) kStencil3Q<M, (N > 0)><<<g.grid, blk, 0, s>>>(A, Out, b, g.p0, g.ichunk, N, D); break;
         CQ(14, 4, 0, 1) CQ(15, 3, 0, 1) CQ(16, 4, 1, 2) CQ(17, 4, 1, 3) CQ(18, 4, 2, 5) CQ(19, 3, 1, 2)
         CQ(20, 4, 1, 4) CQ(21, 4, 3, 5)
 #undef CQ

@@ -355,6 +355,7 @@ bool isLive(Obj *o, uint32_t kind);
 void trackObj(Obj *o);
 void untrackObj(Obj *o);
 void varDrop(Var *v);     // forget a variable, its device copy and the graphs that name it
+bool varInRegion(const Var *v);  // registered in the current region
 // a new array on the caller's descriptor, or on its own header for desc == null
 // (sizes per axis, shadow widths); no storage yet
 Array *arrayNew(DvmType desc[], int rank, DvmType typeSize, const long ext[], const long shLo[], const long shHi[]);

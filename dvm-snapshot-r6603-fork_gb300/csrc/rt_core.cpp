@@ -201,6 +201,8 @@ static bool inCurrentRegion(const Var *v) {
     return false;
 }
 
+bool varInRegion(const Var *v) { return inCurrentRegion(v); }
+
 // Variables known from earlier regions and loops that overlap [lo, hi), other
 // than `keep`: the program's memory there now holds something else, so unless
 // the current region registered them they are forgotten, device copies and

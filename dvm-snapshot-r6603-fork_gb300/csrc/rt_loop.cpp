@@ -690,7 +690,13 @@ void dvmh_loop_reduction_C(DvmType curLoop, DvmType redType, void *arrayAddr, Dv
     r.init.assign(r.addr, r.addr + r.esize * r.count);
     if (loc) r.initLoc.assign(r.locAddr, r.locAddr + r.locSize * r.count);
     // the result lives in the variable's device copy; a variable the region did
-    // not register becomes known here and is written back at loop end
+    // not register becomes known here and is written back at loop end.  Such a
+    // variable is the program's host memory to the reference, which reads the
+    // initial value from it here: while its host copy is current the program
+    // may have written it since, so the device copy is refreshed from it; after
+    // a loop left a newer result on the device (async and batched modes, no
+    // get_actual since), that result is the initial value.  A variable the
+    // region registered follows the region's actuality.
     size_t off = 0;
     Var *v = varAt(r.addr, &off);
     if (!v) {
@@ -701,7 +707,7 @@ void dvmh_loop_reduction_C(DvmType curLoop, DvmType redType, void *arrayAddr, Dv
     r.var = v;
     r.varOff = off;
     ensureVarDev(v);
-    if (!v->devActual) {
+    if (!v->devActual || (v->hostActual && !varInRegion(v))) {
         varH2D(v);
         v->devActual = true;
     }
@@ -715,7 +721,7 @@ void dvmh_loop_reduction_C(DvmType curLoop, DvmType redType, void *arrayAddr, Dv
         r.locVar = lv;
         r.locVarOff = loff;
         ensureVarDev(lv);
-        if (!lv->devActual) {
+        if (!lv->devActual || (lv->hostActual && !varInRegion(lv))) {
             varH2D(lv);
             lv->devActual = true;
         }

@@ -80,3 +80,86 @@ def test_learned_tuner_beats_untrained_methods(rt):
     assert r["ratio_geomean"] <= r["random_k_ratio_geomean"], r
     assert r["ratio_geomean"] < r["default_block_ratio_geomean"], r
     assert r["within_5pct"] >= r["random_k_within_5pct"], r
+
+
+def _variant_info(rt):
+    rt.dvmhgb_tuner_variant_count.restype = ctypes.c_long
+    H = ctypes.c_void_p()
+    nv, ch, ex = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+    es = ctypes.c_double()
+    best = (ctypes.c_double * 64)()
+    out = []
+    for i in range(int(rt.dvmhgb_tuner_variant_count())):
+        assert rt.dvmhgb_tuner_variant_info(ctypes.c_long(i), ctypes.byref(H), ctypes.byref(nv), ctypes.byref(ch),
+                                            best, 64, ctypes.byref(ex), ctypes.byref(es)) == 0
+        out.append({"handler": H.value, "n": nv.value, "chosen": ch.value, "best": list(best[:nv.value]),
+                    "explored": ex.value, "seconds": es.value})
+    return out
+
+
+def test_variant_tuning_in_batched_mode_keeps_results_and_the_fastest(rt):
+    """Exhaustive variant tuning of the Jacobi-3D pair in batched mode: while
+    variants are being tried the flushes run uncaptured (one variant per step),
+    every variant is timed once, the fastest is kept and captured; every step,
+    whichever variant ran it, is bit-exact against the oracle."""
+    from oracle import orc
+    _, g = ge.package()
+    n, steps, seed = 34, 30, 21
+    e_ref, A_ref, B_ref = orc.jacobi_run(3, n, steps, seed)
+    g.set_mode("batched")
+    rt.dvmhgb_tuner_reset()
+    rt.dvmhgb_set_tuning(1)
+    try:
+        j = g.Jacobi(3, n, seed)
+        g.reset_stats()
+        eps = j.run(steps)
+        A, B = j.fetch()
+        j.close()
+        st = g.stats()
+        info = _variant_info(rt)
+    finally:
+        rt.dvmhgb_set_tuning(0)
+        rt.dvmhgb_tuner_reset()
+    assert np.array_equal(eps, e_ref) and np.array_equal(A, A_ref) and np.array_equal(B, B_ref)
+    fused = ctypes.cast(g.workloads().loop_jac3d_fused_cuda, ctypes.c_void_p).value
+    rec = [r for r in info if r["handler"] == fused]
+    assert len(rec) == 1, info
+    r = rec[0]
+    assert r["n"] == 25 and r["explored"] == 25 and all(b > 0 for b in r["best"]), r
+    assert r["chosen"] == int(np.argmin(r["best"])), r
+    assert st["graphs_captured"] >= 1 and st["graph_replays"] >= 1, st  # captured once the search ended
+
+
+def test_variant_model_prunes_the_search(rt):
+    """Model-guided variant tuning: with a variant model installed the runtime
+    tries only floor(0.1 n) variants in the model's order (2 of the pair's 25)
+    and keeps the faster of them; results stay bit-exact."""
+    from oracle import orc
+    _, g = ge.package()
+    P = rt.dvmhgb_mlp_nparams()
+    fp = ctypes.POINTER(ctypes.c_float)
+    rng = np.random.default_rng(4)
+    params = (0.05 * rng.standard_normal(P)).astype(np.float32)
+    mean, std = np.zeros(24, dtype=np.float32), np.ones(24, dtype=np.float32)
+    assert rt.dvmhgb_tuner_set_variant_model(params.ctypes.data_as(fp), mean.ctypes.data_as(fp),
+                                             std.ctypes.data_as(fp)) == 0
+    n, steps, seed = 34, 8, 22
+    e_ref, A_ref, B_ref = orc.jacobi_run(3, n, steps, seed)
+    g.set_mode("batched")
+    rt.dvmhgb_tuner_reset()
+    rt.dvmhgb_set_tuning(2)
+    try:
+        j = g.Jacobi(3, n, seed)
+        eps = j.run(steps)
+        A, B = j.fetch()
+        j.close()
+        info = _variant_info(rt)
+    finally:
+        rt.dvmhgb_set_tuning(0)
+        rt.dvmhgb_tuner_reset()
+    assert np.array_equal(eps, e_ref) and np.array_equal(A, A_ref) and np.array_equal(B, B_ref)
+    fused = ctypes.cast(g.workloads().loop_jac3d_fused_cuda, ctypes.c_void_p).value
+    r = [x for x in info if x["handler"] == fused][0]
+    tried = [v for v, b in enumerate(r["best"]) if b > 0]
+    assert r["explored"] == 2 and len(tried) == 2, r
+    assert r["chosen"] in tried and r["best"][r["chosen"]] == min(r["best"][v] for v in tried), r
