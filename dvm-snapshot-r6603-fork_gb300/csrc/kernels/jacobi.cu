@@ -611,6 +611,196 @@ __device__ __forceinline__ void planes3(const double *__restrict__ A, double *Ou
     }
 }
 
+// The update and stencil loops in one pass with the fixed-point sums
+// (kStencil3QF): eps = Max(|B - A|, eps); A = B over the box, then
+// Bnew = (6 neighbours of A_new) / 6 with A_new = B inside the box and A
+// outside it.  The stencil part is planes3's (q61 sums; planes whose
+// neighbourhood leaves the fixed-point range on the FP64 unit).  The update
+// of a plane of the chunk is done when that plane's values are converted:
+// A_old, loaded beside B, enters |B - A_old| -- exact as a difference of q61
+// values, rounded once at the end (RN is monotone and odd, so
+// RN(max |b - a|) = max |RN(b - a)|), or on the FP64 unit for a value outside
+// the range -- and B is stored into A.  Nothing reads A inside the box
+// afterwards (the stencil's source there is B), so the early store is safe.
+// 32 bytes per cell: A and B read, A and Bnew written.
+template <int MINB>
+__global__ void __launch_bounds__(TX *TY, MINB) kStencil3QF(double *A, const double *__restrict__ B, double *Out,
+                                                              Box3 b, long p0, int ichunk, double *items) {
+    __shared__ ulonglong2 sm[2][TY + 2][TX];
+    __shared__ double shr[TY];
+    const int lane = threadIdx.x, ty = threadIdx.y;
+    const long kb = 2 * (p0 + (long)blockIdx.x * TX);
+    const long jb = b.lo1 + (long)blockIdx.y * TY;
+    const long ib = b.lo0 + (long)blockIdx.z * ichunk;
+    const long ie = ib + ichunk - 1 < b.hi0 ? ib + ichunk - 1 : b.hi0;
+    const long k = kb + 2 * lane;
+    const bool kA = k < b.e2, kA1 = k + 1 < b.e2;  // k >= 0 always
+    const bool kI0 = k >= b.lo2 && k <= b.hi2, kI1 = k + 1 >= b.lo2 && k + 1 <= b.hi2;
+    const bool edgeLane = lane == 0 || lane == TX - 1;
+    const long hc = lane == 0 ? kb - 1 : kb + 2 * TX;
+    const bool hcA = edgeLane && hc >= 0 && hc < b.e2, hcI = hc >= b.lo2 && hc <= b.hi2;
+    const long j = jb + ty;
+    const long jo = j * b.s1;
+    const bool jA = j < b.e1, jI = j <= b.hi1;  // j >= lo1 always
+    const bool haloWarp = ty == 0 || ty == TY - 1;
+    const long hr = ty == 0 ? jb - 1 : jb + TY;
+    const bool hrA = haloWarp && hr >= 0 && hr < b.e1, hrI = hr >= b.lo1 && hr <= b.hi1;
+    const long hro = hr * b.s1;
+    const int hrIdx = ty == 0 ? 0 : TY + 1;
+    const long s0 = b.s0;
+
+    auto planeOk = [&](long ii) { return ii >= 0 && ii < b.e0; };
+    auto planeIn = [&](long ii) { return ii >= b.lo0 && ii <= b.hi0; };
+    // the stencil's source pair at plane ii, row offset roff: B inside the box, A outside (0 beyond the array)
+    auto srcPair = [&](long ii, long roff, bool ok, bool rowIn) -> double2 {
+        double2 v = make_double2(0.0, 0.0);
+        if (ok && planeOk(ii)) {
+            const long off = ii * s0 + roff + k;
+            const bool iin = planeIn(ii) && rowIn;
+            const bool in0 = iin && kI0, in1 = iin && kI1;
+            if (in0 && in1) {
+                v = ld2(B + off);
+            } else {
+                v = ld2(A + off);
+                if (in0 || in1) {
+                    const double2 w = ld2(B + off);
+                    if (in0) v.x = w.x;
+                    if (in1) v.y = w.y;
+                }
+            }
+            if (!kA1) v.y = 0.0;
+        }
+        return v;
+    };
+    auto srcEdge = [&](long ii) -> double {
+        if (!(jA && hcA && planeOk(ii))) return 0.0;
+        const long off = ii * s0 + jo + hc;
+        return (planeIn(ii) && jI && hcI) ? B[off] : A[off];
+    };
+    auto srcAt = [&](long i, long jj, long kk) -> double {
+        if (!inArr3(b, i, jj, kk)) return 0.0;
+        const long off = i * s0 + jj * b.s1 + kk;
+        return inBox3(b, i, jj, kk) ? B[off] : A[off];
+    };
+    auto cv = [](double x, bool &bad) -> uint64_t {
+        bad |= !sf::q61_ok(x);
+        return sf::q61(x);
+    };
+    auto nativeCell = [&](long i, long kk) -> double {
+        const double a = srcAt(i - 1, j, kk), bb = srcAt(i, j - 1, kk), c = srcAt(i, j, kk - 1);
+        const double d = srcAt(i, j, kk + 1), e = srcAt(i, j + 1, kk), f = srcAt(i + 1, j, kk);
+        return sf::div3p2(sf::nadd(sf::nadd(sf::nadd(sf::nadd(sf::nadd(a, bb), c), d), e), f), 1);
+    };
+    // the update loop on the own pair of plane ii, a plane of this chunk (inside the box):
+    // eps = Max(|B - A|, eps) and A = B for the pair's elements in the box
+    uint64_t qmax = 0, mb = 0;  // eps: fixed-point part, FP64-unit part (bit pattern)
+    bool seen = false;
+    const bool ownUpd = jA && kA && jI && (kI0 || kI1);
+    auto aOld = [&](long ii) -> double2 {
+        return (ownUpd && ii >= ib && ii <= ie) ? ld2(A + ii * s0 + jo + k) : make_double2(0.0, 0.0);
+    };
+    auto update = [&](long ii, double2 bs, double2 ao) {
+        if (!ownUpd || ii < ib || ii > ie) return;
+        const bool ok0 = sf::q61_ok(bs.x) && sf::q61_ok(ao.x), ok1 = sf::q61_ok(bs.y) && sf::q61_ok(ao.y);
+        const uint64_t b0 = sf::q61(bs.x), a0 = sf::q61(ao.x), b1 = sf::q61(bs.y), a1 = sf::q61(ao.y);
+        const uint64_t d0 = b0 > a0 ? b0 - a0 : a0 - b0, d1 = b1 > a1 ? b1 - a1 : a1 - b1;
+        if (kI0 && ok0 && d0 > qmax) qmax = d0;
+        if (kI1 && ok1 && d1 > qmax) qmax = d1;
+        if ((kI0 && !ok0) || (kI1 && !ok1)) {  // rare: a value outside the fixed-point range
+            if (kI0 && !ok0) mb = sf::absmax_bits(sf::nadd(bs.x, -ao.x), mb);
+            if (kI1 && !ok1) mb = sf::absmax_bits(sf::nadd(bs.y, -ao.y), mb);
+        }
+        seen = true;
+        double *pa = A + ii * s0 + jo + k;
+        if (kI0 && kI1) st2cs(pa, bs);
+        else if (kI0) pa[0] = bs.x;
+        else pa[1] = bs.y;
+    };
+
+    // planes ib-1, ib, ib+1 (own pair), the edge column of ib and ib+1, the halo row of ib and ib+1;
+    // the update of planes ib and ib+1
+    bool bad = false;
+    double2 t = srcPair(ib - 1, jo, jA && kA, jI);
+    uint64_t pmx = cv(t.x, bad), pmy = cv(t.y, bad);
+    const double2 tc = srcPair(ib, jo, jA && kA, jI), ac = aOld(ib);
+    const double2 tp = srcPair(ib + 1, jo, jA && kA, jI), ap = aOld(ib + 1);
+    uint64_t pcx = cv(tc.x, bad), pcy = cv(tc.y, bad);
+    uint64_t ppx = cv(tp.x, bad), ppy = cv(tp.y, bad);
+    update(ib, tc, ac);
+    update(ib + 1, tp, ap);
+    uint64_t ec = cv(srcEdge(ib), bad), ep = cv(srcEdge(ib + 1), bad);
+    uint64_t hpx = 0, hpy = 0;
+    if (haloWarp) {
+        t = srcPair(ib, hro, hrA && kA, hrI);
+        sm[0][hrIdx][lane] = make_ulonglong2(cv(t.x, bad), cv(t.y, bad));
+        t = srcPair(ib + 1, hro, hrA && kA, hrI);
+        hpx = cv(t.x, bad);
+        hpy = cv(t.y, bad);
+    }
+    sm[0][1 + ty][lane] = make_ulonglong2(pcx, pcy);
+    unsigned flags = __syncthreads_or(bad) ? 7u : 0u;  // planes i-1, i, i+1 in bits 2, 1, 0
+    int cur = 0;
+    for (long i = ib; i <= ie; i++) {
+        // plane i+2 in flight: the source, and A_old where it is a plane of this chunk
+        const double2 q = srcPair(i + 2, jo, jA && kA, jI);
+        const double2 aq = aOld(i + 2);
+        const double eqd = srcEdge(i + 2);
+        double2 hq = make_double2(0.0, 0.0);
+        if (haloWarp) hq = srcPair(i + 2, hro, hrA && kA, hrI);
+
+        // plane i
+        double v0, v1;
+        if (flags == 0) {
+            const ulonglong2 up = sm[cur][ty][lane], dn = sm[cur][ty + 2][lane];
+            uint64_t left = __shfl_up_sync(0xffffffffu, pcy, 1), right = __shfl_down_sync(0xffffffffu, pcx, 1);
+            if (lane == 0) left = ec;
+            if (lane == TX - 1) right = ec;
+            // (((((A[i-1] + A[j-1]) + A[k-1]) + A[k+1]) + A[j+1]) + A[i+1]) / 6, left to right
+            v0 = sf::q61_div6(sf::q61_add(
+                sf::q61_add(sf::q61_add(sf::q61_add(sf::q61_add(pmx, up.x), left), pcy), dn.x), ppx));
+            v1 = sf::q61_div6(sf::q61_add(
+                sf::q61_add(sf::q61_add(sf::q61_add(sf::q61_add(pmy, up.y), pcx), right), dn.y), ppy));
+        } else {  // rare: a value outside the fixed-point range near this plane
+            v0 = (jI && kI0) ? nativeCell(i, k) : 0.0;
+            v1 = (jI && kI1) ? nativeCell(i, k + 1) : 0.0;
+        }
+        if (jI) {
+            double *out = Out + i * s0 + jo + k;
+            if (kI0 && kI1) st2cs(out, make_double2(v0, v1));
+            else if (kI0) out[0] = v0;
+            else if (kI1) out[1] = v1;
+        }
+
+        // plane i+2: updated (when it is this chunk's) and converted; plane i+1 staged; one barrier; rotate
+        update(i + 2, q, aq);
+        bad = false;
+        const uint64_t qx = cv(q.x, bad), qy = cv(q.y, bad), eq = cv(eqd, bad);
+        uint64_t hqx = 0, hqy = 0;
+        if (haloWarp) {
+            hqx = cv(hq.x, bad);
+            hqy = cv(hq.y, bad);
+            sm[cur ^ 1][hrIdx][lane] = make_ulonglong2(hpx, hpy);
+        }
+        sm[cur ^ 1][1 + ty][lane] = make_ulonglong2(ppx, ppy);
+        flags = ((flags << 1) | (__syncthreads_or(bad) ? 1u : 0u)) & 7u;
+        cur ^= 1;
+        pmx = pcx, pmy = pcy;
+        pcx = ppx, pcy = ppy;
+        ppx = qx, ppy = qy;
+        ec = ep, ep = eq;
+        hpx = hqx, hpy = hqy;
+    }
+    // RN(max |b - a|) from the fixed-point part, then the MAX with the FP64-unit part
+    double m = -__builtin_huge_val();
+    if (seen) {
+        const double qd = __ull2double_rn(qmax) * 0x1p-61;
+        const double f = sf::from(mb);
+        m = qd > f ? qd : f;
+    }
+    m = ctaMax(m, shr);
+    if (ty == 0 && lane == 0) items[blockIdx.x + gridDim.x * ((long)blockIdx.y + (long)gridDim.y * blockIdx.z)] = m;
+}
+
 // CTAs started on each SM (any starting value: only its residue matters); the
 // share of native CTAs is counted per SM, so that every SM runs both kinds at
 // once -- a split by block index alone can put all native CTAs on some SMs
@@ -881,6 +1071,10 @@ constexpr int V3_UNFUSED = V3, UNFUSED_STN = 13;
 // the first plane of the next chunk), and nothing an update reads is written
 // by a stencil running beside it
 constexpr int V3_OVERLAP = V3 + 1, V3_OVERLAP_Q = V3 + 2, OVL_CHUNKS = 8;
+// ... and the one-pass fixed-point pair (kStencil3QF), registers capped for
+// four / three CTAs per SM
+constexpr int V3_QF = V3 + 3;
+bool isQF(int v) { return v == V3_QF || v == V3_QF + 1; }
 
 template <bool FUSED>
 void launch3(int variant, const St3Geom &g, double *A, const double *B, double *Out, const Box3 &b, double *items,
@@ -1010,6 +1204,10 @@ int runOverlap(double *A, const double *B, const long st[3], const long ext[3], 
 long dvmhgb_jac3d_fused_items(const long lo[3], const long hi[3], int native) {
     if (native == V3_UNFUSED || isQ3(native)) return dvmhgb_jac3d_update_items(lo, hi);
     if (native == V3_OVERLAP || native == V3_OVERLAP_Q) return ovlItems(lo, hi);
+    if (isQF(native)) {
+        St3Geom g = st3Geom(lo, hi, TY);
+        return (long)g.grid.x * g.grid.y * g.grid.z;
+    }
     if (native < 0 || native >= V3) return -1;
     St3Geom g = st3Geom(lo, hi, TY * jtOf3(native));
     return (long)g.grid.x * g.grid.y * g.grid.z;
@@ -1030,6 +1228,21 @@ int dvmhgb_jac3d_fused(double *A, const double *B, double *Bnew, const long st[3
                           (cudaStream_t)stream);
     }
     if (Bnew == B) return -1;  // the fused kernel reads B while it writes the next B
+    if (isQF(native)) {
+        St3Geom g = st3Geom(lo, hi, TY);
+        if (!g.ok || !A || !B || !Bnew || !items || !rows16(st, 3) || !aligned16(A) || !aligned16(B) ||
+            !aligned16(Bnew))
+            return -1;
+        Box3 b{st[0], st[1], ext[0], ext[1], ext[2], lo[0], lo[1], lo[2], hi[0], hi[1], hi[2]};
+        dim3 blk(TX, TY);
+        if (native == V3_QF)
+            kStencil3QF<4><<<g.grid, blk, 0, (cudaStream_t)stream>>>(A, B, Bnew, b, g.p0, g.ichunk, items);
+        else
+            kStencil3QF<3><<<g.grid, blk, 0, (cudaStream_t)stream>>>(A, B, Bnew, b, g.p0, g.ichunk, items);
+        dvmhgb_count_launches(1);
+        if (cudaGetLastError() != cudaSuccess) return -1;
+        return dvmhgb_copy_outside_box(3, B, Bnew, st, ext, lo, hi, stream);
+    }
     if (native < 0 || native >= V3) return -1;
     St3Geom g = st3Geom(lo, hi, TY * jtOf3(native));
     if (!g.ok || !A || !B || !Bnew || !items || !rows16(st, 3) || !aligned16(A) || !aligned16(B) || !aligned16(Bnew))

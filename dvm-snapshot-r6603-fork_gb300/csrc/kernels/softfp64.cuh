@@ -389,11 +389,30 @@ SF_HD bool q61_ok(double x) {
     return (h >> 20) - 1014u <= 8u || bits(x) == 0;  // exponent field 1014..1022 and sign clear, or +0
 }
 
-// x * 2^61 for a q61_ok x (an arbitrary value for any other x)
+// the high word of (hi:lo) << sh and the low word of (hi:lo) >> sh, sh < 32
+SF_HD uint32_t fshl(uint32_t lo, uint32_t hi, uint32_t sh) {
+#ifdef __CUDA_ARCH__
+    return __funnelshift_l(lo, hi, sh);
+#else
+    return (uint32_t)(((((uint64_t)hi << 32) | lo) << sh) >> 32);
+#endif
+}
+SF_HD uint32_t fshr(uint32_t lo, uint32_t hi, uint32_t sh) {
+#ifdef __CUDA_ARCH__
+    return __funnelshift_r(lo, hi, sh);
+#else
+    return (uint32_t)((((uint64_t)hi << 32) | lo) >> sh);
+#endif
+}
+
+// x * 2^61 for a q61_ok x (an arbitrary value for any other x): the
+// significand shifted left by the exponent field - 1014 (0..8)
 SF_HD uint64_t q61(double x) {
-    uint64_t X = bits(x);
-    uint32_t e = hi32(X) >> 20;
-    uint64_t m = ((X & MANT) | HID) << ((e - 1014u) & 63u);
+    const uint64_t X = bits(x);
+    const uint32_t h = hi32(X), l = (uint32_t)X;
+    const uint32_t sh = ((h >> 20) - 1014u) & 31u;
+    const uint32_t mh = (h & 0xFFFFFu) | 0x100000u;  // the significand's high word with the hidden bit
+    const uint64_t m = ((uint64_t)fshl(l, mh, sh) << 32) | (uint32_t)(l << sh);
     return X == 0 ? 0 : m;
 }
 
@@ -422,21 +441,29 @@ SF_HD uint64_t q61_add(uint64_t s, uint64_t t) {
 }
 
 // RN((s * 2^-61) / 6) for a q61 value s with at most 53 significant bits
+// that is 0 or at least 2^32 -- every sum of q61 values is: a nonzero q61
+// value is at least 2^52 (2^-9 * 2^61).  The quotient's significand comes
+// from floor(n / 3) of s normalised to bit 63 (the multiply-high reciprocal
+// identity), its rounding from the bits below and the remainder.
 SF_HD double q61_div6(uint64_t s) {
-    const int c = clz64(s | 1);  // s == 0 is handled at the end
-    const uint64_t n = s << c;   // leading one at bit 63
+    const uint32_t sh_ = hi32(s), sl = (uint32_t)s;
+    const int c = 31 - msb32(sh_);  // leading zeros of s (32 for s == 0, handled at the end)
+    const uint32_t cc = (uint32_t)c & 31u;
+    const uint64_t n = ((uint64_t)fshl(sl, sh_, cc) << 32) | (uint32_t)(sl << cc);  // leading one at bit 63
     const uint64_t q = mulhi(n, 0xAAAAAAAAAAAAAAABull) >> 1;  // floor(n / 3), in [2^61, 2^63)
-    const uint64_t r = n - 3 * q;
-    const bool top = (q >> 62) != 0;
-    const int sh = top ? 10 : 9;
-    uint64_t m = q >> sh;
-    const uint64_t guard = (q >> (sh - 1)) & 1;
-    const uint64_t sticky = (q & ((1ull << (sh - 1)) - 1)) | r;
-    m += guard & (uint64_t)((sticky != 0) | (m & 1));
-    const uint64_t e = (uint64_t)((top ? 1023 : 1022) - c);  // exponent field of the quotient
+    const uint32_t r = (uint32_t)n - 3u * (uint32_t)q;         // n - 3q, in {0, 1, 2}
+    const uint32_t qh = hi32(q), ql = (uint32_t)q;
+    const uint32_t top = qh >> 30;  // q >= 2^62: the significand is q's bits 62..10, else 61..9
+    const uint32_t sh = 9u + top;
+    const uint32_t mh = qh >> sh, ml = fshr(ql, qh, sh);
+    const uint32_t guard = (ql >> (sh - 1u)) & 1u;
+    const uint32_t sticky = (ql & ((1u << (sh - 1u)) - 1u)) | r;
+    const uint32_t inc = guard & (uint32_t)((sticky != 0) | (ml & 1u));
+    const uint64_t m = (((uint64_t)mh << 32) | ml) + inc;
+    const uint32_t e = (top ? 1023u : 1022u) - (uint32_t)c;  // exponent field of the quotient
     // the significand's leading one adds 1 to the exponent field; a rounding
     // carry to 2^53 adds 2, which is the next binade with a zero significand
-    const uint64_t res = ((e - 1) << 52) + m;
+    const uint64_t res = ((uint64_t)(e - 1u) << 52) + m;
     return from(s == 0 ? 0 : res);
 }
 

@@ -57,6 +57,7 @@ static void rankByVariantModel(const std::vector<std::vector<float>> &feats, std
 
 struct VariantState {
     std::map<int, double> best;  // variant -> best seconds seen
+    std::map<int, int> runs;     // variant -> timed executions
     int nvariants = 0;
     int chosen = -1;
     std::vector<int> order;      // model-guided: variants fastest first by the model
@@ -69,6 +70,18 @@ static std::unordered_map<uint64_t, VariantState> vstate;
 static std::vector<uint64_t> vorder;  // keys in the order first seen
 static long uncapturedFlushes = 0;    // flushes run eagerly since tuning was reset
 static std::vector<Record> vdb;       // the variant database
+
+// timed executions of each variant tried (the fastest counts): one run of a
+// variant can carry first-use costs (a second buffer, a stream) or noise
+static int tuneReps() {
+    static int r = 0;
+    if (r == 0) {
+        const char *e = getenv("DVMH_GB_TUNE_REPS");
+        r = e ? atoi(e) : 2;
+        if (r < 1) r = 1;
+    }
+    return r;
+}
 
 static double tuneFrac() {
     static double f = -1;
@@ -108,13 +121,20 @@ void tunerPick(Loop *l, int block[3], int *variant) {
     (void)variant;  // the variant is chosen when the handler asks (dvmhgb_loop_variant)
 }
 
+static bool tried(const VariantState &vs, int v) {
+    auto it = vs.runs.find(v);
+    return it != vs.runs.end() && it->second >= tuneReps();
+}
+
 static bool explorationDone(const VariantState &vs) {
     if (vs.explore >= 0) {
         for (int i = 0; i < vs.explore; i++)
-            if (!vs.best.count(vs.order[i])) return false;
+            if (!tried(vs, vs.order[i])) return false;
         return true;
     }
-    return (int)vs.best.size() >= vs.nvariants;
+    for (int v = 0; v < vs.nvariants; v++)
+        if (!tried(vs, v)) return false;
+    return true;
 }
 
 int tunerVariant(SpecLoop *s, int nvariants, int dflt, const float *desc, int ndesc, bool bestOnly) {
@@ -140,10 +160,10 @@ int tunerVariant(SpecLoop *s, int nvariants, int dflt, const float *desc, int nd
     if (!bestOnly && !explorationDone(vs)) {
         if (vs.explore >= 0) {
             for (int i = 0; i < vs.explore && v < 0; i++)
-                if (!vs.best.count(vs.order[i])) v = vs.order[i];
+                if (!tried(vs, vs.order[i])) v = vs.order[i];
         } else {
             for (int c = 0; c < nvariants && v < 0; c++)
-                if (!vs.best.count(c)) v = c;
+                if (!tried(vs, c)) v = c;
         }
         exploring = v >= 0;
     }
@@ -171,6 +191,7 @@ void tunerRecord(uint64_t key, int variant, bool exploring, const float *vf, dou
     VariantState &vs = it->second;
     auto b = vs.best.find(variant);
     if (b == vs.best.end() || seconds < b->second) vs.best[variant] = seconds;
+    vs.runs[variant]++;
     if (exploring) {
         vs.explored++;
         vs.exploreSeconds += seconds;

@@ -207,7 +207,8 @@ def run(rt, n_loops=2000, n_test=200, seed=20261207, reps=2, epochs=200, frac=0.
 # runtime.  Every timed execution goes into the runtime's variant database.
 # Protocol, per program:
 #   1. exhaustive tuning (mode 1) at a few training sizes: the runtime tries
-#      every variant once, in successive steps, and records each;
+#      every variant twice (DVMH_GB_TUNE_REPS), in successive steps, and
+#      records each run;
 #   2. the variant model (same MLP, same kernels) is trained on those records,
 #      log-times centred per loop shape, and installed in the runtime;
 #   3. at the configuration's own size (never seen in training): exhaustive
@@ -221,14 +222,15 @@ def run(rt, n_loops=2000, n_test=200, seed=20261207, reps=2, epochs=200, frac=0.
 def _programs(g, seed):
     """name -> (training sizes, configuration size, maker(size) -> object with run/close)."""
     return {
-        "jacobi2d_1024": ([258, 514, 2050], 1024, lambda n: g.Jacobi(2, n, seed)),
-        "jacobi3d_512": ([130, 194, 258, 322], 512, lambda n: g.Jacobi(3, n, seed)),
-        "sor3d_384": ([66, 130, 194], 384, lambda n: g.Sor(n, 1.5, seed + 2)),
-        "heat_256x2048": ([(64, 512), (128, 1024)], (256, 2048), lambda p: g.Heat(p[0], 64, p[1], 0.2, seed + 3)),
+        "jacobi2d_1024": ([642, 770, 898, 1154, 1282, 1538], 1024, lambda n: g.Jacobi(2, n, seed)),
+        "jacobi3d_512": ([322, 386, 450, 578], 512, lambda n: g.Jacobi(3, n, seed)),
+        "sor3d_384": ([258, 322, 354, 418, 450], 384, lambda n: g.Sor(n, 1.5, seed + 2)),
+        "heat_256x2048": ([(128, 1024), (192, 1536), (320, 2048)], (256, 2048),
+                          lambda p: g.Heat(p[0], 64, p[1], 0.2, seed + 3)),
     }
 
 
-def _variant_runs(g, rt, mode, maker, size, steps_cap=64):
+def _variant_runs(g, rt, mode, maker, size, steps_cap=200):
     """Tunes one program at one size in `mode`; returns the variant record of
     the handler with the most variants (the program's main loop)."""
     rt.dvmhgb_tuner_reset()

@@ -44,7 +44,7 @@ void stencilDesc(int v, float *d) {
     }
 }
 const float *variantDesc(int handler) {
-    static float upd[3 * NDESC], stn[DVMHGB_JAC3D_VARIANTS * NDESC], fus[(DVMHGB_JAC3D_VARIANTS + 3) * NDESC];
+    static float upd[3 * NDESC], stn[DVMHGB_JAC3D_VARIANTS * NDESC], fus[DVMHGB_JAC3D_FUSED_VARIANTS * NDESC];
     static bool ready = false;
     if (!ready) {
         for (int v = 0; v < 3; v++) upd[v * NDESC] = 1, upd[v * NDESC + 1] = 1, upd[v * NDESC + 2] = (float)v;
@@ -53,9 +53,15 @@ const float *variantDesc(int handler) {
             d[0] = 1, d[1] = 2;
             stencilDesc(v, d);
         }
-        for (int v = 0; v < DVMHGB_JAC3D_VARIANTS + 3; v++) {
+        for (int v = 0; v < DVMHGB_JAC3D_FUSED_VARIANTS; v++) {
             float *d = fus + v * NDESC;
             d[0] = 1, d[1] = 3;
+            if (v >= DVMHGB_JAC3D_FUSED_Q) {  // one pass, fixed point
+                stencilDesc(DVMHGB_JAC3D_VARIANTS - 8, d);
+                d[5] = v == DVMHGB_JAC3D_FUSED_Q ? 4.0f : 3.0f;
+                d[7] = 0;
+                continue;
+            }
             const int sv = v < DVMHGB_JAC3D_VARIANTS ? v
                                                      : (v == DVMHGB_JAC3D_OVERLAP_Q ? DVMHGB_JAC3D_VARIANTS - 8 : 13);
             stencilDesc(sv, d);
@@ -153,14 +159,16 @@ extern "C" void loop_jac3d_fused_cuda(DvmType refs[2], DvmType A_hdr[], DvmType 
     cudaStream_t stream;
     dvmh_loop_cuda_get_config_C(upd, 0, 0, &threads, &stream, 0);
     dvmh_loop_cuda_get_config_C(stn, 0, 0, &threads, &stream, 0);
-    // + the pair: unfused, overlapped (two stencils)
-    const int variant = dvmhgb_loop_variant_desc(upd, DVMHGB_JAC3D_VARIANTS + 3, DEF_FUSED, variantDesc(3), NDESC);
+    // + the pair: unfused, overlapped (two stencils), one pass in fixed point (two)
+    const int variant = dvmhgb_loop_variant_desc(upd, DVMHGB_JAC3D_FUSED_VARIANTS, DEF_FUSED, variantDesc(3), NDESC);
     double eps, *eps_grid = 0;
     dvmh_loop_cuda_register_red_C(upd, 1, (void **)&eps_grid, 0);
     dvmh_loop_red_init_C(upd, 1, &eps, 0);
     dvmh_loop_cuda_red_prepare_C(upd, 1, dvmhgb_jac3d_fused_items(lo, hi, variant), 0);
     // the fused kernel writes the next B into a second buffer; the unfused pair writes B itself
-    double *Bnew = variant >= DVMHGB_JAC3D_UNFUSED ? B.base : (double *)dvmhgb_loop_alt_buffer(stn, B_hdr);
+    double *Bnew = (variant >= DVMHGB_JAC3D_UNFUSED && variant < DVMHGB_JAC3D_FUSED_Q)
+                       ? B.base
+                       : (double *)dvmhgb_loop_alt_buffer(stn, B_hdr);
     // (the update-then-fixed-point-stencil variants could also write B in place; they keep the one-pass shape)
     check(dvmhgb_jac3d_fused(A.base, B.base, Bnew, A.st, A.ext, lo, hi, eps_grid, variant, stream),
           "loop_jac3d_fused_cuda");

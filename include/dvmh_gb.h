@@ -74,7 +74,9 @@ void dvmhgb_force_variant(int v);
  * floor(0.1 x nvariants) of them (none: the model's first choice is taken as
  * it is); every timed execution is recorded with its features in the
  * runtime's variant database.  Exhaustive tuning tries every variant, as
- * dvmhgb_loop_variant does.  In batched mode, flushes run without graph
+ * dvmhgb_loop_variant does.  A variant counts as tried after two timed runs
+ * (environment DVMH_GB_TUNE_REPS), its fastest kept; environment
+ * DVMH_GB_TUNE_FRAC changes the 0.1.  In batched mode, flushes run without graph
  * capture while a loop's variants are being tried, then are captured with
  * the chosen one. */
 #define DVMHGB_VARIANT_NDESC 16

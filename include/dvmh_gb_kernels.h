@@ -61,6 +61,11 @@ int dvmhgb_jac3d_stencil(const double *A, double *B, const long st[3], const lon
 #define DVMHGB_JAC3D_OVERLAP (DVMHGB_JAC3D_VARIANTS + 1)
 /* DVMHGB_JAC3D_OVERLAP_Q: the same with the fixed-point stencil (variant 14) */
 #define DVMHGB_JAC3D_OVERLAP_Q (DVMHGB_JAC3D_VARIANTS + 2)
+/* DVMHGB_JAC3D_FUSED_Q (+ 1): the two loops in one pass with the fixed-point
+ * sums (32 bytes per cell), registers capped for 4 (3) CTAs per SM; the update
+ * of a plane is done as its values arrive; Bnew must not be B */
+#define DVMHGB_JAC3D_FUSED_Q (DVMHGB_JAC3D_VARIANTS + 3)
+#define DVMHGB_JAC3D_FUSED_VARIANTS (DVMHGB_JAC3D_VARIANTS + 5)
 long dvmhgb_jac3d_fused_items(const long lo[3], const long hi[3], int native);
 int dvmhgb_jac3d_fused(double *A, const double *B, double *Bnew, const long st[3], const long ext[3],
                        const long lo[3], const long hi[3], double *items, int native, void *stream);

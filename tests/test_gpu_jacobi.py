@@ -130,7 +130,7 @@ def test_plain_mode_no_fusion(g):
     assert s["fused_pairs"] == 0 and s["graphs_captured"] == 0 and s["handler_calls"] == 6
 
 
-@pytest.mark.parametrize("variant", list(range(25)))
+@pytest.mark.parametrize("variant", list(range(27)))
 def test_jacobi3d_variants_vs_oracle(g, variant):
     """Every kernel variant of the 3-D loops (rows per thread x additions on the
     FP64 unit, the rest on the integer pipe; the fixed-point stencils; the
@@ -164,7 +164,7 @@ def _stencil_ref(A):
     return t / 6.0, c
 
 
-@pytest.mark.parametrize("variant", list(range(22)))
+@pytest.mark.parametrize("variant", list(range(22)) + [25, 26])
 def test_jacobi3d_kernels_signs_and_tiny_values(g, variant):
     """The kernels directly through the C ABI on values that take every path:
     negative values (no integer-pipe additions for that CTA), values below
@@ -191,7 +191,8 @@ def test_jacobi3d_kernels_signs_and_tiny_values(g, variant):
     sp = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
     assert L.dvmhgb_jac3d_fused(vp(Ad), vp(Bd), vp(Bnew), st, ext, lo, hi, vp(items), variant, sp) == 0
     Bs = torch.full_like(Bd, 7.0)
-    assert L.dvmhgb_jac3d_stencil(vp(Bd), vp(Bs), st, ext, lo, hi, variant, sp) == 0
+    sv = variant if variant < 22 else 14  # the one-pass fixed-point pair has no stencil-only form
+    assert L.dvmhgb_jac3d_stencil(vp(Bd), vp(Bs), st, ext, lo, hi, sv, sp) == 0
     torch.cuda.synchronize()
     # reference: update on the interior, then the stencil of the updated A
     An = A.clone()

@@ -100,11 +100,11 @@ def _variant_info(rt):
 def test_variant_tuning_in_batched_mode_keeps_results_and_the_fastest(rt):
     """Exhaustive variant tuning of the Jacobi-3D pair in batched mode: while
     variants are being tried the flushes run uncaptured (one variant per step),
-    every variant is timed once, the fastest is kept and captured; every step,
+    every variant is timed twice, the fastest is kept and captured; every step,
     whichever variant ran it, is bit-exact against the oracle."""
     from oracle import orc
     _, g = ge.package()
-    n, steps, seed = 34, 30, 21
+    n, steps, seed = 34, 60, 21
     e_ref, A_ref, B_ref = orc.jacobi_run(3, n, steps, seed)
     g.set_mode("batched")
     rt.dvmhgb_tuner_reset()
@@ -125,15 +125,15 @@ def test_variant_tuning_in_batched_mode_keeps_results_and_the_fastest(rt):
     rec = [r for r in info if r["handler"] == fused]
     assert len(rec) == 1, info
     r = rec[0]
-    assert r["n"] == 25 and r["explored"] == 25 and all(b > 0 for b in r["best"]), r
+    assert r["n"] == 27 and r["explored"] == 54 and all(b > 0 for b in r["best"]), r  # each variant twice
     assert r["chosen"] == int(np.argmin(r["best"])), r
     assert st["graphs_captured"] >= 1 and st["graph_replays"] >= 1, st  # captured once the search ended
 
 
 def test_variant_model_prunes_the_search(rt):
     """Model-guided variant tuning: with a variant model installed the runtime
-    tries only floor(0.1 n) variants in the model's order (2 of the pair's 25)
-    and keeps the faster of them; results stay bit-exact."""
+    tries only floor(0.1 n) variants in the model's order (2 of the pair's 27,
+    twice each) and keeps the faster of them; results stay bit-exact."""
     from oracle import orc
     _, g = ge.package()
     P = rt.dvmhgb_mlp_nparams()
@@ -143,7 +143,7 @@ def test_variant_model_prunes_the_search(rt):
     mean, std = np.zeros(24, dtype=np.float32), np.ones(24, dtype=np.float32)
     assert rt.dvmhgb_tuner_set_variant_model(params.ctypes.data_as(fp), mean.ctypes.data_as(fp),
                                              std.ctypes.data_as(fp)) == 0
-    n, steps, seed = 34, 8, 22
+    n, steps, seed = 34, 10, 22
     e_ref, A_ref, B_ref = orc.jacobi_run(3, n, steps, seed)
     g.set_mode("batched")
     rt.dvmhgb_tuner_reset()
@@ -161,5 +161,5 @@ def test_variant_model_prunes_the_search(rt):
     fused = ctypes.cast(g.workloads().loop_jac3d_fused_cuda, ctypes.c_void_p).value
     r = [x for x in info if x["handler"] == fused][0]
     tried = [v for v, b in enumerate(r["best"]) if b > 0]
-    assert r["explored"] == 2 and len(tried) == 2, r
+    assert r["explored"] == 4 and len(tried) == 2, r
     assert r["chosen"] in tried and r["best"][r["chosen"]] == min(r["best"][v] for v in tried), r
