@@ -22,6 +22,7 @@
 // 128-bit access.  The stencil kernels stream the outermost axis through
 // registers (plane i-1, i, i+1 per thread) and stage plane i with its halo in
 // shared memory (2.5-D blocking): every A element comes from HBM once.
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include <atomic>
@@ -801,6 +802,8 @@ __global__ void __launch_bounds__(TX *TY, MINB) kStencil3QF(double *A, const dou
     if (ty == 0 && lane == 0) items[blockIdx.x + gridDim.x * ((long)blockIdx.y + (long)gridDim.y * blockIdx.z)] = m;
 }
 
+#include "stencil_tma.cuh"
+
 // CTAs started on each SM (any starting value: only its residue matters); the
 // share of native CTAs is counted per SM, so that every SM runs both kinds at
 // once -- a split by block index alone can put all native CTAs on some SMs
@@ -1055,12 +1058,15 @@ __global__ void kCopyOutside(const double *__restrict__ src, double *__restrict_
 // row per thread, registers capped for three / four CTAs per SM; v = 14..21:
 // the q61 fixed-point stencil (kStencil3Q) with (CTAs per SM, native CTAs of
 // every den): 14 (4, 0 of 1), 15 (3, 0 of 1), 16 (4, 1 of 2), 17 (4, 1 of 3),
-// 18 (4, 2 of 5), 19 (3, 1 of 2), 20 (4, 1 of 4), 21 (4, 3 of 5) (the fused
-// entry point runs the update and then this stencil into the second buffer:
-// there is no one-pass q61 form)
-constexpr int V3Q = 14, V3 = 22;
+// 18 (4, 2 of 5), 19 (3, 1 of 2), 20 (4, 1 of 4), 21 (4, 3 of 5); v = 22, 23:
+// the q61 stencil with its planes staged by TMA (kStencil3T), a ring of 6 / 4
+// plane slots, four CTAs per SM; v = 24, 25, 26: ring of 6 with 1, 2, 3 of the
+// 8 warps on the FP64 unit (the fused entry point runs the update and then the
+// stencil into the second buffer for v = 14..26)
+constexpr int V3Q = 14, V3T = 22, V3 = 27;
 int jtOf3(int v) { return (v >= 6 && v < 12) ? 2 : 1; }
 bool isQ3(int v) { return v >= V3Q && v < V3; }
+bool isT3(int v) { return v >= V3T && v < V3; }
 // the fused entry point's extra variants: the two loops as two kernels (the
 // update, then the stencil with variant UNFUSED_STN into the second buffer)
 constexpr int V3_UNFUSED = V3, UNFUSED_STN = 13;
@@ -1075,6 +1081,10 @@ constexpr int V3_OVERLAP = V3 + 1, V3_OVERLAP_Q = V3 + 2, OVL_CHUNKS = 8;
 // four / three CTAs per SM
 constexpr int V3_QF = V3 + 3;
 bool isQF(int v) { return v == V3_QF || v == V3_QF + 1; }
+// ... and the one-pass pair with its planes staged by TMA (kStencil3T<true>),
+// a ring of 5 / 4 planes, four CTAs per SM
+constexpr int V3_TF = V3 + 5;
+bool isTF(int v) { return v == V3_TF || v == V3_TF + 1; }
 
 template <bool FUSED>
 void launch3(int variant, const St3Geom &g, double *A, const double *B, double *Out, const Box3 &b, double *items,
@@ -1134,7 +1144,48 @@ int dvmhgb_jac3d_stencil(const double *A, double *B, const long st[3], const lon
     St3Geom g = st3Geom(lo, hi, TY * jtOf3(native));
     if (!g.ok || !A || !B || !rows16(st, 3) || !aligned16(A) || !aligned16(B)) return -1;
     Box3 b{st[0], st[1], ext[0], ext[1], ext[2], lo[0], lo[1], lo[2], hi[0], hi[1], hi[2]};
-    launch3<false>(native, g, (double *)A, nullptr, B, b, nullptr, (cudaStream_t)stream);
+    if (isT3(native)) {
+        CUtensorMap map;
+        if (!encodeMap3(&map, A, ext, st, tma::BX, tma::BY)) return -1;
+        dim3 blk(TX, TY);
+        cudaStream_t s = (cudaStream_t)stream;
+        int *status = dvmhgb_status_word();
+        double *a = (double *)A;
+        const int w = native - V3T - 1;  // FP64-unit warps (v >= V3T + 2)
+        if (native == V3T) {
+            kStencil3T<0, 6, 4, 0><<<g.grid, blk, tma::smemBytes(false, 6), s>>>(map, map, map, a, nullptr, B, b,
+                                                                                 g.p0, g.ichunk, nullptr, status);
+        } else if (native == V3T + 1) {
+            kStencil3T<0, 4, 4, 0><<<g.grid, blk, tma::smemBytes(false, 4), s>>>(map, map, map, a, nullptr, B, b,
+                                                                                 g.p0, g.ichunk, nullptr, status);
+        } else {
+            const int smem = tma::smemBytes(false, 6, true);  // above 48 KB: opted in once per device
+            static std::atomic<unsigned long long> optedIn{0};
+            const int dev = gbdev::current();
+            if (dev < 0 || dev >= 64) return -1;
+            if (!(optedIn.load() >> dev & 1ull)) {
+                if (cudaFuncSetAttribute(kStencil3T<0, 6, 4, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem) !=
+                        cudaSuccess ||
+                    cudaFuncSetAttribute(kStencil3T<0, 6, 4, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem) !=
+                        cudaSuccess ||
+                    cudaFuncSetAttribute(kStencil3T<0, 6, 4, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem) !=
+                        cudaSuccess)
+                    return -1;
+                optedIn.fetch_or(1ull << dev);
+            }
+            if (w == 1)
+                kStencil3T<0, 6, 4, 1><<<g.grid, blk, smem, s>>>(map, map, map, a, nullptr, B, b, g.p0, g.ichunk,
+                                                                  nullptr, status);
+            else if (w == 2)
+                kStencil3T<0, 6, 4, 2><<<g.grid, blk, smem, s>>>(map, map, map, a, nullptr, B, b, g.p0, g.ichunk,
+                                                                  nullptr, status);
+            else
+                kStencil3T<0, 6, 4, 3><<<g.grid, blk, smem, s>>>(map, map, map, a, nullptr, B, b, g.p0, g.ichunk,
+                                                                  nullptr, status);
+        }
+    } else {
+        launch3<false>(native, g, (double *)A, nullptr, B, b, nullptr, (cudaStream_t)stream);
+    }
     dvmhgb_count_launches(1);
     return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }
@@ -1173,17 +1224,24 @@ struct Ovl {
 };
 Ovl ovlState[OVL_DEVICES];
 
-int runOverlap(double *A, const double *B, const long st[3], const long ext[3], const long lo[3], const long hi[3],
-               double *items, int stencilVariant, cudaStream_t s1) {
+Ovl *ovlFor() {
     int dev = 0;
-    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= OVL_DEVICES) return -1;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= OVL_DEVICES) return nullptr;
     Ovl &o = ovlState[dev];
     if (!o.ready) {
-        if (cudaStreamCreateWithFlags(&o.s2, cudaStreamNonBlocking) != cudaSuccess) return -1;
+        if (cudaStreamCreateWithFlags(&o.s2, cudaStreamNonBlocking) != cudaSuccess) return nullptr;
         for (auto &e : o.ev)
-            if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) return -1;
+            if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) return nullptr;
         o.ready = true;
     }
+    return &o;
+}
+
+int runOverlap(double *A, const double *B, const long st[3], const long ext[3], const long lo[3], const long hi[3],
+               double *items, int stencilVariant, cudaStream_t s1) {
+    Ovl *op = ovlFor();
+    if (!op) return -1;
+    Ovl &o = *op;
     const int K = ovlCount(lo, hi);
     long clo[OVL_CHUNKS][3], chi[OVL_CHUNKS][3];
     for (int q = 0; q < K; q++) ovlChunk(lo, hi, q, K, clo[q], chi[q]);
@@ -1204,7 +1262,7 @@ int runOverlap(double *A, const double *B, const long st[3], const long ext[3], 
 long dvmhgb_jac3d_fused_items(const long lo[3], const long hi[3], int native) {
     if (native == V3_UNFUSED || isQ3(native)) return dvmhgb_jac3d_update_items(lo, hi);
     if (native == V3_OVERLAP || native == V3_OVERLAP_Q) return ovlItems(lo, hi);
-    if (isQF(native)) {
+    if (isQF(native) || isTF(native)) {
         St3Geom g = st3Geom(lo, hi, TY);
         return (long)g.grid.x * g.grid.y * g.grid.z;
     }
@@ -1228,6 +1286,29 @@ int dvmhgb_jac3d_fused(double *A, const double *B, double *Bnew, const long st[3
                           (cudaStream_t)stream);
     }
     if (Bnew == B) return -1;  // the fused kernel reads B while it writes the next B
+    if (isTF(native)) {
+        St3Geom g = st3Geom(lo, hi, TY);
+        if (!g.ok || !A || !B || !Bnew || A == B || !items || !rows16(st, 3) || !aligned16(A) || !aligned16(B) ||
+            !aligned16(Bnew))
+            return -1;
+        Box3 b{st[0], st[1], ext[0], ext[1], ext[2], lo[0], lo[1], lo[2], hi[0], hi[1], hi[2]};
+        CUtensorMap mapB, mapA, mapT;
+        if (!encodeMap3(&mapB, B, ext, st, tma::BX, tma::BY) || !encodeMap3(&mapA, A, ext, st, tma::BX, tma::BY) ||
+            !encodeMap3(&mapT, A, ext, st, 2 * TX, TY))
+            return -1;
+        dim3 blk(TX, TY);
+        cudaStream_t s = (cudaStream_t)stream;
+        int *status = dvmhgb_status_word();
+        if (native == V3_TF)
+            kStencil3T<2, 5, 4, 0><<<g.grid, blk, tma::smemBytes(true, 5), s>>>(mapB, mapA, mapT, A, B, Bnew, b, g.p0,
+                                                                                g.ichunk, items, status);
+        else
+            kStencil3T<2, 4, 4, 0><<<g.grid, blk, tma::smemBytes(true, 4), s>>>(mapB, mapA, mapT, A, B, Bnew, b, g.p0,
+                                                                                g.ichunk, items, status);
+        dvmhgb_count_launches(1);
+        if (cudaGetLastError() != cudaSuccess) return -1;
+        return dvmhgb_copy_outside_box(3, B, Bnew, st, ext, lo, hi, stream);
+    }
     if (isQF(native)) {
         St3Geom g = st3Geom(lo, hi, TY);
         if (!g.ok || !A || !B || !Bnew || !items || !rows16(st, 3) || !aligned16(A) || !aligned16(B) ||

@@ -28,6 +28,7 @@
 // host FPU) and for the device.
 #pragma once
 
+#include <cmath>
 #include <cstdint>
 #include <cstring>
 
@@ -440,6 +441,60 @@ SF_HD uint64_t q61_add(uint64_t s, uint64_t t) {
     return u & ~(uint64_t)mask;
 }
 
+// The same addition in the form the TMA-staged stencil uses.  There the
+// q61 sums keep the integer ALU pipe busy (shifts, masks, compares) while the
+// multiply-add pipe idles, so: the 64-bit additions are 32 x 32 + 64-bit
+// multiply-adds by a `one` the compiler cannot see (they go to the
+// multiply-add pipe), and the rounding constants come from a 33-entry table
+// indexed by the position of the sum's leading bit (a shared-memory load).
+// Rounding to nearest even by adding half: v = u + half carries into the kept
+// bits iff the dropped part is at least half; it was exactly half iff v's
+// dropped bits are then 0, and the tie goes to even by clearing v's last kept
+// bit as well (it is already 0 when u's was 1, the carry having cleared it).
+struct Q61Round {
+    uint32_t half, mask;  // half of the last kept bit's weight (0: nothing dropped), the dropped bits
+};
+constexpr int Q61_ROUND_ENTRIES = 33;
+// entry idx = msb(high word of the sum) + 1, 0 for a zero high word
+SF_HD Q61Round q61_round_entry(int idx) {
+    const int r = idx - 21 < 0 ? 0 : idx - 21;  // bits beyond 53 (msb index - 52)
+    return Q61Round{r ? 1u << (r - 1) : 0u, (1u << r) - 1u};
+}
+
+// a * one + c in 64 bits (one == 1)
+SF_HD uint64_t madw(uint32_t a, uint32_t one, uint64_t c) {
+#ifdef __CUDA_ARCH__
+    uint64_t d;
+    asm("mad.wide.u32 %0, %1, %2, %3;" : "=l"(d) : "r"(a), "r"(one), "l"(c));
+    return d;
+#else
+    return (uint64_t)a * one + c;
+#endif
+}
+// a * b + c in 32 bits
+SF_HD uint32_t mad32(uint32_t a, uint32_t b, uint32_t c) {
+#ifdef __CUDA_ARCH__
+    uint32_t d;
+    asm("mad.lo.u32 %0, %1, %2, %3;" : "=r"(d) : "r"(a), "r"(b), "r"(c));
+    return d;
+#else
+    return a * b + c;
+#endif
+}
+
+// q61_add(s, t); tab = the Q61_ROUND_ENTRIES entries q61_round_entry(0..32),
+// one == 1, two == 2
+SF_HD uint64_t q61_add_t(uint64_t s, uint64_t t, const Q61Round *tab, uint32_t one, uint32_t two) {
+    const uint64_t u0 = madw((uint32_t)s, one, t);
+    const uint32_t uh = mad32(hi32(s), one, hi32(u0));
+    const uint64_t u = ((uint64_t)uh << 32) | (uint32_t)u0;
+    const Q61Round e = tab[msb32(uh) + 1];
+    const uint64_t v = madw(e.half, one, u);
+    const uint32_t lo = (uint32_t)v;
+    const uint32_t clr = (lo & e.mask) == 0 ? mad32(e.half, two, e.mask) : e.mask;  // tie: the last kept bit too
+    return ((uint64_t)hi32(v) << 32) | (lo & ~clr);
+}
+
 // RN((s * 2^-61) / 6) for a q61 value s with at most 53 significant bits
 // that is 0 or at least 2^32 -- every sum of q61 values is: a nonzero q61
 // value is at least 2^52 (2^-9 * 2^61).  The quotient's significand comes
@@ -474,6 +529,28 @@ SF_HD double q61_to(uint64_t s) {
     const int p = 63 - c;  // msb index
     const uint64_t m = p >= 52 ? s >> (p - 52) : s << (52 - p);
     return from(((uint64_t)(p - 61 + 1023 - 1) << 52) + m);
+}
+
+// RN(x / 6) on the FP64 unit by one multiply and two fused multiply-adds:
+// q = RN(x z) with z = RN(1/6) is within an ulp of x / 6, the residual
+// r = x - 6 q is exact in an FMA, and RN(q + r z) is the correctly rounded
+// quotient (Markstein's correction theorem: P. Markstein, "Computation of
+// elementary functions on the IBM RISC System/6000 processor", IBM J. Res.
+// Dev. 34(1), 1990; Muller et al., Handbook of Floating-Point Arithmetic,
+// 2nd ed., sec. 4.7).  For x = +0 or a normal x with 2^-1000 < |x| < 2^1000
+// (no underflow of r, no overflow); the stencil uses it for sums in [2^-9, 6)
+// and +0.  Three FP64-unit operations instead of the integer pipe's ~40.
+SF_HD double div6_fma(double x) {
+    const double z = 0x1.5555555555555p-3;  // RN(1/6)
+#ifdef __CUDA_ARCH__
+    const double q = __dmul_rn(x, z);
+    const double r = __fma_rn(-q, 6.0, x);
+    return __fma_rn(r, z, q);
+#else
+    const double q = x * z;
+    const double r = std::fma(-q, 6.0, x);
+    return std::fma(r, z, q);
+#endif
 }
 
 // Max(|t|, m) on bit patterns: for non-negative doubles the IEEE order is the

@@ -17,12 +17,14 @@
 #include "dvmh_gb_kernels.h"
 
 #define R 3
-// default kernel variants (v = 6 * (rows per thread - 1) + additions on the FP64 unit)
-#define DEF_STN 13   // all additions on the FP64 unit, one row a thread, four CTAs per SM
-// the fused pair: the update and the stencil kernels overlapped in chunks of planes (on GB300 the stencil is
-// FP64-issue bound and the update HBM bound; the one-pass fused kernel, variant 12, is 11% slower despite its
-// 32 vs 40 B/cell, the two kernels back to back 5%)
-#define DEF_FUSED DVMHGB_JAC3D_OVERLAP
+// default kernel variants, the fastest measured on GB300 at 512^3 (ms per call): the stencil with its planes
+// staged by TMA, sums in q61 fixed point on the integer pipes and 2 of the CTA's 8 warps on the FP64 unit
+// (0.822; the TMA stencil without FP64-unit warps 0.884, the register-staged fixed-point stencil 1.213, all
+// additions on the FP64 unit 1.464)
+#define DEF_STN 25
+// the pair: the update kernel, then that stencil into the second buffer (1.354 per step; the one-pass TMA pair
+// 1.66, the update and the TMA stencil running at the same time 1.66, the register-staged one-pass pair 2.01)
+#define DEF_FUSED 25
 
 namespace {
 
@@ -31,16 +33,23 @@ namespace {
 // then for stencils: fixed-point sums, FP64-unit additions per cell, rows per
 // thread, CTAs per SM, share of CTAs on the FP64 unit, and for the pair how it
 // runs (0 one pass, 1 update then stencil, 2 the two overlapped in chunks).
+// (the fixed-point feature is 1 for the register-staged kernels and 1 + ring/6
+// for the TMA-staged ones; the share on the FP64 unit is that of CTAs or of
+// warps)
 constexpr int NDESC = 8;
+constexpr int V_Q = 14, V_T = 22;  // first fixed-point stencil variant, first TMA-staged one
 void stencilDesc(int v, float *d) {
     static const int q[8][3] = {{4, 0, 1}, {3, 0, 1}, {4, 1, 2}, {4, 1, 3}, {4, 2, 5}, {3, 1, 2}, {4, 1, 4}, {4, 3, 5}};
     if (v < 12) {
         d[2] = 0, d[3] = (float)(v % 6), d[4] = (float)(1 + v / 6), d[5] = 2, d[6] = 1;
-    } else if (v < DVMHGB_JAC3D_VARIANTS - 8) {
+    } else if (v < V_Q) {
         d[2] = 0, d[3] = 5, d[4] = 1, d[5] = v == 12 ? 3.0f : 4.0f, d[6] = 1;
-    } else {
-        const int *c = q[v - (DVMHGB_JAC3D_VARIANTS - 8)];
+    } else if (v < V_T) {
+        const int *c = q[v - V_Q];
         d[2] = 1, d[3] = 5, d[4] = 1, d[5] = (float)c[0], d[6] = (float)c[1] / (float)c[2];
+    } else {  // ring of 6 (4 for V_T + 1); from V_T + 2 on, 1.. of the 8 warps on the FP64 unit
+        d[2] = v == V_T + 1 ? 1.0f + 4.0f / 6.0f : 2.0f, d[3] = 5, d[4] = 1, d[5] = 4;
+        d[6] = v >= V_T + 2 ? (float)(v - V_T - 1) / 8.0f : 0.0f;
     }
 }
 const float *variantDesc(int handler) {
@@ -56,16 +65,21 @@ const float *variantDesc(int handler) {
         for (int v = 0; v < DVMHGB_JAC3D_FUSED_VARIANTS; v++) {
             float *d = fus + v * NDESC;
             d[0] = 1, d[1] = 3;
+            if (v >= DVMHGB_JAC3D_FUSED_T) {  // one pass, fixed point, TMA-staged (rings of 5, 4)
+                stencilDesc(V_T, d);
+                d[2] = v == DVMHGB_JAC3D_FUSED_T ? 1.0f + 5.0f / 6.0f : 1.0f + 4.0f / 6.0f;
+                d[7] = 0;
+                continue;
+            }
             if (v >= DVMHGB_JAC3D_FUSED_Q) {  // one pass, fixed point
-                stencilDesc(DVMHGB_JAC3D_VARIANTS - 8, d);
+                stencilDesc(V_Q, d);
                 d[5] = v == DVMHGB_JAC3D_FUSED_Q ? 4.0f : 3.0f;
                 d[7] = 0;
                 continue;
             }
-            const int sv = v < DVMHGB_JAC3D_VARIANTS ? v
-                                                     : (v == DVMHGB_JAC3D_OVERLAP_Q ? DVMHGB_JAC3D_VARIANTS - 8 : 13);
+            const int sv = v < DVMHGB_JAC3D_VARIANTS ? v : (v == DVMHGB_JAC3D_OVERLAP_Q ? V_Q : 13);
             stencilDesc(sv, d);
-            d[7] = v < DVMHGB_JAC3D_VARIANTS - 8 ? 0.0f : (v < DVMHGB_JAC3D_OVERLAP ? 1.0f : 2.0f);
+            d[7] = v < V_Q ? 0.0f : (v < DVMHGB_JAC3D_OVERLAP ? 1.0f : 2.0f);
         }
         ready = true;
     }
@@ -165,11 +179,10 @@ extern "C" void loop_jac3d_fused_cuda(DvmType refs[2], DvmType A_hdr[], DvmType 
     dvmh_loop_cuda_register_red_C(upd, 1, (void **)&eps_grid, 0);
     dvmh_loop_red_init_C(upd, 1, &eps, 0);
     dvmh_loop_cuda_red_prepare_C(upd, 1, dvmhgb_jac3d_fused_items(lo, hi, variant), 0);
-    // the fused kernel writes the next B into a second buffer; the unfused pair writes B itself
-    double *Bnew = (variant >= DVMHGB_JAC3D_UNFUSED && variant < DVMHGB_JAC3D_FUSED_Q)
-                       ? B.base
-                       : (double *)dvmhgb_loop_alt_buffer(stn, B_hdr);
-    // (the update-then-fixed-point-stencil variants could also write B in place; they keep the one-pass shape)
+    // a one-pass kernel writes the next B into a second buffer; the pairs of two kernels (the update, then a
+    // stencil that reads only A) write B itself
+    double *Bnew = (variant >= V_Q && variant < DVMHGB_JAC3D_FUSED_Q) ? B.base
+                                                                       : (double *)dvmhgb_loop_alt_buffer(stn, B_hdr);
     check(dvmhgb_jac3d_fused(A.base, B.base, Bnew, A.st, A.ext, lo, hi, eps_grid, variant, stream),
           "loop_jac3d_fused_cuda");
     dvmh_loop_cuda_red_finish_C(upd, 1);

@@ -41,15 +41,21 @@ int dvmhgb_jac3d_update(double *A, const double *B, const long st[3], const long
  * FP64 unit), with a share of the CTAs computing natively so that the FP64
  * unit works beside the integer pipe -- (CTAs per SM, native CTAs of every
  * den): 14 (4, 0/1), 15 (3, 0/1), 16 (4, 1/2), 17 (4, 1/3), 18 (4, 2/5),
- * 19 (3, 1/2), 20 (4, 1/4), 21 (4, 3/5); -1 for v outside
- * 0..DVMHGB_JAC3D_VARIANTS-1 */
-#define DVMHGB_JAC3D_VARIANTS 22
+ * 19 (3, 1/2), 20 (4, 1/4), 21 (4, 3/5); v = 22, 23: the fixed-point sums
+ * with the source planes staged in shared memory by TMA box copies, a ring of
+ * 6 / 4 planes per CTA (a copy that does not land within about 2^22 polls
+ * writes DVMHGB_ERR_TMA_TIMEOUT to dvmhgb_status_word() and the CTA stops);
+ * v = 24, 25, 26: ring of 6, with 1, 2, 3 of the CTA's 8 warps computing their
+ * cells on the FP64 unit (division by 6 as one multiply and two FMAs);
+ * -1 for v outside 0..DVMHGB_JAC3D_VARIANTS-1 */
+#define DVMHGB_JAC3D_VARIANTS 27
+#define DVMHGB_ERR_TMA_TIMEOUT 0x544D4101
 int dvmhgb_jac3d_stencil(const double *A, double *B, const long st[3], const long ext[3], const long lo[3],
                          const long hi[3], int native, void *stream);
 /* loops 1+2 fused (same box): reads A, B; writes A = B and Bnew = stencil(A_new)
  * into Bnew (a second buffer of B's layout), B's values outside the box copied
  * into Bnew; MAX partials, one per CTA (the count depends on the variant).
- * Variants 0..13 as above (one pass), 14..21 the update kernel and then the
+ * Variants 0..13 as above (one pass), 14..26 the update kernel and then the
  * fixed-point stencil of that variant, and DVMHGB_JAC3D_UNFUSED: the update
  * and the stencil kernels (variant 13) one after the other (Bnew may then be B
  * itself: the stencil reads only A; the one-pass variants reject Bnew == B) */
@@ -65,7 +71,11 @@ int dvmhgb_jac3d_stencil(const double *A, double *B, const long st[3], const lon
  * sums (32 bytes per cell), registers capped for 4 (3) CTAs per SM; the update
  * of a plane is done as its values arrive; Bnew must not be B */
 #define DVMHGB_JAC3D_FUSED_Q (DVMHGB_JAC3D_VARIANTS + 3)
-#define DVMHGB_JAC3D_FUSED_VARIANTS (DVMHGB_JAC3D_VARIANTS + 5)
+/* DVMHGB_JAC3D_FUSED_T (+ 1): the two loops in one pass with the fixed-point
+ * sums and the planes of B (A outside the box) and A's own cells staged by TMA
+ * box copies, a ring of 5 (4) planes per CTA; Bnew must not be B */
+#define DVMHGB_JAC3D_FUSED_T (DVMHGB_JAC3D_VARIANTS + 5)
+#define DVMHGB_JAC3D_FUSED_VARIANTS (DVMHGB_JAC3D_VARIANTS + 7)
 long dvmhgb_jac3d_fused_items(const long lo[3], const long hi[3], int native);
 int dvmhgb_jac3d_fused(double *A, const double *B, double *Bnew, const long st[3], const long ext[3],
                        const long lo[3], const long hi[3], double *items, int native, void *stream);

@@ -133,18 +133,22 @@ static double q61Operand(uint64_t r, uint64_t q) {
 
 extern "C" long softfp64_check_q61(long n, uint64_t seed) {
     volatile double six = 6.0;
+    volatile uint32_t one = 1, two = 2;
+    sf::Q61Round tab[sf::Q61_ROUND_ENTRIES];
+    for (int e = 0; e < sf::Q61_ROUND_ENTRIES; e++) tab[e] = sf::q61_round_entry(e);
     long bad = 0;
     for (long i = 0; i < n; i++) {
         double v[6];
         for (int k = 0; k < 6; k++) v[k] = q61Operand(mix(seed + 12 * i + 2 * k), mix(seed + 12 * i + 2 * k + 1));
         double t = v[0];
-        uint64_t s = sf::q61(v[0]);
+        uint64_t s = sf::q61(v[0]), st = s;
         for (int k = 0; k < 6; k++) {
             if (!sf::q61_ok(v[k]) || sf::q61_to(sf::q61(v[k])) != v[k]) bad++;
             if (k == 0) continue;
             t = t + v[k];
             s = sf::q61_add(s, sf::q61(v[k]));
-            bad += !same(sf::q61_to(s), t);
+            st = sf::q61_add_t(st, sf::q61(v[k]), tab, one, two);
+            bad += !same(sf::q61_to(s), t) + (st != s);
         }
         bad += !same(sf::q61_div6(s), t / six);
     }
@@ -153,5 +157,25 @@ extern "C" long softfp64_check_q61(long n, uint64_t seed) {
     for (double x : outside) bad += sf::q61_ok(x);
     const double inside[] = {0.0, 0x1p-9, 0x1.fffffffffffffp-1, 0.5, 0.1};
     for (double x : inside) bad += !sf::q61_ok(x);
+    return bad;
+}
+
+// RN(x / 6) by div6_fma against the host FPU's division: q61 stencil sums
+// (six operands of q61Operand, summed left to right), and normal doubles with
+// random significands and exponents in (-1000, 1000), both signs
+extern "C" long softfp64_check_div6_fma(long n, uint64_t seed) {
+    volatile double six = 6.0;
+    long bad = 0;
+    for (long i = 0; i < n; i++) {
+        double t = q61Operand(mix(seed + 14 * i), mix(seed + 14 * i + 1));
+        for (int k = 1; k < 6; k++) t = t + q61Operand(mix(seed + 14 * i + 2 * k), mix(seed + 14 * i + 2 * k + 1));
+        bad += !same(sf::div6_fma(t), t / six);
+        const uint64_t r = mix(seed + 14 * i + 12), q = mix(seed + 14 * i + 13);
+        const double x = sf::from(((q & 1) << 63) | ((uint64_t)(1023 - 999 + (q >> 1) % 1998) << 52) | (r & sf::MANT));
+        bad += !same(sf::div6_fma(x), x / six);
+    }
+    const double edge[] = {0.0, 0x1p-9, 0x1.fffffffffffffp-1, 6.0 - 0x1p-50, 3.0, 6.0, 0x1.5555555555555p-3, 0x1p-999,
+                           0x1.fffffffffffffp999};
+    for (double x : edge) bad += !same(sf::div6_fma(x), x / six);
     return bad;
 }

@@ -94,7 +94,7 @@ def jac_ref():
     return orc.jacobi_run(3, 512, 10, SEED, threads=os.cpu_count() or 1)
 
 
-@pytest.mark.parametrize("variant", [-1, 14, 16])
+@pytest.mark.parametrize("variant", [-1, 14, 16, 22, 25])
 @pytest.mark.parametrize("mode", ["plain", "batched"])
 def test_jacobi3d_512_ten_iterations(g, jac_ref, mode, variant):
     e_ref, A_ref, B_ref = jac_ref

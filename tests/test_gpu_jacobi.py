@@ -5,7 +5,7 @@ import pytest
 
 import __graft_entry__ as ge
 from oracle import orc
-from tests.util import sha, unhex
+from tests.util import J3_FUSED, J3_IN_PLACE, J3_ONE_PASS_Q, J3_STENCILS, sha, unhex
 
 pytestmark = pytest.mark.gpu
 
@@ -130,7 +130,7 @@ def test_plain_mode_no_fusion(g):
     assert s["fused_pairs"] == 0 and s["graphs_captured"] == 0 and s["handler_calls"] == 6
 
 
-@pytest.mark.parametrize("variant", list(range(27)))
+@pytest.mark.parametrize("variant", list(range(J3_FUSED)))
 def test_jacobi3d_variants_vs_oracle(g, variant):
     """Every kernel variant of the 3-D loops (rows per thread x additions on the
     FP64 unit, the rest on the integer pipe; the fixed-point stencils; the
@@ -164,7 +164,7 @@ def _stencil_ref(A):
     return t / 6.0, c
 
 
-@pytest.mark.parametrize("variant", list(range(22)) + [25, 26])
+@pytest.mark.parametrize("variant", list(range(J3_STENCILS)) + J3_ONE_PASS_Q)
 def test_jacobi3d_kernels_signs_and_tiny_values(g, variant):
     """The kernels directly through the C ABI on values that take every path:
     negative values (no integer-pipe additions for that CTA), values below
@@ -191,7 +191,7 @@ def test_jacobi3d_kernels_signs_and_tiny_values(g, variant):
     sp = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
     assert L.dvmhgb_jac3d_fused(vp(Ad), vp(Bd), vp(Bnew), st, ext, lo, hi, vp(items), variant, sp) == 0
     Bs = torch.full_like(Bd, 7.0)
-    sv = variant if variant < 22 else 14  # the one-pass fixed-point pair has no stencil-only form
+    sv = variant if variant < J3_STENCILS else 14  # the one-pass fixed-point pair has no stencil-only form
     assert L.dvmhgb_jac3d_stencil(vp(Bd), vp(Bs), st, ext, lo, hi, sv, sp) == 0
     torch.cuda.synchronize()
     # reference: update on the interior, then the stencil of the updated A
@@ -205,6 +205,47 @@ def test_jacobi3d_kernels_signs_and_tiny_values(g, variant):
     assert torch.equal(Bnew.cpu()[0], B[0]), variant  # outside the box: B's values
     s2, _ = _stencil_ref(B)
     assert torch.equal(Bs.cpu()[1:-1, 1:-1, 1:-1], s2), variant
+
+
+@pytest.mark.parametrize("variant", list(range(J3_FUSED)))
+def test_jacobi3d_fused_sub_box(g, variant):
+    """The update and stencil loops over a box that leaves several planes,
+    rows and columns of the array outside it on every side (A != B there), as
+    one fused call: A = B and eps inside the box only; the stencil's source is
+    B inside the box and A outside it; the next B holds the stencil inside the
+    box and B's values outside it.  Values mostly in the fixed-point range, a
+    few outside it.  Bit-exact against float64 on the CPU."""
+    import ctypes
+    import torch
+    L = g.runtime()
+    L.dvmhgb_jac3d_fused_items.restype = ctypes.c_long
+    n0, n1, n2 = 30, 45, 202  # row pitch 202: 16-byte aligned rows
+    LA = ctypes.c_long * 3
+    lo_, hi_ = (3, 5, 7), (25, 38, 190)
+    st, ext, lo, hi = LA(n1 * n2, n2, 1), LA(n0, n1, n2), LA(*lo_), LA(*hi_)
+    gen = torch.Generator().manual_seed(300 + variant)
+    A = 0.25 + 0.5 * torch.rand(n0, n1, n2, dtype=torch.float64, generator=gen)
+    B = 0.25 + 0.5 * torch.rand(n0, n1, n2, dtype=torch.float64, generator=gen)
+    B[17, 20, 100], A[9, 30, 60], A[2, 10, 50] = -0.5, 3.0, 1.25  # outside the range: planes on the FP64 unit
+    Ad, Bd = A.cuda(), B.cuda()
+    in_place = variant in J3_IN_PLACE  # the two-kernel pairs write the next B over B
+    Bnew = Bd if in_place else torch.full_like(Bd, 7.0)
+    vp = lambda t: ctypes.c_void_p(t.data_ptr())
+    items = torch.empty(L.dvmhgb_jac3d_fused_items(lo, hi, variant), dtype=torch.float64, device="cuda")
+    sp = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    assert L.dvmhgb_jac3d_fused(vp(Ad), vp(Bd), vp(Bnew), st, ext, lo, hi, vp(items), variant, sp) == 0
+    torch.cuda.synchronize()
+    box = tuple(slice(a, b + 1) for a, b in zip(lo_, hi_))
+    An = A.clone()
+    An[box] = B[box]
+    eps_ref = (B[box] - A[box]).abs().max().item()
+    s_ref, _ = _stencil_ref(An)
+    inner = tuple(slice(a - 1, b) for a, b in zip(lo_, hi_))  # the box in _stencil_ref's interior coordinates
+    want = B.clone()
+    want[box] = s_ref[inner]
+    assert items.max().item() == eps_ref, variant
+    assert torch.equal(Ad.cpu(), An), variant
+    assert torch.equal(Bnew.cpu().view(torch.int64), want.view(torch.int64)), variant
 
 
 @pytest.mark.parametrize("native", [0, 1, 2])
@@ -284,7 +325,7 @@ def test_subarray_actuality(g, mode):
     assert eps[0] == e_ref, mode
 
 
-@pytest.mark.parametrize("variant", list(range(14, 22)))
+@pytest.mark.parametrize("variant", list(range(14, J3_STENCILS)))
 def test_jacobi3d_fixed_point_stencil_range_edges(g, variant):
     """The fixed-point stencil computes a plane on the FP64 unit when any value
     its cells read lies outside +0 and [2^-9, 1).  Values on both sides of

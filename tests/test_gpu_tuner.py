@@ -11,6 +11,7 @@ import pytest
 
 import __graft_entry__ as ge
 from oracle import mlp_ref
+from tests.util import J3_FUSED
 
 pytestmark = pytest.mark.gpu
 
@@ -104,7 +105,7 @@ def test_variant_tuning_in_batched_mode_keeps_results_and_the_fastest(rt):
     whichever variant ran it, is bit-exact against the oracle."""
     from oracle import orc
     _, g = ge.package()
-    n, steps, seed = 34, 60, 21
+    n, steps, seed = 34, 2 * J3_FUSED + 10, 21
     e_ref, A_ref, B_ref = orc.jacobi_run(3, n, steps, seed)
     g.set_mode("batched")
     rt.dvmhgb_tuner_reset()
@@ -125,14 +126,14 @@ def test_variant_tuning_in_batched_mode_keeps_results_and_the_fastest(rt):
     rec = [r for r in info if r["handler"] == fused]
     assert len(rec) == 1, info
     r = rec[0]
-    assert r["n"] == 27 and r["explored"] == 54 and all(b > 0 for b in r["best"]), r  # each variant twice
+    assert r["n"] == J3_FUSED and r["explored"] == 2 * J3_FUSED and all(b > 0 for b in r["best"]), r  # twice each
     assert r["chosen"] == int(np.argmin(r["best"])), r
     assert st["graphs_captured"] >= 1 and st["graph_replays"] >= 1, st  # captured once the search ended
 
 
 def test_variant_model_prunes_the_search(rt):
     """Model-guided variant tuning: with a variant model installed the runtime
-    tries only floor(0.1 n) variants in the model's order (2 of the pair's 27,
+    tries only floor(0.1 n) variants in the model's order (3 of the pair's 34,
     twice each) and keeps the faster of them; results stay bit-exact."""
     from oracle import orc
     _, g = ge.package()
@@ -161,5 +162,5 @@ def test_variant_model_prunes_the_search(rt):
     fused = ctypes.cast(g.workloads().loop_jac3d_fused_cuda, ctypes.c_void_p).value
     r = [x for x in info if x["handler"] == fused][0]
     tried = [v for v, b in enumerate(r["best"]) if b > 0]
-    assert r["explored"] == 4 and len(tried) == 2, r
+    assert r["explored"] == 6 and len(tried) == 3, r
     assert r["chosen"] in tried and r["best"][r["chosen"]] == min(r["best"][v] for v in tried), r

@@ -53,6 +53,16 @@ def test_softfp64_matches_gb300_fp64_unit():
     assert list(bad) == [0, 0, 0, 0], "mismatches add/sub/mul/div6: %s" % list(bad)
 
 
+@pytest.mark.parametrize("seed", [3, 20261204])
+def test_div6_fma_matches_host_division(hostlib, seed):
+    """RN(x / 6) from one multiply and two FMAs (Markstein's correction) equals
+    the host FPU's division on stencil sums and on normal doubles of both signs
+    across the exponent range the method covers."""
+    hostlib.softfp64_check_div6_fma.restype = ctypes.c_long
+    hostlib.softfp64_check_div6_fma.argtypes = [ctypes.c_long, ctypes.c_uint64]
+    assert hostlib.softfp64_check_div6_fma(4_000_000, seed) == 0
+
+
 @pytest.mark.parametrize("seed", [5, 20261205])
 def test_q61_chain_matches_host_fpu(hostlib, seed):
     """The fixed-point form of the Jacobi stencil: five additions and the division by 6."""
