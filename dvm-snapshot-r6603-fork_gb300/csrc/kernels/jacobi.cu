@@ -1086,6 +1086,28 @@ bool isQF(int v) { return v == V3_QF || v == V3_QF + 1; }
 constexpr int V3_TF = V3 + 5;
 bool isTF(int v) { return v == V3_TF || v == V3_TF + 1; }
 
+// the TMA-staged stencil alone (kStencil3T, M = 0) with NS slots and W
+// FP64-unit warps; a launch above 48 KB of shared memory is opted in once per
+// device
+template <int NS, int W>
+int launchT(const CUtensorMap &map, double *A, double *Out, const Box3 &b, const St3Geom &g, cudaStream_t s) {
+    const int smem = tma::smemBytes(false, NS, W > 0);
+    if (smem > 48 * 1024) {
+        static std::atomic<unsigned long long> optedIn{0};
+        const int dev = gbdev::current();
+        if (dev < 0 || dev >= 64) return -1;
+        if (!(optedIn.load() >> dev & 1ull)) {
+            if (cudaFuncSetAttribute(kStencil3T<0, NS, 4, W>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem) !=
+                cudaSuccess)
+                return -1;
+            optedIn.fetch_or(1ull << dev);
+        }
+    }
+    kStencil3T<0, NS, 4, W><<<g.grid, dim3(TX, TY), smem, s>>>(map, map, map, A, nullptr, Out, b, g.p0, g.ichunk,
+                                                               nullptr, dvmhgb_status_word());
+    return 0;
+}
+
 template <bool FUSED>
 void launch3(int variant, const St3Geom &g, double *A, const double *B, double *Out, const Box3 &b, double *items,
              cudaStream_t s) {
@@ -1147,41 +1169,13 @@ int dvmhgb_jac3d_stencil(const double *A, double *B, const long st[3], const lon
     if (isT3(native)) {
         CUtensorMap map;
         if (!encodeMap3(&map, A, ext, st, tma::BX, tma::BY)) return -1;
-        dim3 blk(TX, TY);
         cudaStream_t s = (cudaStream_t)stream;
-        int *status = dvmhgb_status_word();
         double *a = (double *)A;
-        const int w = native - V3T - 1;  // FP64-unit warps (v >= V3T + 2)
-        if (native == V3T) {
-            kStencil3T<0, 6, 4, 0><<<g.grid, blk, tma::smemBytes(false, 6), s>>>(map, map, map, a, nullptr, B, b,
-                                                                                 g.p0, g.ichunk, nullptr, status);
-        } else if (native == V3T + 1) {
-            kStencil3T<0, 4, 4, 0><<<g.grid, blk, tma::smemBytes(false, 4), s>>>(map, map, map, a, nullptr, B, b,
-                                                                                 g.p0, g.ichunk, nullptr, status);
-        } else {
-            const int smem = tma::smemBytes(false, 6, true);  // above 48 KB: opted in once per device
-            static std::atomic<unsigned long long> optedIn{0};
-            const int dev = gbdev::current();
-            if (dev < 0 || dev >= 64) return -1;
-            if (!(optedIn.load() >> dev & 1ull)) {
-                if (cudaFuncSetAttribute(kStencil3T<0, 6, 4, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem) !=
-                        cudaSuccess ||
-                    cudaFuncSetAttribute(kStencil3T<0, 6, 4, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem) !=
-                        cudaSuccess ||
-                    cudaFuncSetAttribute(kStencil3T<0, 6, 4, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem) !=
-                        cudaSuccess)
-                    return -1;
-                optedIn.fetch_or(1ull << dev);
-            }
-            if (w == 1)
-                kStencil3T<0, 6, 4, 1><<<g.grid, blk, smem, s>>>(map, map, map, a, nullptr, B, b, g.p0, g.ichunk,
-                                                                  nullptr, status);
-            else if (w == 2)
-                kStencil3T<0, 6, 4, 2><<<g.grid, blk, smem, s>>>(map, map, map, a, nullptr, B, b, g.p0, g.ichunk,
-                                                                  nullptr, status);
-            else
-                kStencil3T<0, 6, 4, 3><<<g.grid, blk, smem, s>>>(map, map, map, a, nullptr, B, b, g.p0, g.ichunk,
-                                                                  nullptr, status);
+        switch (native - V3T) {
+#define CT(V, NS, W) \
+    case V: if (launchT<NS, W>(map, a, B, b, g, s) != 0) return -1; break;
+            CT(0, 6, 0) CT(1, 4, 0) CT(2, 6, 1) CT(3, 6, 2) CT(4, 6, 3)
+#undef CT
         }
     } else {
         launch3<false>(native, g, (double *)A, nullptr, B, b, nullptr, (cudaStream_t)stream);

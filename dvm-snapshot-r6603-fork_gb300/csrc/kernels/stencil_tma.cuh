@@ -26,7 +26,7 @@
 // every thread has finished step t - 1, the last reader of q = t - 1, so
 // thread 0 issues the copy of q = t - 1 + NS into that slot.  Each thread's
 // generic-proxy writes of a slot are followed by a proxy fence before that
-// barrier.  Every wait is bounded: after POLL_LIMIT polls the kernel writes
+// barrier.  Every wait is bounded: after 2 s of the global timer the kernel writes
 // DVMHGB_ERR_TMA_TIMEOUT to the status word (when one is given), the CTA
 // leaves its loop, and thread 0 waits (bounded again) for the copies still in
 // flight before the CTA exits.
@@ -42,10 +42,9 @@
 // Fused (M = 2): the chunk's own cells also do the update loop,
 // eps = Max(|B - A|, eps); A = B.  Each plane of the chunk
 // also brings A's values of the CTA's own 64 x TY cells (a second box of A,
-// same mbarrier); the conversion pass then takes |B - A_old| -- exact as a
-// difference of q61 values, rounded once at the end (RN is monotone, so
-// RN(max |b - a|) = max RN(|b - a|)), on the FP64 unit for a value outside the
-// range -- and stores B into A.  Nothing reads A inside the box after that
+// same mbarrier); before converting its own pair, each thread takes
+// |B - A_old| on the FP64 unit (idle beside the q61 sums) into its MAX and
+// stores B into A.  Nothing reads A inside the box after that
 // store except this CTA's own tile copy, which landed before it.  32 bytes a
 // cell: A and B read, A and Out written.
 //
@@ -71,7 +70,8 @@ constexpr int BOX_BYTES = BX * BY * 8;
 constexpr int SLOT = (BOX_BYTES + 127) / 128 * 128;
 constexpr int TILE_BYTES = 2 * TX * TY * 8;  // the CTA's own cells of a plane
 constexpr int PAIRS = BX * BY / 2;           // element pairs of a box
-constexpr long POLL_LIMIT = 1L << 22;
+constexpr uint64_t WAIT_LIMIT_NS = 2000000000ull;  // a wait gives up after 2 s
+constexpr uint32_t SUSPEND_HINT_NS = 1000000;       // a waiting thread sleeps up to 1 ms per poll
 
 constexpr int QSLOTS = 4;  // the q61 ring of the launches with FP64-unit warps
 constexpr int slotBytes(bool fused) { return SLOT + (fused ? TILE_BYTES : 0); }
@@ -87,23 +87,33 @@ __device__ __forceinline__ void mbarInit(uint32_t bar, uint32_t count) {
     asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
 }
 
+// one poll: the thread may sleep until the phase completes (or the hint's time passes)
 __device__ __forceinline__ bool mbarTryWait(uint32_t bar, uint32_t parity) {
     uint32_t ok;
     asm volatile(
         "{\n\t.reg .pred p;\n\t"
-        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n\t"
         "selp.u32 %0, 1, 0, p;\n\t}"
         : "=r"(ok)
-        : "r"(bar), "r"(parity)
+        : "r"(bar), "r"(parity), "r"(SUSPEND_HINT_NS)
         : "memory");
     return ok != 0;
 }
 
-// wait (at most POLL_LIMIT polls) for the phase of `parity` to complete
+__device__ __forceinline__ uint64_t nowNs() {
+    uint64_t t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+// wait for the phase of `parity` to complete, at most WAIT_LIMIT_NS of the
+// global timer (the clock is read only once the first poll has failed)
 __device__ __forceinline__ bool mbarWait(uint32_t bar, uint32_t parity) {
-    for (long n = 0; n < POLL_LIMIT; n++)
-        if (mbarTryWait(bar, parity)) return true;
-    return false;
+    if (mbarTryWait(bar, parity)) return true;
+    const uint64_t t0 = nowNs();
+    while (!mbarTryWait(bar, parity))
+        if (nowNs() - t0 > WAIT_LIMIT_NS) return false;
+    return true;
 }
 
 // thread 0's arrival on the slot's mbarrier, expecting `bytes` of copies
@@ -172,36 +182,50 @@ __global__ void __launch_bounds__(TX *TY, MINB)
         issued = q + 1;
     };
 
-    // the thread's pairs of a box (u = 0 .. NP - 1: pair tid + u TX TY) and,
-    // fused, what they are: bit 0 a pair of the box, bits 1, 2 element 0, 1
-    // outside the loop box but inside the array (A's value replaces B's in
-    // the planes inside the box), bits 3, 4 element 0, 1 an own cell inside
-    // the box (updated); goff: the pair's offset in a plane, toff: its place
-    // in the own-cell tile
-    int pr[NP], toff[NP];
+    // the thread's pairs of a box -- u = 0: its own pair (row ty + 1, pair
+    // lane + 1 of the row: the cells whose stencil it computes), u = 1: one of
+    // the 84 halo pairs (rows 0 and TY + 1, then the first and last pair of
+    // rows 1..TY) for the first 84 threads -- and, source A_new, what they
+    // are: bit 0 a pair of the box, bits 1, 2 element 0, 1 outside the loop
+    // box but inside the array (A's value replaces B's in the planes inside
+    // the box); goff: the pair's offset in a plane
+    static_assert(NP == 2 && tma::PAIRS - TX * TY == 2 * (tma::BX / 2) + 2 * TY, "own pairs, then halo pairs");
+    int pr[NP];
     unsigned fl[NP];
     long goff[NP];
 #pragma unroll
     for (int u = 0; u < NP; u++) {
-        const int p = tid + u * TX * TY, r = p / (tma::BX / 2), cp = p % (tma::BX / 2);
+        constexpr int RP = tma::BX / 2;  // pairs of a row
+        int r, cp;
+        if (u == 0) {
+            r = ty + 1, cp = lane + 1;
+        } else if (tid < RP) {
+            r = 0, cp = tid;
+        } else if (tid < 2 * RP) {
+            r = TY + 1, cp = tid - RP;
+        } else {
+            r = 1 + (tid - 2 * RP) / 2, cp = (tid - 2 * RP) & 1 ? RP - 1 : 0;
+        }
+        const int p = u == 0 || tid < tma::PAIRS - TX * TY ? r * RP + cp : tma::PAIRS;
         const long jj = jb - 1 + r, kk = kb - 2 + 2 * cp;
         const bool inJ = jj >= b.lo1 && jj <= b.hi1, aJ = jj >= 0 && jj < b.e1;
         const bool ik0 = kk >= b.lo2 && kk <= b.hi2, ik1 = kk + 1 >= b.lo2 && kk + 1 <= b.hi2;
         const bool ak0 = kk >= 0 && kk < b.e2, ak1 = kk + 1 >= 0 && kk + 1 < b.e2;
-        const bool own = r >= 1 && r <= TY && cp >= 1 && cp <= TX;
         pr[u] = p;
-        toff[u] = (r - 1) * TX + cp - 1;
         goff[u] = jj * b.s1 + kk;
         fl[u] = p < tma::PAIRS ? 1u : 0u;
         if (S && p < tma::PAIRS) fl[u] |= (aJ && ak0 && !(inJ && ik0) ? 2u : 0u) | (aJ && ak1 && !(inJ && ik1) ? 4u : 0u);
-        if (U && p < tma::PAIRS) fl[u] |= (own && inJ && ik0 ? 8u : 0u) | (own && inJ && ik1 ? 16u : 0u);
     }
-    uint64_t qmax = 0, mb = 0;  // fused eps: fixed-point part, FP64-unit part (bit pattern)
+    // fused: the update loop on the thread's own pair -- the cells whose stencil it computes
+    const bool ownUpd = U && jI && (kI0 || kI1);
+    const int tilePair = ty * TX + lane;
+    double *ownA = A + j * b.s1 + k;
+    uint64_t mb = 0;  // fused eps: Max(|B - A|) as a bit pattern
     bool seen = false;
 
-    // wait for plane q (in step q - 2), [fused: replace the elements outside the
-    // box, do the update of the own cells], convert it in place to q61; the
-    // thread's range flag
+    // wait for plane q (in step q - 2), [fused: do the update of the own pair,
+    // replace the elements outside the box], convert it to q61 (in place, or
+    // into the q61 ring); the thread's range flag
     auto arrive = [&](int q) -> bool {
         if (!tma::mbarWait(barOf(q), parityOf(q))) {
             if (status) atomicExch(status, DVMHGB_ERR_TMA_TIMEOUT);
@@ -211,7 +235,20 @@ __global__ void __launch_bounds__(TX *TY, MINB)
         const bool zIn = S && planeIn(z), upd = U && q >= 1 && q <= nplanes;
         bool bad = false;
         ulonglong2 *s2 = reinterpret_cast<ulonglong2 *>(slotOf(q)), *d2 = reinterpret_cast<ulonglong2 *>(qslotOf(q));
-        const ulonglong2 *tile = reinterpret_cast<const ulonglong2 *>(slotOf(q) + tma::SLOT / 8);
+        if (U && upd && ownUpd) {  // before this thread's conversion of its own pair overwrites B's doubles
+            const ulonglong2 br = s2[pr[0]];
+            const ulonglong2 ar = reinterpret_cast<const ulonglong2 *>(slotOf(q) + tma::SLOT / 8)[tilePair];
+            const double x = __longlong_as_double((long long)br.x), y = __longlong_as_double((long long)br.y);
+            const double ax = __longlong_as_double((long long)ar.x), ay = __longlong_as_double((long long)ar.y);
+            // |B - A| on the FP64 unit (idle beside the q61 sums), MAX on the bit patterns
+            if (kI0) mb = sf::absmax_bits(sf::nadd(x, -ax), mb);
+            if (kI1) mb = sf::absmax_bits(sf::nadd(y, -ay), mb);
+            seen = true;
+            double *pa = ownA + z * b.s0;
+            if (kI0 && kI1) st2cs(pa, make_double2(x, y));
+            else if (kI0) pa[0] = x;
+            else pa[1] = y;
+        }
 #pragma unroll
         for (int u = 0; u < NP; u++) {
             if (!(fl[u] & 1u)) continue;
@@ -225,23 +262,6 @@ __global__ void __launch_bounds__(TX *TY, MINB)
             }
             bad |= !sf::q61_ok(x) || !sf::q61_ok(y);
             d2[pr[u]] = make_ulonglong2(sf::q61(x), sf::q61(y));
-            if (U && upd && (fl[u] & 24u)) {
-                const ulonglong2 ar = tile[toff[u]];
-                const double ax = __longlong_as_double((long long)ar.x), ay = __longlong_as_double((long long)ar.y);
-                const bool u0 = (fl[u] & 8u) != 0, u1 = (fl[u] & 16u) != 0;
-                const bool ok0 = sf::q61_ok(x) && sf::q61_ok(ax), ok1 = sf::q61_ok(y) && sf::q61_ok(ay);
-                const uint64_t b0 = sf::q61(x), a0 = sf::q61(ax), b1 = sf::q61(y), a1 = sf::q61(ay);
-                const uint64_t d0 = b0 > a0 ? b0 - a0 : a0 - b0, d1 = b1 > a1 ? b1 - a1 : a1 - b1;
-                if (u0 && ok0 && d0 > qmax) qmax = d0;
-                if (u1 && ok1 && d1 > qmax) qmax = d1;
-                if (u0 && !ok0) mb = sf::absmax_bits(sf::nadd(x, -ax), mb);  // rare: outside the range
-                if (u1 && !ok1) mb = sf::absmax_bits(sf::nadd(y, -ay), mb);
-                seen = true;
-                double *pa = A + z * b.s0 + goff[u];
-                if (u0 && u1) st2cs(pa, make_double2(x, y));
-                else if (u0) pa[0] = x;
-                else pa[1] = y;
-            }
         }
         // these generic-proxy writes come before the slot's next TMA copy
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
@@ -322,13 +342,8 @@ __global__ void __launch_bounds__(TX *TY, MINB)
         }
         out += b.s0;
     }
-    if (U) {  // RN(max |b - a|) from the fixed-point part, then the MAX with the FP64-unit part
-        double m = -__builtin_huge_val();
-        if (seen) {
-            const double qd = __ull2double_rn(qmax) * 0x1p-61;
-            const double f = sf::from(mb);
-            m = qd > f ? qd : f;
-        }
+    if (U) {
+        double m = seen ? sf::from(mb) : -__builtin_huge_val();
         m = ctaMax(m, shr);
         if (tid == 0) items[blockIdx.x + gridDim.x * ((long)blockIdx.y + (long)gridDim.y * blockIdx.z)] = m;
     }

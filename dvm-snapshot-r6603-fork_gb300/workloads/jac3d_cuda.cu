@@ -47,9 +47,10 @@ void stencilDesc(int v, float *d) {
     } else if (v < V_T) {
         const int *c = q[v - V_Q];
         d[2] = 1, d[3] = 5, d[4] = 1, d[5] = (float)c[0], d[6] = (float)c[1] / (float)c[2];
-    } else {  // ring of 6 (4 for V_T + 1); from V_T + 2 on, 1.. of the 8 warps on the FP64 unit
-        d[2] = v == V_T + 1 ? 1.0f + 4.0f / 6.0f : 2.0f, d[3] = 5, d[4] = 1, d[5] = 4;
-        d[6] = v >= V_T + 2 ? (float)(v - V_T - 1) / 8.0f : 0.0f;
+    } else {  // TMA-staged: ring planes, warps (of 8) on the FP64 unit
+        static const int t[5][2] = {{6, 0}, {4, 0}, {6, 1}, {6, 2}, {6, 3}};
+        const int *c = t[v - V_T];
+        d[2] = 1.0f + (float)c[0] / 6.0f, d[3] = 5, d[4] = 1, d[5] = 4, d[6] = (float)c[1] / 8.0f;
     }
 }
 const float *variantDesc(int handler) {

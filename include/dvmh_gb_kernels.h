@@ -43,7 +43,7 @@ int dvmhgb_jac3d_update(double *A, const double *B, const long st[3], const long
  * den): 14 (4, 0/1), 15 (3, 0/1), 16 (4, 1/2), 17 (4, 1/3), 18 (4, 2/5),
  * 19 (3, 1/2), 20 (4, 1/4), 21 (4, 3/5); v = 22, 23: the fixed-point sums
  * with the source planes staged in shared memory by TMA box copies, a ring of
- * 6 / 4 planes per CTA (a copy that does not land within about 2^22 polls
+ * 6 / 4 planes per CTA (a copy that does not land within 2 s
  * writes DVMHGB_ERR_TMA_TIMEOUT to dvmhgb_status_word() and the CTA stops);
  * v = 24, 25, 26: ring of 6, with 1, 2, 3 of the CTA's 8 warps computing their
  * cells on the FP64 unit (division by 6 as one multiply and two FMAs);
