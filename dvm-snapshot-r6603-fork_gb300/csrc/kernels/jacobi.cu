@@ -1104,7 +1104,7 @@ int launchT(const CUtensorMap &map, double *A, double *Out, const Box3 &b, const
         }
     }
     kStencil3T<0, NS, 4, W><<<g.grid, dim3(TX, TY), smem, s>>>(map, map, map, A, nullptr, Out, b, g.p0, g.ichunk,
-                                                               nullptr, dvmhgb_status_word());
+                                                               nullptr, dvmhgb_status_word(), nullptr);
     return 0;
 }
 
@@ -1295,10 +1295,10 @@ int dvmhgb_jac3d_fused(double *A, const double *B, double *Bnew, const long st[3
         int *status = dvmhgb_status_word();
         if (native == V3_TF)
             kStencil3T<2, 5, 4, 0><<<g.grid, blk, tma::smemBytes(true, 5), s>>>(mapB, mapA, mapT, A, B, Bnew, b, g.p0,
-                                                                                g.ichunk, items, status);
+                                                                                g.ichunk, items, status, nullptr);
         else
-            kStencil3T<2, 4, 4, 0><<<g.grid, blk, tma::smemBytes(true, 4), s>>>(mapB, mapA, mapT, A, B, Bnew, b, g.p0,
-                                                                                g.ichunk, items, status);
+            kStencil3T<2, 5, 3, 0><<<g.grid, blk, tma::smemBytes(true, 5), s>>>(mapB, mapA, mapT, A, B, Bnew, b, g.p0,
+                                                                                g.ichunk, items, status, nullptr);
         dvmhgb_count_launches(1);
         if (cudaGetLastError() != cudaSuccess) return -1;
         return dvmhgb_copy_outside_box(3, B, Bnew, st, ext, lo, hi, stream);
@@ -1327,6 +1327,54 @@ int dvmhgb_jac3d_fused(double *A, const double *B, double *Bnew, const long st[3
     dvmhgb_count_launches(1);
     if (cudaGetLastError() != cudaSuccess) return -1;
     return dvmhgb_copy_outside_box(3, B, Bnew, st, ext, lo, hi, stream);
+}
+
+long dvmhgb_jac3d_stnupd_items(const long lo[3], const long hi[3], int variant) {
+    if (variant < 0 || variant >= DVMHGB_JAC3D_STNUPD_VARIANTS) return -1;
+    St3Geom g = st3Geom(lo, hi, TY);
+    return (long)g.grid.x * g.grid.y * g.grid.z;
+}
+
+int dvmhgb_jac3d_stnupd(const double *A, double *Aalt, double *B, const long st[3], const long ext[3],
+                        const long lo[3], const long hi[3], double *items, int variant, void *stream) {
+    if (variant < 0 || variant >= DVMHGB_JAC3D_STNUPD_VARIANTS) return -1;
+    St3Geom g = st3Geom(lo, hi, TY);
+    if (!g.ok || !A || !Aalt || !B || !items || A == Aalt || A == B || Aalt == B || !rows16(st, 3) ||
+        !aligned16(A) || !aligned16(Aalt) || !aligned16(B))
+        return -1;
+    Box3 b{st[0], st[1], ext[0], ext[1], ext[2], lo[0], lo[1], lo[2], hi[0], hi[1], hi[2]};
+    CUtensorMap map;
+    if (!encodeMap3(&map, A, ext, st, tma::BX, tma::BY)) return -1;
+    cudaStream_t s = (cudaStream_t)stream;
+    double *a = (double *)A;
+    const int smem = tma::smemBytes(false, 6, true);  // above 48 KB: opted in once per device
+    static std::atomic<unsigned long long> optedIn{0};
+    const int dev = gbdev::current();
+    if (dev < 0 || dev >= 64) return -1;
+    if (!(optedIn.load() >> dev & 1ull)) {
+        if (cudaFuncSetAttribute(kStencil3T<3, 6, 4, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem) !=
+                cudaSuccess ||
+            cudaFuncSetAttribute(kStencil3T<3, 6, 4, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem) !=
+                cudaSuccess ||
+            cudaFuncSetAttribute(kStencil3T<3, 6, 4, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem) !=
+                cudaSuccess)
+            return -1;
+        optedIn.fetch_or(1ull << dev);
+    }
+    int *status = dvmhgb_status_word();
+    const dim3 blk(TX, TY);
+    if (variant == 0)
+        kStencil3T<3, 6, 4, 0><<<g.grid, blk, smem, s>>>(map, map, map, a, nullptr, B, b, g.p0, g.ichunk, items, status,
+                                                         Aalt);
+    else if (variant == 1)
+        kStencil3T<3, 6, 4, 1><<<g.grid, blk, smem, s>>>(map, map, map, a, nullptr, B, b, g.p0, g.ichunk, items, status,
+                                                         Aalt);
+    else
+        kStencil3T<3, 6, 4, 2><<<g.grid, blk, smem, s>>>(map, map, map, a, nullptr, B, b, g.p0, g.ichunk, items, status,
+                                                         Aalt);
+    dvmhgb_count_launches(1);
+    if (cudaGetLastError() != cudaSuccess) return -1;
+    return dvmhgb_copy_outside_box(3, A, Aalt, st, ext, lo, hi, stream);  // A's cells outside the box carry over
 }
 
 long dvmhgb_jac2d_update_items(const long lo[2], const long hi[2]) {

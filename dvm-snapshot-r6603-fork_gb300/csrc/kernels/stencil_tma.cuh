@@ -48,6 +48,13 @@
 // store except this CTA's own tile copy, which landed before it.  32 bytes a
 // cell: A and B read, A and Out written.
 //
+// Stencil then update (M = 3): a time step's stencil loop followed by the next
+// step's update loop, eps = Max(|B - A|, eps); A = B.  The new B of a cell is
+// in a register when its A (the stencil's own source value) is in the slot, so
+// the update needs no pass of its own: |B - A| on the FP64 unit, and B stored
+// into A's second buffer, which becomes A when the pair ends (A itself is
+// still read by the CTAs around).  24 bytes a cell: A read, B and A written.
+//
 // FP64-unit warps (W > 0): the q61 sums keep the integer pipes busy while the
 // FP64 unit idles, so the last W warps of the CTA compute their cells on the
 // FP64 unit -- five additions in the source order and RN(sum / 6) by
@@ -134,20 +141,24 @@ __device__ __forceinline__ void copyBox(const CUtensorMap *map, uint32_t dst, ui
 
 // mapS: the stencil's source box copies (M = 0: A, else B); mapA (M >= 1):
 // A's box copies for planes outside the loop box; mapT (M = 2): A's own-cell
-// tiles.  items (M = 2): one MAX partial per CTA.
+// tiles.  items (M = 2, 3): one MAX partial per CTA; Out2 (M = 3): A's second
+// buffer.
 template <int M, int NS, int MINB, int W>
 __global__ void __launch_bounds__(TX *TY, MINB)
     kStencil3T(const __grid_constant__ CUtensorMap mapS, const __grid_constant__ CUtensorMap mapA,
                const __grid_constant__ CUtensorMap mapT, double *A, const double *__restrict__ B, double *Out, Box3 b,
-               long p0, int ichunk, double *items, int *status) {
+               long p0, int ichunk, double *items, int *status, double *Out2) {
     static_assert(NS >= 4, "the ring holds planes i - 1, i, i + 1 and the slot being refilled");
-    constexpr bool S = M >= 1, U = M == 2;  // source A_new; the update loop too
+    static_assert(M >= 0 && M <= 3 && M != 1, "modes 0, 2 and 3");
+    constexpr bool S = M == 2, U = M == 2;  // source A_new; the update loop too
+    constexpr bool E = M == 3;              // the next step's update loop after the stencil
+    constexpr bool QR = W > 0 || E;         // the q61 values in their own ring, the slots keep the doubles
     constexpr int SB = tma::slotBytes(U);
     constexpr int NP = (tma::PAIRS + TX * TY - 1) / (TX * TY);  // box pairs a thread converts
     extern __shared__ unsigned char dyn[];
     unsigned char *base = dyn + ((128u - (tma::smemAddr(dyn) & 127u)) & 127u);
-    uint64_t *qring = reinterpret_cast<uint64_t *>(base + NS * SB);  // W > 0
-    uint64_t *bars = reinterpret_cast<uint64_t *>(base + NS * SB + (W > 0 ? tma::QSLOTS * tma::SLOT : 0));
+    uint64_t *qring = reinterpret_cast<uint64_t *>(base + NS * SB);  // QR
+    uint64_t *bars = reinterpret_cast<uint64_t *>(base + NS * SB + (QR ? tma::QSLOTS * tma::SLOT : 0));
     // the timeout flag, one per parity of the step: a thread sets the flag of
     // its step before the step's barrier and every thread reads it after that
     // barrier, so a flag set in step t + 1 cannot reach a thread still reading
@@ -167,7 +178,7 @@ __global__ void __launch_bounds__(TX *TY, MINB)
 
     auto slotOf = [&](int q) { return reinterpret_cast<uint64_t *>(base + (size_t)(q % NS) * SB); };
     // where plane q's q61 values go: in place, or (W > 0) the q61 ring, the slot keeping the doubles
-    auto qslotOf = [&](int q) { return W > 0 ? qring + (size_t)(q % tma::QSLOTS) * (tma::SLOT / 8) : slotOf(q); };
+    auto qslotOf = [&](int q) { return QR ? qring + (size_t)(q % tma::QSLOTS) * (tma::SLOT / 8) : slotOf(q); };
     auto barOf = [&](int q) { return tma::smemAddr(bars + q % NS); };
     auto parityOf = [](int q) { return (uint32_t)((q / NS) & 1); };
     auto planeIn = [&](long z) { return z >= b.lo0 && z <= b.hi0; };
@@ -258,7 +269,7 @@ __global__ void __launch_bounds__(TX *TY, MINB)
                 const double *pa = A + z * b.s0 + goff[u];
                 if (fl[u] & 2u) x = pa[0];
                 if (fl[u] & 4u) y = pa[1];
-                if (W > 0) s2[pr[u]] = make_ulonglong2(sf::bits(x), sf::bits(y));  // the FP64-unit warps' source
+                if (QR) s2[pr[u]] = make_ulonglong2(sf::bits(x), sf::bits(y));  // the slot keeps the source doubles
             }
             bad |= !sf::q61_ok(x) || !sf::q61_ok(y);
             d2[pr[u]] = make_ulonglong2(sf::q61(x), sf::q61(y));
@@ -298,6 +309,7 @@ __global__ void __launch_bounds__(TX *TY, MINB)
     bool stop = stopAt[1] != 0;  // (a timeout of q = 0 is seen in step 0)
     const int r0 = (ty + 1) * tma::BX + 2 + 2 * lane;  // the thread's pair in a slot
     double *out = Out + ib * b.s0 + j * b.s1 + k;
+    double *const outBase = out, *const out2 = E ? Out2 + ib * b.s0 + j * b.s1 + k : nullptr;
     for (int t = 0; t < nplanes && !stop; t++) {
         const long i = ib + t;
         flags = ((flags << 1) | (__syncthreads_or(arrive(t + 2)) ? 1u : 0u)) & 7u;
@@ -340,9 +352,19 @@ __global__ void __launch_bounds__(TX *TY, MINB)
             else if (kI0) out[0] = v0;
             else if (kI1) out[1] = v1;
         }
+        if (E && jI) {  // the next update: eps = Max(|B - A|, eps) with A's doubles of the slot; A = B into A's second buffer
+            const double2 a = *reinterpret_cast<const double2 *>(reinterpret_cast<const double *>(slotOf(t + 1)) + r0);
+            if (kI0) mb = sf::absmax_bits(sf::nadd(v0, -a.x), mb);
+            if (kI1) mb = sf::absmax_bits(sf::nadd(v1, -a.y), mb);
+            seen = seen || kI0 || kI1;
+            double *o2 = out2 + (out - outBase);
+            if (kI0 && kI1) st2cs(o2, make_double2(v0, v1));
+            else if (kI0) o2[0] = v0;
+            else if (kI1) o2[1] = v1;
+        }
         out += b.s0;
     }
-    if (U) {
+    if (U || E) {
         double m = seen ? sf::from(mb) : -__builtin_huge_val();
         m = ctaMax(m, shr);
         if (tid == 0) items[blockIdx.x + gridDim.x * ((long)blockIdx.y + (long)gridDim.y * blockIdx.z)] = m;

@@ -67,6 +67,7 @@ struct Settings {
     int tuneMode = 0;           // 0 off, 1 exhaustive, 2 model-guided (DVMH_OPT_PARAMS)
     int graphCacheMax = 64;
     bool fuse = true;
+    bool defer = true;          // DVMH_GB_DEFER: loops that start a fusion rule may wait in the queue for their second
     bool hostProf = false;      // DVMH_GB_HOSTPROF: time the ABI entry points on the host
     bool autoTfm = true;        // DVMH_GB_AUTOTFM: honour dvmh_loop_autotransform_C (else keep natural layouts)
     bool reduceDeps = false;    // DVMH_REDUCE_DEPS: no dependence on ACROSS axes with one iteration
@@ -231,6 +232,7 @@ struct Loop : Obj {
     bool hasHost = false, hasCuda = false;
     std::string file;
     long line = 0;
+    size_t regionElems = 0;  // the most elements of the region's arrays (a queued loop may outlive its region)
 };
 
 struct RegionVar {
@@ -374,6 +376,14 @@ void regularRegionEnd();  // data exit of the variables a region (or a loop outs
 // ---------------------------------------------------------------- loops / batching (rt_loop.cpp)
 
 void queueFlush();  // run or replay everything queued (batched mode)
+// run the queued loops up to the last one that names v (a parameter or a
+// reduction variable); later loops stay queued
+void queueFlushVar(const Var *v);
+// the same for the last queued loop that names any variable (a region's end:
+// loops over arrays alone may stay queued past it)
+void queueFlushVars();
+void queueRegionEnded(const Region *r);  // queued loops of an ended region forget it
+Var *regularVarOfHeader(const void *p);  // the rank-0 regular variable whose header p is, or null
 bool queueBusy();
 void loopsAtExit();
 void graphsForget(const Obj *a);  // drop the cached graphs that name a freed array or variable

@@ -129,6 +129,7 @@ static void loadSettings() {
     if (const char *t = getenv("DVMH_OPT_PARAMS")) settings.tuneMode = atoi(t);
     if (const char *h = getenv("DVMH_GB_HOSTPROF")) settings.hostProf = atoi(h) != 0;
     if (const char *f = getenv("DVMH_GB_FUSE")) settings.fuse = atoi(f) != 0;
+    if (const char *f = getenv("DVMH_GB_DEFER")) settings.defer = atoi(f) != 0;
     if (const char *t = getenv("DVMH_GB_AUTOTFM")) settings.autoTfm = atoi(t) != 0;
     if (const char *r = getenv("DVMH_REDUCE_DEPS")) settings.reduceDeps = atoi(r) != 0;
 }
@@ -888,9 +889,11 @@ void dvmh_region_end_C(DvmType curRegion) {
     GB_PROF("dvmh_region_end_C");
     Region *r = regionOf(curRegion, "dvmh_region_end");
     GB_CHECK(!st.curLoop, "region ends inside a parallel loop");
-    // everything queued inside the region is launched by its end: handler
-    // parameters may point at variables that live only as long as the region
-    queueFlush();
+    // every queued loop that names a variable is launched by the region's end:
+    // handler parameters may point at variables that live only as long as the
+    // region; loops over arrays alone may stay queued (they forget the region)
+    queueFlushVars();
+    queueRegionEnded(r);
     for (auto &ra : r->arrays)
         if (ra.intent & INTENT_OUT) {
             ra.arr->devActual = true;

@@ -289,7 +289,7 @@ Staging &stageFor(const Var *v) {
 void varH2D(Var *v) {
     GB_PROF("varH2D");
     ensureVarDev(v);
-    queueFlush();
+    queueFlushVar(v);  // the queued loops that name v run first; the others do not see the copy
     Staging &s = stageFor(v);
     GB_CUDA(cudaEventSynchronize(s.done));
     memcpy(s.buf, v->addr, v->size);
@@ -312,7 +312,7 @@ void varForgetStaging(const Var *v) {
 void varD2H(Var *v) {
     GB_PROF("varD2H");
     GB_INTERNAL(v->dev, "variable without a device copy");
-    queueFlush();
+    queueFlushVar(v);
     Staging &s = stageFor(v);
     GB_CUDA(cudaEventSynchronize(s.done));
     GB_CUDA(cudaMemcpyAsync(s.buf, v->dev, v->size, cudaMemcpyDeviceToHost, gpu.stream));

@@ -382,7 +382,9 @@ static void runQueued(const std::vector<Loop *> &q) {
             DvmHandlerFunc fused = nullptr;
             for (auto &r : fusionRules)
                 if (r.first == l->cuda.func && r.second == q[i + 1]->cuda.func) fused = r.fused;
-            if (fused && l->region == q[i + 1]->region && l->cuda.nparams + q[i + 1]->cuda.nparams <= 40) {
+            // the same region, or a first loop left queued past its region's end (it names arrays only)
+            const bool regionsOk = l->region == q[i + 1]->region || l->region == nullptr;
+            if (fused && regionsOk && l->cuda.nparams + q[i + 1]->cuda.nparams <= 40) {
                 runFused(fused, l, q[i + 1]);
                 i += 2;
                 continue;
@@ -494,11 +496,66 @@ static void dropGraph(CachedGraph &g) {
     for (void *p : g.hostScratch) hostFree(p);
 }
 
-void queueFlush() {
+// the variable a queued loop's parameter names -- its address, or the header
+// of a rank-0 regular variable -- or null (an array descriptor, no variable)
+static const Var *paramVar(const void *p) {
+    if (isArrayDesc(p)) return nullptr;
+    size_t off = 0;
+    if (const Var *v = varAt(p, &off)) return v;
+    return regularVarOfHeader(p);
+}
+
+static bool loopNamesVar(const Loop *l, const Var *v) {
+    for (int i = 0; i < l->cuda.nparams; i++) {
+        const Var *pv = paramVar(l->cuda.params[i]);
+        if (pv && (v == nullptr || pv == v)) return true;
+    }
+    for (auto &r : l->reds)
+        if ((r.var && (v == nullptr || r.var == v)) || (r.locVar && (v == nullptr || r.locVar == v))) return true;
+    return false;
+}
+
+static void queueFlushPrefix(size_t count);
+
+// A queued loop may wait for a later one only when that can pay: it names no
+// variable, and a fusion rule starts with its handler (the next loop may be
+// the rule's second).  Every other loop runs at the first flush that reaches it.
+static bool deferrable(const Loop *l) {
+    if (!settings.defer || !settings.fuse || loopNamesVar(l, nullptr)) return false;
+    for (auto &r : fusionRules)
+        if (r.first == l->cuda.func) return true;
+    return false;
+}
+
+void queueFlushVar(const Var *v) {
+    size_t last = 0;
+    for (size_t i = 0; i < queue.size(); i++)
+        if (loopNamesVar(queue[i], v) || !deferrable(queue[i])) last = i + 1;
+    if (last) queueFlushPrefix(last);
+}
+
+void queueFlushVars() { queueFlushVar(nullptr); }
+
+void queueRegionEnded(const Region *r) {
+    for (Loop *l : queue)
+        if (l->region == r) l->region = nullptr;
+}
+
+void queueFlush() { queueFlushPrefix(queue.size()); }
+
+// Run (or replay) the first `count` queued loops as one group; the rest stay
+// queued, in order.  A loop stays queued past a variable's host access or its
+// region's end only if it is deferrable (above) and does not name that
+// variable (handler parameters may point at variables that live only as long
+// as the region; arrays live until they are freed, which flushes everything).
+// So a time step's last loop over arrays alone can meet the next step's first
+// loop in one group, where a fusion rule joins them.
+static void queueFlushPrefix(size_t count) {
     GB_PROF("queueFlush");
-    if (queue.empty() || ctx.capturing) return;
-    std::vector<Loop *> q;
-    q.swap(queue);
+    if (queue.empty() || ctx.capturing || count == 0) return;
+    if (count > queue.size()) count = queue.size();
+    std::vector<Loop *> q(queue.begin(), queue.begin() + (long)count);
+    queue.erase(queue.begin(), queue.begin() + (long)count);
     stats.flushes++;
     if (settings.tuneMode && tunerExploring()) {
         // variants are still being tried: run the queue as it is, each handler timed on its own
@@ -819,6 +876,7 @@ void dvmh_loop_perform_C(DvmType curLoop) {
         return;
     }
     if (settings.mode == MODE_BATCHED) {
+        for (auto &ra : l->region->arrays) l->regionElems = std::max(l->regionElems, ra.arr->delems);
         afterReductions(l, false);
         queue.push_back(l);
         return;
@@ -891,7 +949,7 @@ DvmType dvmh_loop_guess_index_type_C(DvmType curLoop) {
     if (l->region)
         for (auto &ra : l->region->arrays) maxElems = std::max(maxElems, ra.arr->delems);
     else
-        maxElems = maxDeviceElems();
+        maxElems = l->regionElems ? l->regionElems : maxDeviceElems();  // queued past the region's end, or outside
     return maxElems < (size_t)2147483647 ? rt_INT : rt_LLONG;
 }
 
@@ -1137,6 +1195,11 @@ void dvmhgb_set_reduce_dependences(int on) {
 }
 
 void dvmhgb_flush(void) { queueFlush(); }
+
+void dvmhgb_set_deferral(int on) {
+    queueFlush();
+    settings.defer = on != 0;
+}
 
 void dvmhgb_sync(void) {
     queueFlush();

@@ -95,6 +95,12 @@ bool regularActual(const void *addr, bool toHost) {
     return true;
 }
 
+Var *regularVarOfHeader(const void *p) {
+    for (auto &kv : regularVars)
+        if (kv.second.var && (const void *)kv.second.var->hdr == p) return kv.second.var;
+    return nullptr;
+}
+
 void regularRegionEnd() {
     std::vector<const char *> pending;
     pending.swap(autoExit);

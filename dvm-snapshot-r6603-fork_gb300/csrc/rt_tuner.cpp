@@ -62,6 +62,7 @@ struct VariantState {
     int chosen = -1;
     std::vector<int> order;      // model-guided: variants fastest first by the model
     int explore = -1;            // variants to try (-1: all)
+    bool ranked = false;         // model-guided: the model has ordered the variants
     int explored = 0;            // executions that tried an untried variant
     double exploreSeconds = 0;   // their summed time
     void *handler = nullptr;
@@ -148,12 +149,17 @@ int tunerVariant(SpecLoop *s, int nvariants, int dflt, const float *desc, int nd
         vs = VariantState();
         vs.handler = s->handler;
         vs.nvariants = nvariants;
-        if (settings.tuneMode == 2 && ndesc > 0 && variantModelReady()) {
-            std::vector<std::vector<float>> feats(nvariants, std::vector<float>(TUNE_NF));
-            for (int v = 0; v < nvariants; v++) variantFeatures(l, desc + (size_t)v * ndesc, ndesc, feats[v].data());
-            rankByVariantModel(feats, vs.order);
-            vs.explore = (int)std::floor(tuneFrac() * nvariants);
-        }
+    }
+    // the model ranks the variants at the first query outside a graph capture
+    // (its inference runs kernels and reads their result); a query inside a
+    // capture gets the default, and the shape counts as exploring until then,
+    // so the next flush runs uncaptured
+    if (!vs.ranked && !bestOnly && settings.tuneMode == 2 && ndesc > 0 && variantModelReady()) {
+        std::vector<std::vector<float>> feats(nvariants, std::vector<float>(TUNE_NF));
+        for (int v = 0; v < nvariants; v++) variantFeatures(l, desc + (size_t)v * ndesc, ndesc, feats[v].data());
+        rankByVariantModel(feats, vs.order);
+        vs.explore = (int)std::floor(tuneFrac() * nvariants);
+        vs.ranked = true;
     }
     int v = -1;
     bool exploring = false;

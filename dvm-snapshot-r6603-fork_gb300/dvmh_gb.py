@@ -109,6 +109,11 @@ def force_variant(v):
     init().dvmhgb_force_variant(int(v))
 
 
+def set_deferral(on):
+    """Whether queued loops that start a fusion rule may wait for the next loop (dvmhgb_set_deferral)."""
+    init().dvmhgb_set_deferral(1 if on else 0)
+
+
 def sync():
     init().dvmhgb_sync()
 

@@ -25,6 +25,8 @@
 // the pair: the update kernel, then that stencil into the second buffer (1.354 per step; the one-pass TMA pair
 // 1.66, the update and the TMA stencil running at the same time 1.66, the register-staged one-pass pair 2.01)
 #define DEF_FUSED 25
+// a step's stencil with the next step's update in one pass (the pairing the runtime forms across steps)
+#define DEF_STNUPD 1
 
 namespace {
 
@@ -55,8 +57,16 @@ void stencilDesc(int v, float *d) {
 }
 const float *variantDesc(int handler) {
     static float upd[3 * NDESC], stn[DVMHGB_JAC3D_VARIANTS * NDESC], fus[DVMHGB_JAC3D_FUSED_VARIANTS * NDESC];
+    static float su[DVMHGB_JAC3D_STNUPD_VARIANTS * NDESC];
     static bool ready = false;
     if (!ready) {
+        for (int v = 0; v < DVMHGB_JAC3D_STNUPD_VARIANTS; v++) {  // handler 4: stencil then the next update, one pass
+            float *d = su + v * NDESC;
+            d[0] = 1, d[1] = 4;
+            stencilDesc(V_T, d);
+            d[6] = (float)v / 8.0f;  // warps on the FP64 unit
+            d[7] = 0;
+        }
         for (int v = 0; v < 3; v++) upd[v * NDESC] = 1, upd[v * NDESC + 1] = 1, upd[v * NDESC + 2] = (float)v;
         for (int v = 0; v < DVMHGB_JAC3D_VARIANTS; v++) {
             float *d = stn + v * NDESC;
@@ -84,7 +94,7 @@ const float *variantDesc(int handler) {
         }
         ready = true;
     }
-    return handler == 1 ? upd : (handler == 2 ? stn : fus);
+    return handler == 1 ? upd : (handler == 2 ? stn : (handler == 3 ? fus : su));
 }
 
 struct ArrDev {
@@ -189,13 +199,51 @@ extern "C" void loop_jac3d_fused_cuda(DvmType refs[2], DvmType A_hdr[], DvmType 
     dvmh_loop_cuda_red_finish_C(upd, 1);
 }
 
-// module initialiser: the fusion rule (the role DvmhModuleInitializer plays for
+// refs[0]: a time step's stencil loop (A_hdr, B_hdr), refs[1]: the next step's
+// update loop (A2_hdr, B2_hdr, eps_ptr) -- the pair the runtime forms when the
+// stencil, naming arrays only, stays queued past its step's region (one pass:
+// the update's |B - A| and A = B on the stencil's new values, 24 bytes a cell)
+extern "C" void loop_jac3d_stnupd_cuda(DvmType refs[2], DvmType A_hdr[], DvmType B_hdr[], DvmType A2_hdr[],
+                                        DvmType B2_hdr[], double *eps_ptr) {
+    DvmType stn = refs[0], upd = refs[1];
+    long lo[R], hi[R], lo2[R], hi2[R];
+    bounds(stn, lo, hi);
+    bounds(upd, lo2, hi2);
+    bool same = A_hdr == A2_hdr && B_hdr == B2_hdr;
+    for (int i = 0; i < R; i++) same = same && lo[i] == lo2[i] && hi[i] == hi2[i];
+    if (!same) {  // not the pattern the one-pass kernel implements: the loops one after the other
+        loop_jac3d_stn_cuda(&stn, A_hdr, B_hdr);
+        loop_jac3d_upd_cuda(&upd, A2_hdr, B2_hdr, eps_ptr);
+        return;
+    }
+    DvmType device_num = dvmh_loop_get_device_num_C(upd);
+    ArrDev A = devArray(upd, device_num, A_hdr), B = devArray(upd, device_num, B_hdr);
+    dim3 threads(0, 0, 0);
+    cudaStream_t stream;
+    dvmh_loop_cuda_get_config_C(stn, 0, 0, &threads, &stream, 0);
+    dvmh_loop_cuda_get_config_C(upd, 0, 0, &threads, &stream, 0);
+    const int variant =
+        dvmhgb_loop_variant_desc(upd, DVMHGB_JAC3D_STNUPD_VARIANTS, DEF_STNUPD, variantDesc(4), NDESC);
+    double eps, *eps_grid = 0;
+    dvmh_loop_cuda_register_red_C(upd, 1, (void **)&eps_grid, 0);
+    dvmh_loop_red_init_C(upd, 1, &eps, 0);
+    dvmh_loop_cuda_red_prepare_C(upd, 1, dvmhgb_jac3d_stnupd_items(lo, hi, variant), 0);
+    // the new A goes into A's second buffer: A is read by the pass; the two swap when the pair ends
+    double *Aalt = (double *)dvmhgb_loop_alt_buffer(upd, A_hdr);
+    check(dvmhgb_jac3d_stnupd(A.base, Aalt, B.base, A.st, A.ext, lo, hi, eps_grid, variant, stream),
+          "loop_jac3d_stnupd_cuda");
+    dvmh_loop_cuda_red_finish_C(upd, 1);
+}
+
+// module initialiser: the fusion rules (the role DvmhModuleInitializer plays for
 // generated code, rts/dvmh/include/dvmhlib2.h:236-247)
 namespace {
 struct Rules {
     Rules() {
         dvmhgb_register_fusion((DvmHandlerFunc)loop_jac3d_upd_cuda, (DvmHandlerFunc)loop_jac3d_stn_cuda,
                                (DvmHandlerFunc)loop_jac3d_fused_cuda);
+        dvmhgb_register_fusion((DvmHandlerFunc)loop_jac3d_stn_cuda, (DvmHandlerFunc)loop_jac3d_upd_cuda,
+                               (DvmHandlerFunc)loop_jac3d_stnupd_cuda);
     }
 } rules;
 }  // namespace

@@ -42,6 +42,16 @@ void dvmhgb_sync(void);    /* flush and wait for the GPU */
  * with dvmhgb_loop_param.  Both apply in batched mode only. */
 void dvmhgb_register_fusion(DvmHandlerFunc first, DvmHandlerFunc second, DvmHandlerFunc fused);
 void dvmhgb_register_batch(DvmHandlerFunc single, DvmHandlerFunc batched);
+/* Deferred loops.  In batched mode a queued loop whose handler starts a fusion
+ * rule, and whose parameters name arrays only (no variable), need not run when
+ * a variable is read or written on the host or when its region ends: it waits
+ * in the queue for the next loop, so that a time step's last loop and the next
+ * step's first loop can meet in one flush (the region's end no longer forces
+ * it: handler parameters that could die with the region are variables, and a
+ * loop naming one is still run by then).  Every access to the loop's arrays,
+ * freeing them, a mode change or dvmhgb_flush still runs it first.  On by
+ * default; dvmhgb_set_deferral(0) or env DVMH_GB_DEFER=0 turns it off. */
+void dvmhgb_set_deferral(int on);
 void *dvmhgb_loop_param(DvmType loopRef, DvmType index);
 /* Device base (natural base) of a second buffer with the same layout as the
  * array; when the loop ends the array's device buffer and this one swap. */

@@ -77,6 +77,19 @@ int dvmhgb_jac3d_stencil(const double *A, double *B, const long st[3], const lon
 #define DVMHGB_JAC3D_FUSED_T (DVMHGB_JAC3D_VARIANTS + 5)
 #define DVMHGB_JAC3D_FUSED_VARIANTS (DVMHGB_JAC3D_VARIANTS + 7)
 long dvmhgb_jac3d_fused_items(const long lo[3], const long hi[3], int native);
+/* The other pairing of the same loops, across a time-step boundary: step n's
+ * stencil loop B = (6 neighbours of A) / 6 followed by step n+1's update loop
+ * eps = Max(|B - A|, eps); A = B over the same box.  B is written in place,
+ * the new A into Aalt (a second buffer of A's layout, to become A: A is still
+ * read while the pass runs; A's cells outside the box are copied over), MAX
+ * partials into items (dvmhgb_jac3d_stnupd_items).  24 bytes a cell.  The
+ * TMA-staged fixed-point stencil, variant = its warps on the FP64 unit (0, 1,
+ * 2 of 8).  The runtime pairs the loops so when a program's time steps leave
+ * the stencil queued past the step's end (deferred loops, dvmh_gb.h). */
+#define DVMHGB_JAC3D_STNUPD_VARIANTS 3
+long dvmhgb_jac3d_stnupd_items(const long lo[3], const long hi[3], int variant);
+int dvmhgb_jac3d_stnupd(const double *A, double *Aalt, double *B, const long st[3], const long ext[3],
+                        const long lo[3], const long hi[3], double *items, int variant, void *stream);
 int dvmhgb_jac3d_fused(double *A, const double *B, double *Bnew, const long st[3], const long ext[3],
                        const long lo[3], const long hi[3], double *items, int native, void *stream);
 

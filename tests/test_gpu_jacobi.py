@@ -114,9 +114,10 @@ def test_batched_mode_fuses_and_replays(g):
     j.close()
     assert s["loops_performed"] == 12
     assert s["fused_pairs"] >= 1
-    # the first call allocates the alternate buffer; afterwards the two buffers of B alternate
-    assert s["graphs_captured"] <= 3
-    assert s["graphs_captured"] + s["graph_replays"] == 6 and s["graph_replays"] >= 3
+    # one group per step: the first step's update alone, then each step's stencil with the next step's update
+    # (deferral); the first pair allocates A's second buffer, afterwards the two buffers of A alternate
+    assert s["graphs_captured"] <= 4
+    assert s["graphs_captured"] + s["graph_replays"] == 6 and s["graph_replays"] >= 2
 
 
 def test_plain_mode_no_fusion(g):
@@ -135,8 +136,10 @@ def test_jacobi3d_variants_vs_oracle(g, variant):
     """Every kernel variant of the 3-D loops (rows per thread x additions on the
     FP64 unit, the rest on the integer pipe; the fixed-point stencils; the
     unfused and overlapped pairs) through the program, plain (separate update
-    and stencil loops) and batched (the fused loop)."""
+    and stencil loops) and batched (the fused loop: deferral off, so that each
+    step's update and stencil meet in one flush)."""
     try:
+        g.set_deferral(False)
         g.force_variant(variant)
         for n, iters in ((19, 4), (66, 3), (131, 2)):
             e_ref, A_ref, B_ref = orc.jacobi_run(3, n, iters, 900 + n)
@@ -150,6 +153,74 @@ def test_jacobi3d_variants_vs_oracle(g, variant):
                 assert np.array_equal(A, A_ref) and np.array_equal(B, B_ref), (variant, n, mode)
     finally:
         g.force_variant(-1)
+        g.set_deferral(True)
+
+
+@pytest.mark.parametrize("variant", [-1, 0, 1, 2])
+def test_jacobi3d_stencil_then_next_update(g, variant):
+    """Batched mode with deferral (the default): each step's stencil, naming
+    arrays only, waits past its region for the next step's update loop, and the
+    fusion rule runs the two as one pass (dvmhgb_jac3d_stnupd: |B - A| and
+    A = B on the new B, A's second buffer swapped in).  eps of every step and
+    the final A, B bit-exact against the oracle; one such pair (run, or its
+    captured graph replayed) per step after the first."""
+    try:
+        g.force_variant(variant)
+        for n, iters in ((19, 4), (66, 5), (131, 3)):
+            e_ref, A_ref, B_ref = orc.jacobi_run(3, n, iters, 700 + n)
+            g.set_mode("batched")
+            j = g.Jacobi(3, n, 700 + n)
+            g.reset_stats()
+            eps = j.run(iters)
+            st = g.stats()
+            A, B = j.fetch()
+            j.close()
+            assert np.array_equal(eps, e_ref), (variant, n)
+            assert np.array_equal(A, A_ref) and np.array_equal(B, B_ref), (variant, n)
+            # every step after the first is one group (a captured graph, replayed once it repeats): the pair
+            assert st["fused_pairs"] >= 1 and st["fused_pairs"] + st["graph_replays"] == iters - 1, (variant, n, st)
+    finally:
+        g.force_variant(-1)
+
+
+@pytest.mark.parametrize("variant", [0, 1, 2])
+def test_jacobi3d_stnupd_kernel_sub_box(g, variant):
+    """dvmhgb_jac3d_stnupd through the C ABI over a box with array cells
+    outside it on every side: B = stencil(A) inside the box (outside untouched),
+    eps = max |B_new - A| over the box, Aalt = B_new inside the box and A's
+    values outside it; values mostly in the fixed-point range, a few outside
+    (planes on the FP64 unit).  Bit-exact against float64 on the CPU."""
+    import ctypes
+    import torch
+    L = g.runtime()
+    L.dvmhgb_jac3d_stnupd_items.restype = ctypes.c_long
+    n0, n1, n2 = 30, 45, 202
+    LA = ctypes.c_long * 3
+    lo_, hi_ = (3, 5, 7), (25, 38, 190)
+    st, ext, lo, hi = LA(n1 * n2, n2, 1), LA(n0, n1, n2), LA(*lo_), LA(*hi_)
+    gen = torch.Generator().manual_seed(500 + variant)
+    A = 0.25 + 0.5 * torch.rand(n0, n1, n2, dtype=torch.float64, generator=gen)
+    B = torch.rand(n0, n1, n2, dtype=torch.float64, generator=gen)
+    A[17, 20, 100], A[9, 30, 60], A[2, 10, 50] = -0.5, 3.0, 1.25  # outside the range
+    Ad, Bd = A.cuda(), B.cuda()
+    Aalt = torch.full_like(Ad, 7.0)
+    vp = lambda t: ctypes.c_void_p(t.data_ptr())
+    items = torch.empty(L.dvmhgb_jac3d_stnupd_items(lo, hi, variant), dtype=torch.float64, device="cuda")
+    sp = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    assert L.dvmhgb_jac3d_stnupd(vp(Ad), vp(Aalt), vp(Bd), st, ext, lo, hi, vp(items), variant, sp) == 0
+    torch.cuda.synchronize()
+    box = tuple(slice(a, b + 1) for a, b in zip(lo_, hi_))
+    inner = tuple(slice(a - 1, b) for a, b in zip(lo_, hi_))
+    s_ref, _ = _stencil_ref(A)
+    Bw = B.clone()
+    Bw[box] = s_ref[inner]
+    Aw = A.clone()
+    Aw[box] = s_ref[inner]
+    eps_ref = (s_ref[inner] - A[box]).abs().max().item()
+    assert torch.equal(Bd.cpu().view(torch.int64), Bw.view(torch.int64)), variant
+    assert torch.equal(Aalt.cpu().view(torch.int64), Aw.view(torch.int64)), variant
+    assert torch.equal(Ad.cpu(), A), variant  # the source is only read
+    assert items.max().item() == eps_ref, variant
 
 
 def _stencil_ref(A):

@@ -108,6 +108,7 @@ def test_variant_tuning_in_batched_mode_keeps_results_and_the_fastest(rt):
     n, steps, seed = 34, 2 * J3_FUSED + 10, 21
     e_ref, A_ref, B_ref = orc.jacobi_run(3, n, steps, seed)
     g.set_mode("batched")
+    g.set_deferral(False)  # each step's update and stencil meet: the pair of the fusion rule with its 34 variants
     rt.dvmhgb_tuner_reset()
     rt.dvmhgb_set_tuning(1)
     try:
@@ -121,6 +122,7 @@ def test_variant_tuning_in_batched_mode_keeps_results_and_the_fastest(rt):
     finally:
         rt.dvmhgb_set_tuning(0)
         rt.dvmhgb_tuner_reset()
+        g.set_deferral(True)
     assert np.array_equal(eps, e_ref) and np.array_equal(A, A_ref) and np.array_equal(B, B_ref)
     fused = ctypes.cast(g.workloads().loop_jac3d_fused_cuda, ctypes.c_void_p).value
     rec = [r for r in info if r["handler"] == fused]
@@ -147,6 +149,74 @@ def test_variant_model_prunes_the_search(rt):
     n, steps, seed = 34, 10, 22
     e_ref, A_ref, B_ref = orc.jacobi_run(3, n, steps, seed)
     g.set_mode("batched")
+    g.set_deferral(False)
+    rt.dvmhgb_tuner_reset()
+    rt.dvmhgb_set_tuning(2)
+    try:
+        j = g.Jacobi(3, n, seed)
+        eps = j.run(steps)
+        A, B = j.fetch()
+        j.close()
+        info = _variant_info(rt)
+    finally:
+        rt.dvmhgb_set_tuning(0)
+        rt.dvmhgb_tuner_reset()
+        g.set_deferral(True)
+    assert np.array_equal(eps, e_ref) and np.array_equal(A, A_ref) and np.array_equal(B, B_ref)
+    fused = ctypes.cast(g.workloads().loop_jac3d_fused_cuda, ctypes.c_void_p).value
+    r = [x for x in info if x["handler"] == fused][0]
+    tried = [v for v, b in enumerate(r["best"]) if b > 0]
+    assert r["explored"] == 6 and len(tried) == 3, r
+    assert r["chosen"] in tried and r["best"][r["chosen"]] == min(r["best"][v] for v in tried), r
+
+
+def test_variant_tuning_of_the_cross_step_pair(rt):
+    """Exhaustive variant tuning with deferral on: the pair is a step's stencil
+    with the next step's update (3 variants, each timed twice); results stay
+    bit-exact, the fastest is kept."""
+    from oracle import orc
+    _, g = ge.package()
+    n, steps, seed = 34, 12, 23
+    e_ref, A_ref, B_ref = orc.jacobi_run(3, n, steps, seed)
+    g.set_mode("batched")
+    rt.dvmhgb_tuner_reset()
+    rt.dvmhgb_set_tuning(1)
+    try:
+        j = g.Jacobi(3, n, seed)
+        eps = j.run(steps)
+        A, B = j.fetch()
+        j.close()
+        info = _variant_info(rt)
+    finally:
+        rt.dvmhgb_set_tuning(0)
+        rt.dvmhgb_tuner_reset()
+    assert np.array_equal(eps, e_ref) and np.array_equal(A, A_ref) and np.array_equal(B, B_ref)
+    pair = ctypes.cast(g.workloads().loop_jac3d_stnupd_cuda, ctypes.c_void_p).value
+    rec = [r for r in info if r["handler"] == pair]
+    assert len(rec) == 1, info
+    r = rec[0]
+    assert r["n"] == 3 and r["explored"] == 6 and all(b > 0 for b in r["best"]), r
+    assert r["chosen"] == int(np.argmin(r["best"])), r
+
+
+def test_model_guided_tuning_of_the_cross_step_pair(rt):
+    """Model-guided variant tuning with deferral on.  The cross-step pair's
+    handler is first asked for its variant inside a graph capture, where the
+    model cannot run; it gets the default there, the next flush runs uncaptured
+    and the model ranks the variants then (floor(0.1 * 3) = 0 tries: the
+    model's first choice).  Results bit-exact."""
+    from oracle import orc
+    _, g = ge.package()
+    P = rt.dvmhgb_mlp_nparams()
+    fp = ctypes.POINTER(ctypes.c_float)
+    rng = np.random.default_rng(5)
+    params = (0.05 * rng.standard_normal(P)).astype(np.float32)
+    mean, std = np.zeros(24, dtype=np.float32), np.ones(24, dtype=np.float32)
+    assert rt.dvmhgb_tuner_set_variant_model(params.ctypes.data_as(fp), mean.ctypes.data_as(fp),
+                                             std.ctypes.data_as(fp)) == 0
+    n, steps, seed = 34, 10, 24
+    e_ref, A_ref, B_ref = orc.jacobi_run(3, n, steps, seed)
+    g.set_mode("batched")
     rt.dvmhgb_tuner_reset()
     rt.dvmhgb_set_tuning(2)
     try:
@@ -159,8 +229,6 @@ def test_variant_model_prunes_the_search(rt):
         rt.dvmhgb_set_tuning(0)
         rt.dvmhgb_tuner_reset()
     assert np.array_equal(eps, e_ref) and np.array_equal(A, A_ref) and np.array_equal(B, B_ref)
-    fused = ctypes.cast(g.workloads().loop_jac3d_fused_cuda, ctypes.c_void_p).value
-    r = [x for x in info if x["handler"] == fused][0]
-    tried = [v for v, b in enumerate(r["best"]) if b > 0]
-    assert r["explored"] == 6 and len(tried) == 3, r
-    assert r["chosen"] in tried and r["best"][r["chosen"]] == min(r["best"][v] for v in tried), r
+    pair = ctypes.cast(g.workloads().loop_jac3d_stnupd_cuda, ctypes.c_void_p).value
+    rec = [r for r in info if r["handler"] == pair]
+    assert len(rec) == 1 and rec[0]["explored"] == 0 and 0 <= rec[0]["chosen"] < 3, info
