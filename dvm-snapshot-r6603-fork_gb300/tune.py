@@ -232,7 +232,9 @@ def _programs(g, seed):
 
 def _variant_runs(g, rt, mode, maker, size, steps_cap=200):
     """Tunes one program at one size in `mode`; returns the variant record of
-    the handler with the most variants (the program's main loop)."""
+    the program's main loop: the handler that ran the most tuned executions
+    (the steps run back to back, as the program runs them, so that a loop the
+    runtime defers to the next step meets it)."""
     rt.dvmhgb_tuner_reset()
     rt.dvmhgb_set_tuning(mode)
     w = maker(size)
@@ -241,7 +243,6 @@ def _variant_runs(g, rt, mode, maker, size, steps_cap=200):
         while steps < steps_cap:
             w.run(1)
             steps += 1
-            g.sync()
             if not rt.dvmhgb_tuner_exploring():
                 break
         w.run(2)  # the kept variant, as it then runs
@@ -262,11 +263,17 @@ def _variant_info(rt):
     for i in range(int(rt.dvmhgb_tuner_variant_count())):
         rt.dvmhgb_tuner_variant_info(ctypes.c_long(i), ctypes.byref(H), ctypes.byref(nv), ctypes.byref(ch), best, 64,
                                      ctypes.byref(ex), ctypes.byref(es))
-        rec = {"nvariants": nv.value, "chosen": ch.value, "best": [best[v] for v in range(nv.value)],
-               "explored": ex.value, "explore_seconds": es.value}
-        if out is None or rec["nvariants"] > out["nvariants"]:
-            out = rec
+        rec = {"handler": H.value, "nvariants": nv.value, "chosen": ch.value,
+               "best": [best[v] for v in range(nv.value)], "explored": ex.value, "explore_seconds": es.value}
+        out = (out or []) + [rec]
     return out
+
+
+def _main_record(recs, handler=None):
+    """The record of `handler`, or (None) of the handler whose exhaustive search took the longest."""
+    if handler is not None:
+        return next(r for r in recs if r["handler"] == handler)
+    return max(recs, key=lambda r: (r["explore_seconds"], r["nvariants"]))
 
 
 def configs_eval(g, seed=20261203, epochs=300, log=print):
@@ -316,8 +323,8 @@ def configs_eval(g, seed=20261203, epochs=300, log=print):
                        "vs model-guided (top floor(0.1 n) tried)", "train_rows": int(len(y)),
            "loss_first_last": [float(losses[0]), float(losses[-1])], "train_seconds": t_train}
     for name, (train, size, maker) in progs.items():
-        ex = _variant_runs(g, rt, 1, maker, size)
-        md = _variant_runs(g, rt, 2, maker, size)
+        ex = _main_record(_variant_runs(g, rt, 1, maker, size))
+        md = _main_record(_variant_runs(g, rt, 2, maker, size), ex["handler"])
         bests = np.array(ex["best"])
         vbest = int(np.argmin(np.where(bests >= 0, bests, np.inf)))
         pick = md["chosen"]

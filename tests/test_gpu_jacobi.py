@@ -202,6 +202,9 @@ def test_jacobi3d_stnupd_kernel_sub_box(g, variant):
     A = 0.25 + 0.5 * torch.rand(n0, n1, n2, dtype=torch.float64, generator=gen)
     B = torch.rand(n0, n1, n2, dtype=torch.float64, generator=gen)
     A[17, 20, 100], A[9, 30, 60], A[2, 10, 50] = -0.5, 3.0, 1.25  # outside the range
+    # in range, but the new B of cell (10, 20, 100) falls below it: 2^-9 / 6 (|B - A| on the FP64 unit)
+    A[9, 20, 100], A[11, 20, 100], A[10, 19, 100], A[10, 21, 100], A[10, 20, 99], A[10, 20, 101] = \
+        2.0 ** -9, 0.0, 0.0, 0.0, 0.0, 0.0
     Ad, Bd = A.cuda(), B.cuda()
     Aalt = torch.full_like(Ad, 7.0)
     vp = lambda t: ctypes.c_void_p(t.data_ptr())
