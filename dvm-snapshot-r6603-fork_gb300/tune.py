@@ -222,7 +222,7 @@ def run(rt, n_loops=2000, n_test=200, seed=20261207, reps=2, epochs=200, frac=0.
 def _programs(g, seed):
     """name -> (training sizes, configuration size, maker(size) -> object with run/close)."""
     return {
-        "jacobi2d_1024": ([642, 770, 898, 1154, 1282, 1538], 1024, lambda n: g.Jacobi(2, n, seed)),
+        "jacobi2d_1024": ([642, 770, 898, 962, 1090, 1154, 1282, 1538], 1024, lambda n: g.Jacobi(2, n, seed)),
         "jacobi3d_512": ([322, 386, 450, 578], 512, lambda n: g.Jacobi(3, n, seed)),
         "sor3d_384": ([258, 322, 354, 418, 450], 384, lambda n: g.Sor(n, 1.5, seed + 2)),
         "heat_256x2048": ([(128, 1024), (192, 1536), (320, 2048)], (256, 2048),
