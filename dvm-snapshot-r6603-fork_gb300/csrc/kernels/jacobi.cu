@@ -1104,7 +1104,7 @@ int launchT(const CUtensorMap &map, double *A, double *Out, const Box3 &b, const
         }
     }
     kStencil3T<0, NS, 4, W><<<g.grid, dim3(TX, TY), smem, s>>>(map, map, map, A, nullptr, Out, b, g.p0, g.ichunk,
-                                                               nullptr, dvmhgb_status_word(), nullptr);
+                                                               nullptr, dvmhgb_status_word(), nullptr, 0);
     return 0;
 }
 
@@ -1295,10 +1295,10 @@ int dvmhgb_jac3d_fused(double *A, const double *B, double *Bnew, const long st[3
         int *status = dvmhgb_status_word();
         if (native == V3_TF)
             kStencil3T<2, 5, 4, 0><<<g.grid, blk, tma::smemBytes(true, 5), s>>>(mapB, mapA, mapT, A, B, Bnew, b, g.p0,
-                                                                                g.ichunk, items, status, nullptr);
+                                                                                g.ichunk, items, status, nullptr, 0);
         else
             kStencil3T<2, 5, 3, 0><<<g.grid, blk, tma::smemBytes(true, 5), s>>>(mapB, mapA, mapT, A, B, Bnew, b, g.p0,
-                                                                                g.ichunk, items, status, nullptr);
+                                                                                g.ichunk, items, status, nullptr, 0);
         dvmhgb_count_launches(1);
         if (cudaGetLastError() != cudaSuccess) return -1;
         return dvmhgb_copy_outside_box(3, B, Bnew, st, ext, lo, hi, stream);
@@ -1363,15 +1363,18 @@ int dvmhgb_jac3d_stnupd(const double *A, double *Aalt, double *B, const long st[
     }
     int *status = dvmhgb_status_word();
     const dim3 blk(TX, TY);
-    if (variant == 0)
+    // (FP64-unit warps, warps with the integer-pipe |B - A|) of each variant
+    static const int wq[DVMHGB_JAC3D_STNUPD_VARIANTS][2] = {{0, 0}, {1, 0}, {2, 0}, {1, 2}, {1, 4}, {2, 3}};
+    const int w = wq[variant][0], qe = wq[variant][1];
+    if (w == 0)
         kStencil3T<3, 6, 4, 0><<<g.grid, blk, smem, s>>>(map, map, map, a, nullptr, B, b, g.p0, g.ichunk, items, status,
-                                                         Aalt);
-    else if (variant == 1)
+                                                         Aalt, qe);
+    else if (w == 1)
         kStencil3T<3, 6, 4, 1><<<g.grid, blk, smem, s>>>(map, map, map, a, nullptr, B, b, g.p0, g.ichunk, items, status,
-                                                         Aalt);
+                                                         Aalt, qe);
     else
         kStencil3T<3, 6, 4, 2><<<g.grid, blk, smem, s>>>(map, map, map, a, nullptr, B, b, g.p0, g.ichunk, items, status,
-                                                         Aalt);
+                                                         Aalt, qe);
     dvmhgb_count_launches(1);
     if (cudaGetLastError() != cudaSuccess) return -1;
     return dvmhgb_copy_outside_box(3, A, Aalt, st, ext, lo, hi, stream);  // A's cells outside the box carry over

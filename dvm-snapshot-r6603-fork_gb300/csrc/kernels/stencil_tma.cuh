@@ -142,12 +142,13 @@ __device__ __forceinline__ void copyBox(const CUtensorMap *map, uint32_t dst, ui
 // mapS: the stencil's source box copies (M = 0: A, else B); mapA (M >= 1):
 // A's box copies for planes outside the loop box; mapT (M = 2): A's own-cell
 // tiles.  items (M = 2, 3): one MAX partial per CTA; Out2 (M = 3): A's second
-// buffer.
+// buffer; qe (M = 3): the first qe warps take the update's |B - A| on the
+// integer pipe (exact q61 differences), the others on the FP64 unit.
 template <int M, int NS, int MINB, int W>
 __global__ void __launch_bounds__(TX *TY, MINB)
     kStencil3T(const __grid_constant__ CUtensorMap mapS, const __grid_constant__ CUtensorMap mapA,
                const __grid_constant__ CUtensorMap mapT, double *A, const double *__restrict__ B, double *Out, Box3 b,
-               long p0, int ichunk, double *items, int *status, double *Out2) {
+               long p0, int ichunk, double *items, int *status, double *Out2, int qe) {
     static_assert(NS >= 4, "the ring holds planes i - 1, i, i + 1 and the slot being refilled");
     static_assert(M >= 0 && M <= 3 && M != 1, "modes 0, 2 and 3");
     constexpr bool S = M == 2, U = M == 2;  // source A_new; the update loop too
@@ -231,8 +232,9 @@ __global__ void __launch_bounds__(TX *TY, MINB)
     const bool ownUpd = U && jI && (kI0 || kI1);
     const int tilePair = ty * TX + lane;
     double *ownA = A + j * b.s1 + k;
-    uint64_t mb = 0;  // fused eps: Max(|B - A|) as a bit pattern
-    bool seen = false;
+    uint64_t mb = 0;    // the update's eps: Max(|B - A|) as a bit pattern (FP64-unit differences)
+    uint64_t qmax = 0;  // M = 3: the largest exact q61 difference (warps below qe)
+    bool seen = false, qdone = false;
 
     // wait for plane q (in step q - 2), [fused: do the update of the own pair,
     // replace the elements outside the box], convert it to q61 (in place, or
@@ -343,6 +345,16 @@ __global__ void __launch_bounds__(TX *TY, MINB)
             // (((((A[i-1] + A[j-1]) + A[k-1]) + A[k+1]) + A[j+1]) + A[i+1]) / 6, left to right
             v0 = sf::q61_div6(add(add(add(add(add(im.x, up.x), left), own.y), dn.x), ip.x));
             v1 = sf::q61_div6(add(add(add(add(add(im.y, up.y), own.x), right), dn.y), ip.y));
+            if (E && jI && ty < qe) {
+                // the next update's |B - A| as an exact difference of q61 values (A's are the plane's own, B's
+                // converted; RN of the largest, once, at the end); a B below the range goes to the FP64 unit
+                const bool ok0 = sf::q61_ok(v0), ok1 = sf::q61_ok(v1);
+                const uint64_t b0 = sf::q61(v0), b1 = sf::q61(v1);
+                const uint64_t d0 = b0 > own.x ? b0 - own.x : own.x - b0, d1 = b1 > own.y ? b1 - own.y : own.y - b1;
+                if (kI0 && ok0 && d0 > qmax) qmax = d0;
+                if (kI1 && ok1 && d1 > qmax) qmax = d1;
+                qdone = ok0 && ok1;
+            }
         } else {  // rare: a value outside the fixed-point range near this plane
             v0 = (jI && kI0) ? nativeCell(i, k) : 0.0;
             v1 = (jI && kI1) ? nativeCell(i, k + 1) : 0.0;
@@ -352,10 +364,13 @@ __global__ void __launch_bounds__(TX *TY, MINB)
             else if (kI0) out[0] = v0;
             else if (kI1) out[1] = v1;
         }
-        if (E && jI) {  // the next update: eps = Max(|B - A|, eps) with A's doubles of the slot; A = B into A's second buffer
+        if (E && jI && !qdone) {  // the next update: eps = Max(|B - A|, eps) on the FP64 unit, A's doubles of the slot
             const double2 a = *reinterpret_cast<const double2 *>(reinterpret_cast<const double *>(slotOf(t + 1)) + r0);
             if (kI0) mb = sf::absmax_bits(sf::nadd(v0, -a.x), mb);
             if (kI1) mb = sf::absmax_bits(sf::nadd(v1, -a.y), mb);
+        }
+        qdone = false;
+        if (E && jI) {  // A = B into A's second buffer
             seen = seen || kI0 || kI1;
             double *o2 = out2 + (out - outBase);
             if (kI0 && kI1) st2cs(o2, make_double2(v0, v1));
@@ -365,7 +380,9 @@ __global__ void __launch_bounds__(TX *TY, MINB)
         out += b.s0;
     }
     if (U || E) {
-        double m = seen ? sf::from(mb) : -__builtin_huge_val();
+        // RN(max |b - a|) of the q61 differences (RN is monotone: the largest, rounded once), with the FP64 part
+        const double qd = __ull2double_rn(qmax) * 0x1p-61, f = sf::from(mb);
+        double m = seen ? (qd > f ? qd : f) : -__builtin_huge_val();
         m = ctaMax(m, shr);
         if (tid == 0) items[blockIdx.x + gridDim.x * ((long)blockIdx.y + (long)gridDim.y * blockIdx.z)] = m;
     }

@@ -26,7 +26,7 @@
 // 1.66, the update and the TMA stencil running at the same time 1.66, the register-staged one-pass pair 2.01)
 #define DEF_FUSED 25
 // a step's stencil with the next step's update in one pass (the pairing the runtime forms across steps)
-#define DEF_STNUPD 1
+#define DEF_STNUPD 5  // 2 FP64-unit warps, 3 warps with the integer-pipe |B - A| (1.092 against 1.130 ms for variant 1, same box)
 
 namespace {
 
@@ -60,12 +60,13 @@ const float *variantDesc(int handler) {
     static float su[DVMHGB_JAC3D_STNUPD_VARIANTS * NDESC];
     static bool ready = false;
     if (!ready) {
+        static const int wq[DVMHGB_JAC3D_STNUPD_VARIANTS][2] = {{0, 0}, {1, 0}, {2, 0}, {1, 2}, {1, 4}, {2, 3}};
         for (int v = 0; v < DVMHGB_JAC3D_STNUPD_VARIANTS; v++) {  // handler 4: stencil then the next update, one pass
             float *d = su + v * NDESC;
             d[0] = 1, d[1] = 4;
             stencilDesc(V_T, d);
-            d[6] = (float)v / 8.0f;  // warps on the FP64 unit
-            d[7] = 0;
+            d[6] = (float)wq[v][0] / 8.0f;  // warps on the FP64 unit
+            d[7] = (float)wq[v][1] / 8.0f;  // warps with the integer-pipe |B - A|
         }
         for (int v = 0; v < 3; v++) upd[v * NDESC] = 1, upd[v * NDESC + 1] = 1, upd[v * NDESC + 2] = (float)v;
         for (int v = 0; v < DVMHGB_JAC3D_VARIANTS; v++) {

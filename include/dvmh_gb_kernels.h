@@ -83,10 +83,12 @@ long dvmhgb_jac3d_fused_items(const long lo[3], const long hi[3], int native);
  * the new A into Aalt (a second buffer of A's layout, to become A: A is still
  * read while the pass runs; A's cells outside the box are copied over), MAX
  * partials into items (dvmhgb_jac3d_stnupd_items).  24 bytes a cell.  The
- * TMA-staged fixed-point stencil, variant = its warps on the FP64 unit (0, 1,
- * 2 of 8).  The runtime pairs the loops so when a program's time steps leave
+ * TMA-staged fixed-point stencil; variants (warps of 8 on the FP64 unit, warps
+ * taking |B - A| as exact fixed-point differences on the integer pipe, the
+ * rest on the FP64 unit): 0 (0, 0), 1 (1, 0), 2 (2, 0), 3 (1, 2), 4 (1, 4),
+ * 5 (2, 3).  The runtime pairs the loops so when a program's time steps leave
  * the stencil queued past the step's end (deferred loops, dvmh_gb.h). */
-#define DVMHGB_JAC3D_STNUPD_VARIANTS 3
+#define DVMHGB_JAC3D_STNUPD_VARIANTS 6
 long dvmhgb_jac3d_stnupd_items(const long lo[3], const long hi[3], int variant);
 int dvmhgb_jac3d_stnupd(const double *A, double *Aalt, double *B, const long st[3], const long ext[3],
                         const long lo[3], const long hi[3], double *items, int variant, void *stream);

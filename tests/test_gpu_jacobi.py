@@ -5,7 +5,7 @@ import pytest
 
 import __graft_entry__ as ge
 from oracle import orc
-from tests.util import J3_FUSED, J3_IN_PLACE, J3_ONE_PASS_Q, J3_STENCILS, sha, unhex
+from tests.util import J3_FUSED, J3_IN_PLACE, J3_ONE_PASS_Q, J3_STENCILS, J3_STNUPD, sha, unhex
 
 pytestmark = pytest.mark.gpu
 
@@ -156,7 +156,7 @@ def test_jacobi3d_variants_vs_oracle(g, variant):
         g.set_deferral(True)
 
 
-@pytest.mark.parametrize("variant", [-1, 0, 1, 2])
+@pytest.mark.parametrize("variant", [-1] + list(range(J3_STNUPD)))
 def test_jacobi3d_stencil_then_next_update(g, variant):
     """Batched mode with deferral (the default): each step's stencil, naming
     arrays only, waits past its region for the next step's update loop, and the
@@ -183,7 +183,7 @@ def test_jacobi3d_stencil_then_next_update(g, variant):
         g.force_variant(-1)
 
 
-@pytest.mark.parametrize("variant", [0, 1, 2])
+@pytest.mark.parametrize("variant", list(range(J3_STNUPD)))
 def test_jacobi3d_stnupd_kernel_sub_box(g, variant):
     """dvmhgb_jac3d_stnupd through the C ABI over a box with array cells
     outside it on every side: B = stencil(A) inside the box (outside untouched),

@@ -11,7 +11,7 @@ import pytest
 
 import __graft_entry__ as ge
 from oracle import mlp_ref
-from tests.util import J3_FUSED
+from tests.util import J3_FUSED, J3_STNUPD
 
 pytestmark = pytest.mark.gpu
 
@@ -172,11 +172,11 @@ def test_variant_model_prunes_the_search(rt):
 
 def test_variant_tuning_of_the_cross_step_pair(rt):
     """Exhaustive variant tuning with deferral on: the pair is a step's stencil
-    with the next step's update (3 variants, each timed twice); results stay
+    with the next step's update (its variants each timed twice); results stay
     bit-exact, the fastest is kept."""
     from oracle import orc
     _, g = ge.package()
-    n, steps, seed = 34, 12, 23
+    n, steps, seed = 34, 2 * J3_STNUPD + 6, 23
     e_ref, A_ref, B_ref = orc.jacobi_run(3, n, steps, seed)
     g.set_mode("batched")
     rt.dvmhgb_tuner_reset()
@@ -195,7 +195,7 @@ def test_variant_tuning_of_the_cross_step_pair(rt):
     rec = [r for r in info if r["handler"] == pair]
     assert len(rec) == 1, info
     r = rec[0]
-    assert r["n"] == 3 and r["explored"] == 6 and all(b > 0 for b in r["best"]), r
+    assert r["n"] == J3_STNUPD and r["explored"] == 2 * J3_STNUPD and all(b > 0 for b in r["best"]), r
     assert r["chosen"] == int(np.argmin(r["best"])), r
 
 
@@ -203,7 +203,7 @@ def test_model_guided_tuning_of_the_cross_step_pair(rt):
     """Model-guided variant tuning with deferral on.  The cross-step pair's
     handler is first asked for its variant inside a graph capture, where the
     model cannot run; it gets the default there, the next flush runs uncaptured
-    and the model ranks the variants then (floor(0.1 * 3) = 0 tries: the
+    and the model ranks the variants then (floor(0.1 * 6) = 0 tries: the
     model's first choice).  Results bit-exact."""
     from oracle import orc
     _, g = ge.package()
@@ -231,4 +231,4 @@ def test_model_guided_tuning_of_the_cross_step_pair(rt):
     assert np.array_equal(eps, e_ref) and np.array_equal(A, A_ref) and np.array_equal(B, B_ref)
     pair = ctypes.cast(g.workloads().loop_jac3d_stnupd_cuda, ctypes.c_void_p).value
     rec = [r for r in info if r["handler"] == pair]
-    assert len(rec) == 1 and rec[0]["explored"] == 0 and 0 <= rec[0]["chosen"] < 3, info
+    assert len(rec) == 1 and rec[0]["explored"] == 0 and 0 <= rec[0]["chosen"] < J3_STNUPD, info

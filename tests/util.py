@@ -35,3 +35,4 @@ J3_FUSED = J3["DVMHGB_JAC3D_FUSED_VARIANTS"]   # variants of the fused pair
 J3_IN_PLACE = (J3["DVMHGB_JAC3D_UNFUSED"], J3["DVMHGB_JAC3D_OVERLAP"], J3["DVMHGB_JAC3D_OVERLAP_Q"])
 J3_ONE_PASS_Q = [J3["DVMHGB_JAC3D_FUSED_Q"], J3["DVMHGB_JAC3D_FUSED_Q"] + 1,
                  J3["DVMHGB_JAC3D_FUSED_T"], J3["DVMHGB_JAC3D_FUSED_T"] + 1]
+J3_STNUPD = J3["DVMHGB_JAC3D_STNUPD_VARIANTS"]  # variants of the cross-step pass
