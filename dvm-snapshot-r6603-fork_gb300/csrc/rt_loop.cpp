@@ -505,10 +505,16 @@ static const Var *paramVar(const void *p) {
     return regularVarOfHeader(p);
 }
 
+// v == nullptr: any parameter that is not an array descriptor counts -- a
+// registered variable or not (an unregistered address could die with its
+// region just the same)
 static bool loopNamesVar(const Loop *l, const Var *v) {
     for (int i = 0; i < l->cuda.nparams; i++) {
-        const Var *pv = paramVar(l->cuda.params[i]);
-        if (pv && (v == nullptr || pv == v)) return true;
+        if (v == nullptr) {
+            if (!isArrayDesc(l->cuda.params[i])) return true;
+            continue;
+        }
+        if (paramVar(l->cuda.params[i]) == v) return true;
     }
     for (auto &r : l->reds)
         if ((r.var && (v == nullptr || r.var == v)) || (r.locVar && (v == nullptr || r.locVar == v))) return true;

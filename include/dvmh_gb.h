@@ -43,7 +43,8 @@ void dvmhgb_sync(void);    /* flush and wait for the GPU */
 void dvmhgb_register_fusion(DvmHandlerFunc first, DvmHandlerFunc second, DvmHandlerFunc fused);
 void dvmhgb_register_batch(DvmHandlerFunc single, DvmHandlerFunc batched);
 /* Deferred loops.  In batched mode a queued loop whose handler starts a fusion
- * rule, and whose parameters name arrays only (no variable), need not run when
+ * rule, and whose parameters are all array descriptors (no variable, no other
+ * address, no reduction), need not run when
  * a variable is read or written on the host or when its region ends: it waits
  * in the queue for the next loop, so that a time step's last loop and the next
  * step's first loop can meet in one flush (the region's end no longer forces
