@@ -183,6 +183,36 @@ def test_jacobi3d_stencil_then_next_update(g, variant):
         g.force_variant(-1)
 
 
+def test_deferred_stencil_meets_other_programs(g):
+    """Batched mode with deferral, the 3-D and 2-D Jacobi programs stepping in
+    turn: the 3-D step's stencil waits in the queue, the 2-D step's loops
+    (which start no deferrable rule) come after it and its region's end runs
+    the queue through them, so the 3-D stencil runs alone there and the next
+    3-D update runs alone too.  Every eps and the final arrays of both
+    programs bit-exact against the oracle; then a mode change and the arrays'
+    fetch run whatever is still queued."""
+    e3, A3, B3 = orc.jacobi_run(3, 40, 4, 71)
+    e2, A2, B2 = orc.jacobi_run(2, 70, 4, 72)
+    g.set_mode("batched")
+    j3 = g.Jacobi(3, 40, 71)
+    j2 = g.Jacobi(2, 70, 72)
+    got3, got2 = [], []
+    try:
+        for _ in range(4):
+            got3.append(j3.run(1)[0])
+            got2.append(j2.run(1)[0])
+        g.set_mode("async")  # a mode change runs the 3-D stencil still queued
+        g.set_mode("batched")
+        A, B = j3.fetch()
+        a, b = j2.fetch()
+    finally:
+        j3.close()
+        j2.close()
+    assert np.array_equal(np.array(got3), e3) and np.array_equal(np.array(got2), e2)
+    assert np.array_equal(A, A3) and np.array_equal(B, B3)
+    assert np.array_equal(a, A2) and np.array_equal(b, B2)
+
+
 @pytest.mark.parametrize("variant", list(range(J3_STNUPD)))
 def test_jacobi3d_stnupd_kernel_sub_box(g, variant):
     """dvmhgb_jac3d_stnupd through the C ABI over a box with array cells
