@@ -318,8 +318,12 @@ bool geo(const long st[3], const long ext[3], const long lo[3], const long hi[3]
     return true;
 }
 
-// variant -> TK: 0 -> 32, 1 -> 16, 2 -> 8; 3: streaming columns (items as for TK = 64: one per 64-wide chunk)
-int tkOf(int variant) { return variant == 0 ? 32 : (variant == 1 ? 16 : (variant == 2 ? 8 : (variant == 3 ? 64 : 0))); }
+// variant -> TK: 0 -> 32, 1 -> 16, 2 -> 8; 3: streaming columns (items as for TK = 64: one per 64-wide chunk);
+// 4: hyperplane tiles of G = 8 hyperplanes (items as for TK = 8)
+int tkOf(int variant) {
+    static const int tk[5] = {32, 16, 8, 64, 8};
+    return variant >= 0 && variant < 5 ? tk[variant] : 0;
+}
 
 template <int TK>
 int sweepT(double *A, const Geo &g, const double *wDev, double *items, void *scratch, int *status, Bound bound,
@@ -561,6 +565,376 @@ int sweepStream(double *A, const Geo &g0, const double *wDev, double *items, voi
     return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }
 
+// ---------------------------------------------------------------- hyperplane tiles (variant 4)
+//
+// The tiles above are boxes: inside one, lane (li, lj) starts li + lj steps
+// late, so a 4 x 8 x TK tile takes TK + 10 steps for TK positions per lane, and
+// on GB300 an FP64 warp instruction costs the same whatever its active lanes.
+// Here a tile is cut along hyperplanes instead.  With (ri, rj, rk) the cell's
+// offsets from the loop box's low corner and h = ri + rj + rk its hyperplane,
+// tile (a, b, c) holds rows ri = 4a .. 4a + 3, rj = 8b .. 8b + 7 and the cells
+// of those rows with h in [G c, G c + G).  Lane (li, lj) takes, at step t, the
+// cell of its row on hyperplane G c + t: every lane is busy at every step
+// (except where a row's window leaves the loop box), and the step order is the
+// skewed order of the box tiles, so every cell sees exactly the values the
+// sequential loop gives it.  A cell (ri, rj, rk) on hyperplane h reads the new
+// values of (ri-1, rj, rk), (ri, rj-1, rk), (ri, rj, rk-1), all on h - 1: so
+// tile (a, b, c) depends on (a-1, b, c), (a-1, b, c-1), (a, b-1, c),
+// (a, b-1, c-1) and (a, b, c-1), all on plane a + b + c - 1 or lower.  Column
+// (a, b) holds the tiles c = cmin .. cmax that meet the loop box; a small
+// kernel lists them plane by plane (a + b + c, then c, then a) before the sweep,
+// and the sweep hands them out in that order (topological: progress as above).
+//
+// Shared memory holds, per row of the tile and of its four face neighbours, a
+// window of the row's positions h - ri - rj - 1 .. for h = G c - 1 .. G c + G:
+// position p of the window is hyperplane G c - 1 + p of the row.  Row i - 1 is
+// read at p = t, row i + 1 at p = t + 2 (the same for j), the row itself at
+// t, t + 1, t + 2.
+//
+// Residual: the canonical tree wants, per row, the pairwise sum of every
+// G-position part of the array index k (parts aligned to multiples of G,
+// positions outside the loop -0.0).  A lane's window [k0, k0 + G) covers the
+// tail of one part and the head of the next; the offset dl = k0 mod G is the
+// same for every window of the row.  Each step keeps nv - old; the lane stores
+// the differences of its last dl positions (the next part's head) for the
+// row's next window before the tile releases its successors -- tile (a, b,
+// c + 1) waits for this tile anyway and loads them with its -1 faces -- and,
+// after the release, squares the carried and its own differences into the
+// part it closes.  The first window of a row writes -0.0 for the parts before
+// it, the last one closes the next part and writes -0.0 for the rest.
+
+template <int G>
+struct Hyp {
+    static constexpr int SKP = G + 3;                  // window: positions 0 .. G + 1 (odd stride: banks)
+    static constexpr int BOX = SI * SJ * SKP;
+    static constexpr int SQS = 2 * G + 1;              // leaves of two parts per lane (padded)
+    static constexpr int WSM = BOX + 32 * SQS;         // doubles of shared memory per warp
+    static constexpr size_t SMEM = sizeof(double) * WSM * WPB;
+    static constexpr int PARTS = 64 / G;
+    static constexpr int LOG = G == 16 ? 4 : 3;
+};
+
+struct HGeo {
+    long s0, s1;
+    long e0, e1, e2;
+    long lo0, lo1, lo2, hi0, hi1, hi2;
+    long na, nb, nk;
+    long ncg;         // tiles of the longest column: c < ncg
+    long nj;          // rows per i in the item layout
+    long kc0, nparts; // first part (of the whole array's k) with items; items per row
+    long ntiles, nlev;
+    long rows;        // rows of the loop box: (hi0 - lo0 + 1) * nj
+};
+
+template <int G>
+__host__ __device__ __forceinline__ long hypCmin(long a, long b) {
+    return (TI * a + TJ * b) / G;
+}
+template <int G>
+__host__ __device__ __forceinline__ long hypCmax(long a, long b, long nk) {
+    return (TI * a + TJ * b + TI + TJ - 2 + nk - 1) / G;
+}
+
+__device__ __forceinline__ unsigned long long hypPack(long a, long b, long c) {
+    return ((unsigned long long)a << 42) | ((unsigned long long)b << 21) | (unsigned long long)c;
+}
+
+// One CTA per plane d: the plane's first index (tiles on planes < d, summed
+// over the columns in closed form) and its tiles in the order (c, then a).
+template <int G>
+__global__ void __launch_bounds__(256) kHypTable(HGeo g, unsigned long long *table) {
+    __shared__ long long part[8];
+    __shared__ int wsum[8];
+    const long d = blockIdx.x;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    long long before = 0;
+    for (long q = tid; q < g.na * g.nb; q += 256) {
+        const long a = q / g.nb, b = q % g.nb, c0 = hypCmin<G>(a, b), cnt = hypCmax<G>(a, b, g.nk) - c0 + 1;
+        const long x = d - a - b - c0;
+        before += x <= 0 ? 0 : (x < cnt ? x : cnt);
+    }
+#pragma unroll
+    for (int o = 16; o; o >>= 1) before += __shfl_xor_sync(0xffffffffu, before, o);
+    if (lane == 0) part[warp] = before;
+    __syncthreads();
+    long long pos = 0;
+    for (int w = 0; w < 8; w++) pos += part[w];
+    // s = a + b from high to low (c = d - s ascending), a ascending inside
+    const long smax = g.na + g.nb - 2 < d ? g.na + g.nb - 2 : d;
+    for (long s = smax; s >= 0; s--) {
+        const long amin = s - (g.nb - 1) > 0 ? s - (g.nb - 1) : 0, amax = s < g.na - 1 ? s : g.na - 1;
+        for (long a0 = amin; a0 <= amax; a0 += 256) {
+            const long a = a0 + tid, b = s - a, c = d - s;
+            const bool in = a <= amax && c >= hypCmin<G>(a, b) && c <= hypCmax<G>(a, b, g.nk);
+            const unsigned m = __ballot_sync(0xffffffffu, in);
+            if (lane == 0) wsum[warp] = __popc(m);
+            __syncthreads();
+            int off = 0, tot = 0;
+            for (int w = 0; w < 8; w++) {
+                off += w < warp ? wsum[w] : 0;
+                tot += wsum[w];
+            }
+            if (in) table[pos + off + __popc(m & ((1u << lane) - 1u))] = hypPack(a, b, c);
+            pos += tot;
+            __syncthreads();  // wsum is rewritten by the next round
+        }
+    }
+}
+
+// bounded wait for *f >= want by one lane; false once the limit ran out (status written, counter stopped)
+__device__ __forceinline__ bool hypWait(const int *f, int want, int *status, unsigned *counter, long limit) {
+    long n = 0;
+    while (ldAcquire(f) < want) {
+        if (++n > limit) {
+            atomicExch(status, ERR_SOR_TIMEOUT);
+            atomicOr(counter, 0x80000000u);  // no warp takes another tile
+            return false;
+        }
+        __nanosleep(64);
+    }
+    return true;
+}
+
+__device__ __forceinline__ double ldH(const double *A, const HGeo &g, long i, long j, long k) {
+    return (i >= 0 && i < g.e0 && j >= 0 && j < g.e1 && k >= 0 && k < g.e2) ? __ldcg(A + i * g.s0 + j * g.s1 + k)
+                                                                             : 0.0;
+}
+
+// pairwise tree over the G leaves of the part starting at array index k = kf: leaf p is d[p]^2 where
+// k = kf + p lies in the loop, -0.0 elsewhere (every lane at the same leaf: warp-uniform)
+template <int G>
+__device__ __forceinline__ double hypTree(const double *d, long kf, long lo2, long hi2) {
+    double stk[Hyp<G>::LOG], v = 0.0;
+#pragma unroll
+    for (int p = 0; p < G; p++) {
+        v = kf + p >= lo2 && kf + p <= hi2 ? d[p] * d[p] : -0.0;
+#pragma unroll
+        for (int l = 0; l < Hyp<G>::LOG; l++) {
+            if (!((p >> l) & 1)) {
+                stk[l] = v;
+                break;
+            }
+            v = stk[l] + v;
+        }
+    }
+    return v;
+}
+
+template <int G>
+__global__ void __launch_bounds__(NT) kSorHyp(double *A, HGeo g, const double *wPtr, int *flags, unsigned *counter,
+                                              const unsigned long long *table, double *carry, double *items,
+                                              int *status, Bound bound) {
+    using H = Hyp<G>;
+    constexpr int SKP = H::SKP, RS = SJ * SKP;  // RS: one step of i in the window box
+    extern __shared__ double sm[];              // per warp: box [SI][SJ][SKP], then leaves [32][SQS]
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, li = lane / TJ, lj = lane % TJ;
+    double *box = sm + (size_t)H::WSM * warp;
+    double *sq = box + H::BOX + lane * H::SQS;
+    const double w = *wPtr;
+    const double c1 = 1.0 - w, c2 = w / 6.0;  // loop invariants, rounded as in the source expression
+    const int nk = (int)g.nk;
+    while (true) {
+        long idx = 0;
+        if (lane == 0) idx = (long)atomicAdd(counter, 1u) + bound.firstIndex;  // >= 2^31 once a warp has failed
+        idx = __shfl_sync(0xffffffffu, idx, 0);
+        if (idx >= g.ntiles) break;
+        const unsigned long long tv = table[idx];
+        const long a = (long)(tv >> 42), b = (long)((tv >> 21) & 0x1fffff), c = (long)(tv & 0x1fffff);
+        const long ra = TI * a, rb = TJ * b, hc = G * c;  // hc: the tile's first hyperplane
+        // 1. before the wait: rows qi 1..5, qj 1..9 (own rows and the +i / +j faces), positions 1 .. G+1 --
+        //    old values that no tile writes before this one is done
+        {
+            constexpr int NV = (SI - 1) * (SJ - 1) * (G + 1), NL = (NV + 31) / 32;
+            double v[NL];
+#pragma unroll
+            for (int u = 0; u < NL; u++) {
+                const int q = u * 32 + lane, r = q / (G + 1), p = 1 + q % (G + 1);
+                const int qi = 1 + r / (SJ - 1), qj = 1 + r % (SJ - 1);
+                const long ri = ra - 1 + qi, rj = rb - 1 + qj;
+                v[u] = q < NV ? ldH(A, g, g.lo0 + ri, g.lo1 + rj, g.lo2 + hc - ri - rj - 1 + p) : 0.0;
+            }
+#pragma unroll
+            for (int u = 0; u < NL; u++) {
+                const int q = u * 32 + lane, r = q / (G + 1), p = 1 + q % (G + 1);
+                const int qi = 1 + r / (SJ - 1), qj = 1 + r % (SJ - 1);
+                if (q < NV) box[(qi * SJ + qj) * SKP + p] = v[u];
+            }
+        }
+        // 2. wait for the five predecessors (bounded)
+        int fail = 0;
+        if (lane < 5) {
+            // lanes 0..4: (a-1,b,c), (a-1,b,c-1), (a,b-1,c), (a,b-1,c-1), (a,b,c-1)
+            const long pa = a - (lane < 2), pb = b - (lane == 2 || lane == 3),
+                       pc = c - (lane == 1 || lane == 3 || lane == 4);
+            if (pa >= 0 && pb >= 0 && pc >= hypCmin<G>(pa, pb) && pc <= hypCmax<G>(pa, pb, g.nk) &&
+                !hypWait(flags + (pa * g.nb + pb) * g.ncg + pc, 1, status, counter, bound.pollLimit))
+                fail = 1;
+        }
+        if (__any_sync(0xffffffffu, fail)) return;
+        __syncwarp();  // orders the acquiring lanes' loads before every lane's face loads
+        const long ri = ra + li, rj = rb + lj, i = g.lo0 + ri, j = g.lo1 + rj;
+        const bool row = i <= g.hi0 && j <= g.hi1;
+        const int rk0 = (int)(hc - ri - rj);                // the row's rk at step 0
+        const long k0 = g.lo2 + rk0;                          // ... and its array index k
+        const long m = (k0 + 4 * G) / G * G - 4 * G;          // floor to a part boundary (k0 > -3G)
+        const int dl = (int)(k0 - m);                         // positions of the part before the window
+        const long rowIdx = row ? (i - g.lo0) * g.nj + (j - g.lo1) : 0;
+        const bool first = c == hypCmin<G>(a, b);
+        const bool res = row && k0 <= g.hi2;                  // the row has a part to close here
+        // 3. the -i face rows (0, 1..8) and -j face rows (1..4, 0) at positions 0 .. G-1, the own rows at 0,
+        //    and the differences the row's previous window carried over (its last dl positions)
+        double cin[G - 1];
+        {
+            constexpr int NV = (TI + TJ) * G, NL = (NV + 31) / 32;
+            double v[NL];
+#pragma unroll
+            for (int u = 0; u < NL; u++) {
+                const int q = u * 32 + lane, r = q / G, p = q % G;
+                const int qi = r < TJ ? 0 : r - TJ + 1, qj = r < TJ ? r + 1 : 0;
+                const long fi = ra - 1 + qi, fj = rb - 1 + qj;
+                v[u] = q < NV ? ldH(A, g, g.lo0 + fi, g.lo1 + fj, g.lo2 + hc - fi - fj - 1 + p) : 0.0;
+            }
+            const double k0v = ldH(A, g, i, j, k0 - 1);
+#pragma unroll
+            for (int q = 0; q < G - 1; q++)
+                cin[q] = res && !first && q < dl ? __ldcg(carry + q * g.rows + rowIdx) : 0.0;
+#pragma unroll
+            for (int u = 0; u < NL; u++) {
+                const int q = u * 32 + lane, r = q / G, p = q % G;
+                const int qi = r < TJ ? 0 : r - TJ + 1, qj = r < TJ ? r + 1 : 0;
+                if (q < NV) box[(qi * SJ + qj) * SKP + p] = v[u];
+            }
+            box[((li + 1) * SJ + lj + 1) * SKP] = k0v;
+        }
+        __syncwarp();
+        double *x = box + ((li + 1) * SJ + (lj + 1)) * SKP + 1;  // x[t]: position t + 1
+        double dv[G];                                              // nv - old of each step
+        // 4. the dependent chain: G steps, every lane on its own row
+#pragma unroll
+        for (int t = 0; t < G; t++) {
+            const int rk = rk0 + t;
+            dv[t] = 0.0;
+            if (row && rk >= 0 && rk < nk) {
+                const double old = x[t];
+                // A[i-1] + A[i+1] + A[j-1] + A[j+1] + A[k-1] + A[k+1], left to right
+                const double s = ((((x[t - RS - 1] + x[t + RS + 1]) + x[t - SKP - 1]) + x[t + SKP + 1]) + x[t - 1]) +
+                                 x[t + 1];
+                const double nv = c1 * old + c2 * s;
+                x[t] = nv;
+                dv[t] = nv - old;
+            }
+            __syncwarp();
+        }
+        // 5. store the tile's cells (row r of the tile at positions 1 .. G) and the differences of the row's
+        //    last dl positions, which the row's next window needs; then release the successors
+#pragma unroll
+        for (int u = 0; u < G; u++) {
+            const int q = u * 32 + lane, r = q / G, p = 1 + q % G, qi = r / TJ, qj = r % TJ;
+            const long ii = ra + qi, jj = rb + qj, rk = hc - ii - jj + p - 1;
+            if (g.lo0 + ii <= g.hi0 && g.lo1 + jj <= g.hi1 && rk >= 0 && rk < nk)
+                A[(g.lo0 + ii) * g.s0 + (g.lo1 + jj) * g.s1 + g.lo2 + rk] = box[((qi + 1) * SJ + qj + 1) * SKP + p];
+        }
+#pragma unroll
+        for (int t = 1; t < G; t++)  // position t is leaf t - G + dl of the next part
+            if (res && t - G + dl >= 0) carry[(t - G + dl) * g.rows + rowIdx] = dv[t];
+        __threadfence();
+        __syncwarp();
+        if (lane == 0) stRelease(flags + (a * g.nb + b) * g.ncg + c, 1);
+        // 6. the residual, off the chain: the leaves of the part [m, m + G) are the carried differences, then
+        //    this window's; squared where k lies in the loop, -0.0 elsewhere
+        if (res) {
+#pragma unroll
+            for (int q = 0; q < G - 1; q++)
+                if (q < dl) sq[q] = cin[q];
+#pragma unroll
+            for (int t = 0; t < G; t++) sq[dl + t] = dv[t];
+            const long P = m / G - g.kc0;  // m / G: exact, m is a multiple of G (possibly negative)
+            double *it = items + rowIdx * g.nparts;
+            if (first)
+                for (long q = 0; q < P && q < g.nparts; q++) it[q] = -0.0;
+            if (P >= 0 && P < g.nparts) it[P] = hypTree<G>(sq, m, g.lo2, g.hi2);
+            if (k0 + G - 1 >= g.hi2) {  // the row ends in this window: the next part, then -0.0 to the end
+                if (P + 1 >= 0 && P + 1 < g.nparts) it[P + 1] = hypTree<G>(sq + G, m + G, g.lo2, g.hi2);
+                for (long q = P + 2 > 0 ? P + 2 : 0; q < g.nparts; q++) it[q] = -0.0;
+            }
+        }
+        __syncwarp();  // the box and the leaves are reused by this warp's next tile
+    }
+}
+
+template <int G>
+bool hypGeo(const long st[3], const long ext[3], const long lo[3], const long hi[3], HGeo &g) {
+    if (hi[0] < lo[0] || hi[1] < lo[1] || hi[2] < lo[2] || lo[0] < 0 || lo[1] < 0 || lo[2] < 0 || (st && st[2] != 1))
+        return false;
+    if (ext && (hi[0] >= ext[0] || hi[1] >= ext[1] || hi[2] >= ext[2])) return false;  // cells stored in the array
+    g.s0 = st ? st[0] : 0;
+    g.s1 = st ? st[1] : 0;
+    g.e0 = ext ? ext[0] : 0;
+    g.e1 = ext ? ext[1] : 0;
+    g.e2 = ext ? ext[2] : 0;
+    g.lo0 = lo[0];
+    g.lo1 = lo[1];
+    g.lo2 = lo[2];
+    g.hi0 = hi[0];
+    g.hi1 = hi[1];
+    g.hi2 = hi[2];
+    g.na = (hi[0] - lo[0] + TI) / TI;
+    g.nb = (hi[1] - lo[1] + TJ) / TJ;
+    g.nk = hi[2] - lo[2] + 1;
+    g.ncg = hypCmax<G>(g.na - 1, g.nb - 1, g.nk) + 1;
+    g.nj = hi[1] - lo[1] + 1;
+    g.rows = (hi[0] - lo[0] + 1) * g.nj;
+    g.kc0 = Hyp<G>::PARTS * (lo[2] / 64);
+    g.nparts = Hyp<G>::PARTS * (hi[2] / 64 - lo[2] / 64 + 1);
+    if (g.na >= (1L << 21) || g.nb >= (1L << 21) || g.ncg >= (1L << 21) || g.nk >= (1L << 30) ||
+        g.na * g.nb * g.ncg >= (1L << 30))
+        return false;
+    long n = 0;
+    for (long a = 0; a < g.na; a++)
+        for (long b = 0; b < g.nb; b++) n += hypCmax<G>(a, b, g.nk) - hypCmin<G>(a, b) + 1;
+    g.ntiles = n;
+    g.nlev = g.na + g.nb + g.ncg - 2;
+    return true;
+}
+
+// scratch: the tile counter (own 256-byte line), one flag per (a, b, c < ncg), the hand-out table, the carries
+struct HypScratch {
+    size_t flagsOff, tableOff, carryOff, bytes;
+};
+template <int G>
+HypScratch hypScratch(const HGeo &g) {
+    HypScratch s;
+    s.flagsOff = 256;
+    s.tableOff = (s.flagsOff + sizeof(int) * (size_t)(g.na * g.nb * g.ncg) + 15) / 16 * 16;
+    s.carryOff = s.tableOff + sizeof(unsigned long long) * (size_t)g.ntiles;
+    s.bytes = s.carryOff + sizeof(double) * (G - 1) * (size_t)g.rows;
+    return s;
+}
+
+template <int G>
+int sweepHyp(double *A, const long st[3], const long ext[3], const long lo[3], const long hi[3], const double *wDev,
+             double *items, void *scratch, int *status, Bound bound, cudaStream_t s) {
+    using H = Hyp<G>;
+    HGeo g;
+    if (!hypGeo<G>(st, ext, lo, hi, g)) return -1;
+    const HypScratch sc = hypScratch<G>(g);
+    char *base = (char *)scratch;
+    unsigned *counter = (unsigned *)base;
+    int *flags = (int *)(base + sc.flagsOff);
+    unsigned long long *table = (unsigned long long *)(base + sc.tableOff);
+    double *carry = (double *)(base + sc.carryOff);
+    if (cudaMemsetAsync(scratch, 0, sc.tableOff, s) != cudaSuccess) return -1;
+    kHypTable<G><<<(unsigned)g.nlev, 256, 0, s>>>(g, table);
+    static std::atomic<int> occCache[gbdev::MAX_DEVICES];
+    const int occ = gbdev::residentCtas(occCache, kSorHyp<G>, NT, H::SMEM);
+    long grid = (long)occ * gbdev::smCount();  // all CTAs resident at once: waits always resolve
+    const long gridCap = (g.ntiles + WPB - 1) / WPB;
+    if (grid > gridCap) grid = gridCap;
+    kSorHyp<G><<<(unsigned)grid, NT, H::SMEM, s>>>(A, g, wDev, flags, counter, table, carry, items, status, bound);
+    dvmhgb_count_launches(2);
+    return cudaGetLastError() == cudaSuccess ? 0 : -1;
+}
+
 }  // namespace
 
 extern "C" {
@@ -574,6 +948,11 @@ long dvmhgb_sor3d_items(const long lo[3], const long hi[3], int variant) {
 long dvmhgb_sor3d_scratch_bytes(const long lo[3], const long hi[3], int variant) {
     const int tk = tkOf(variant);
     if (!tk) return -1;
+    if (variant == 4) {
+        HGeo g;
+        if (!hypGeo<8>(nullptr, nullptr, lo, hi, g)) return -1;
+        return (long)hypScratch<8>(g).bytes;
+    }
     long ntiles = ((hi[0] - lo[0] + TI) / TI) * ((hi[1] - lo[1] + TJ) / TJ) * (64 / tk) * (hi[2] / 64 - lo[2] / 64 + 1);
     return (ntiles + 64) * (long)sizeof(int);
 }
@@ -587,6 +966,7 @@ int dvmhgb_sor3d_sweep_bounded(double *A, const long st[3], const long ext[3], c
     if (pollLimit < 1 || firstIndex < 0 || firstIndex >= (1L << 30)) return -1;
     const Bound bound{pollLimit, (unsigned)firstIndex};
     cudaStream_t s = (cudaStream_t)stream;
+    if (variant == 4) return sweepHyp<8>(A, st, ext, lo, hi, wDev, items, scratch, status, bound, s);
     switch (tk) {
         case 64: return sweepStream(A, g, wDev, items, scratch, status, bound, s);
         case 32: return sweepT<32>(A, g, wDev, items, scratch, status, bound, s);

@@ -15,8 +15,9 @@
 #define SOR_DEFAULT_VARIANT 1
 
 // the variants as the tuner's variant model sees them: family 3 (this program),
-// the tile depth along k (64: streaming columns), streaming
-static const float sorDesc[4 * 3] = {3, 32, 0, 3, 16, 0, 3, 8, 0, 3, 64, 1};
+// the tile depth along k (64: streaming columns; hyperplanes per tile for the
+// hyperplane tiles), tile kind (0 box, 1 streaming column, 2 hyperplane tile)
+static const float sorDesc[5 * 3] = {3, 32, 0, 3, 16, 0, 3, 8, 0, 3, 64, 1, 3, 8, 2};
 
 extern "C" void loop_sor3d_cuda(DvmType *pLoopRef, DvmType A_hdr[], double *s_ptr, double *w_ptr) {
     (void)s_ptr;
@@ -46,7 +47,7 @@ extern "C" void loop_sor3d_cuda(DvmType *pLoopRef, DvmType A_hdr[], double *s_pt
     double s, *s_grid = 0;
     dvmh_loop_cuda_register_red_C(loop_ref, 1, (void **)&s_grid, 0);
     dvmh_loop_red_init_C(loop_ref, 1, &s, 0);
-    // tile depth along k (32, 16, 8): chosen by the runtime's variant tuner
+    // tile shape: chosen by the runtime's variant tuner
     const int variant = dvmhgb_loop_variant_desc(loop_ref, DVMHGB_SOR3D_VARIANTS, SOR_DEFAULT_VARIANT, sorDesc, 3);
     dvmh_loop_cuda_red_prepare_C(loop_ref, 1, dvmhgb_sor3d_items(lo, hi, variant), 0);
     void *scratch = dvmhgb_loop_scratch(loop_ref, dvmhgb_sor3d_scratch_bytes(lo, hi, variant));
