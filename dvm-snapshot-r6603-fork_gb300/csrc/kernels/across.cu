@@ -319,10 +319,10 @@ bool geo(const long st[3], const long ext[3], const long lo[3], const long hi[3]
 }
 
 // variant -> TK: 0 -> 32, 1 -> 16, 2 -> 8; 3: streaming columns (items as for TK = 64: one per 64-wide chunk);
-// 4: hyperplane tiles of G = 8 hyperplanes (items as for TK = 8)
+// 4, 5: hyperplane tiles of G = 8 hyperplanes, 4 x 8 rows per warp or 16 x 8 rows per CTA (items as for TK = 8)
 int tkOf(int variant) {
-    static const int tk[5] = {32, 16, 8, 64, 8};
-    return variant >= 0 && variant < 5 ? tk[variant] : 0;
+    static const int tk[6] = {32, 16, 8, 64, 8, 8};
+    return variant >= 0 && variant < 6 ? tk[variant] : 0;
 }
 
 template <int TK>
@@ -565,7 +565,7 @@ int sweepStream(double *A, const Geo &g0, const double *wDev, double *items, voi
     return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }
 
-// ---------------------------------------------------------------- hyperplane tiles (variant 4)
+// ---------------------------------------------------------------- hyperplane tiles (variants 4 and 5)
 //
 // The tiles above are boxes: inside one, lane (li, lj) starts li + lj steps
 // late, so a 4 x 8 x TK tile takes TK + 10 steps for TK positions per lane, and
@@ -624,15 +624,17 @@ struct HGeo {
     long kc0, nparts; // first part (of the whole array's k) with items; items per row
     long ntiles, nlev;
     long rows;        // rows of the loop box: (hi0 - lo0 + 1) * nj
+    long ti, tj;      // rows of a tile along i and j
 };
 
+// the first and last tile of column (a, b): the hyperplanes its rows' cells lie on
 template <int G>
-__host__ __device__ __forceinline__ long hypCmin(long a, long b) {
-    return (TI * a + TJ * b) / G;
+__host__ __device__ __forceinline__ long hypCmin(const HGeo &g, long a, long b) {
+    return (g.ti * a + g.tj * b) / G;
 }
 template <int G>
-__host__ __device__ __forceinline__ long hypCmax(long a, long b, long nk) {
-    return (TI * a + TJ * b + TI + TJ - 2 + nk - 1) / G;
+__host__ __device__ __forceinline__ long hypCmax(const HGeo &g, long a, long b) {
+    return (g.ti * a + g.tj * b + g.ti + g.tj - 2 + g.nk - 1) / G;
 }
 
 __device__ __forceinline__ unsigned long long hypPack(long a, long b, long c) {
@@ -649,7 +651,7 @@ __global__ void __launch_bounds__(256) kHypTable(HGeo g, unsigned long long *tab
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     long long before = 0;
     for (long q = tid; q < g.na * g.nb; q += 256) {
-        const long a = q / g.nb, b = q % g.nb, c0 = hypCmin<G>(a, b), cnt = hypCmax<G>(a, b, g.nk) - c0 + 1;
+        const long a = q / g.nb, b = q % g.nb, c0 = hypCmin<G>(g, a, b), cnt = hypCmax<G>(g, a, b) - c0 + 1;
         const long x = d - a - b - c0;
         before += x <= 0 ? 0 : (x < cnt ? x : cnt);
     }
@@ -665,7 +667,7 @@ __global__ void __launch_bounds__(256) kHypTable(HGeo g, unsigned long long *tab
         const long amin = s - (g.nb - 1) > 0 ? s - (g.nb - 1) : 0, amax = s < g.na - 1 ? s : g.na - 1;
         for (long a0 = amin; a0 <= amax; a0 += 256) {
             const long a = a0 + tid, b = s - a, c = d - s;
-            const bool in = a <= amax && c >= hypCmin<G>(a, b) && c <= hypCmax<G>(a, b, g.nk);
+            const bool in = a <= amax && c >= hypCmin<G>(g, a, b) && c <= hypCmax<G>(g, a, b);
             const unsigned m = __ballot_sync(0xffffffffu, in);
             if (lane == 0) wsum[warp] = __popc(m);
             __syncthreads();
@@ -766,7 +768,7 @@ __global__ void __launch_bounds__(NT) kSorHyp(double *A, HGeo g, const double *w
             // lanes 0..4: (a-1,b,c), (a-1,b,c-1), (a,b-1,c), (a,b-1,c-1), (a,b,c-1)
             const long pa = a - (lane < 2), pb = b - (lane == 2 || lane == 3),
                        pc = c - (lane == 1 || lane == 3 || lane == 4);
-            if (pa >= 0 && pb >= 0 && pc >= hypCmin<G>(pa, pb) && pc <= hypCmax<G>(pa, pb, g.nk) &&
+            if (pa >= 0 && pb >= 0 && pc >= hypCmin<G>(g, pa, pb) && pc <= hypCmax<G>(g, pa, pb) &&
                 !hypWait(flags + (pa * g.nb + pb) * g.ncg + pc, 1, status, counter, bound.pollLimit))
                 fail = 1;
         }
@@ -779,7 +781,7 @@ __global__ void __launch_bounds__(NT) kSorHyp(double *A, HGeo g, const double *w
         const long m = (k0 + 4 * G) / G * G - 4 * G;          // floor to a part boundary (k0 > -3G)
         const int dl = (int)(k0 - m);                         // positions of the part before the window
         const long rowIdx = row ? (i - g.lo0) * g.nj + (j - g.lo1) : 0;
-        const bool first = c == hypCmin<G>(a, b);
+        const bool first = c == hypCmin<G>(g, a, b);
         const bool res = row && k0 <= g.hi2;                  // the row has a part to close here
         // 3. the -i face rows (0, 1..8) and -j face rows (1..4, 0) at positions 0 .. G-1, the own rows at 0,
         //    and the differences the row's previous window carried over (its last dl positions)
@@ -825,21 +827,41 @@ __global__ void __launch_bounds__(NT) kSorHyp(double *A, HGeo g, const double *w
             }
             __syncwarp();
         }
-        // 5. store the tile's cells (row r of the tile at positions 1 .. G) and the differences of the row's
-        //    last dl positions, which the row's next window needs; then release the successors
-#pragma unroll
-        for (int u = 0; u < G; u++) {
-            const int q = u * 32 + lane, r = q / G, p = 1 + q % G, qi = r / TJ, qj = r % TJ;
+        // 5. store what the successors read -- the rows li = 3 and lj = 7, the last position of the others, and
+        //    the differences of the row's last dl positions (the row's next window needs them) -- release the
+        //    successors, then store the tile's other cells (read by no tile of this sweep)
+        auto store = [&](int r, int p) {  // row r of the tile, window position p (1 .. G)
+            const int qi = r / TJ, qj = r % TJ;
             const long ii = ra + qi, jj = rb + qj, rk = hc - ii - jj + p - 1;
             if (g.lo0 + ii <= g.hi0 && g.lo1 + jj <= g.hi1 && rk >= 0 && rk < nk)
                 A[(g.lo0 + ii) * g.s0 + (g.lo1 + jj) * g.s1 + g.lo2 + rk] = box[((qi + 1) * SJ + qj + 1) * SKP + p];
+        };
+#pragma unroll
+        for (int u = (TI - 1) * TJ * G / 32; u < TI * TJ * G / 32; u++) {  // rows li = 3
+            const int q = u * 32 + lane;
+            store(q / G, 1 + q % G);
+        }
+        {
+            constexpr int NE = (TI - 1) * G + (TI - 1) * (TJ - 1);  // rows lj = 7 (li < 3), last positions
+#pragma unroll
+            for (int u = 0; u < (NE + 31) / 32; u++) {
+                const int e = u * 32 + lane, f = e - (TI - 1) * G;
+                if (e < (TI - 1) * G) store((e / G) * TJ + TJ - 1, 1 + e % G);
+                else if (e < NE) store((f / (TJ - 1)) * TJ + f % (TJ - 1), G);
+            }
         }
 #pragma unroll
         for (int t = 1; t < G; t++)  // position t is leaf t - G + dl of the next part
             if (res && t - G + dl >= 0) carry[(t - G + dl) * g.rows + rowIdx] = dv[t];
-        __threadfence();
+        // the warp barrier orders every lane's stores before lane 0's release at GPU scope, which publishes
+        // them (release cumulativity) without a sequentially consistent fence in every lane
         __syncwarp();
         if (lane == 0) stRelease(flags + (a * g.nb + b) * g.ncg + c, 1);
+#pragma unroll
+        for (int u = 0; u < (TI - 1) * TJ * G / 32; u++) {  // rows li < 3, lj < 7 at positions 1 .. G - 1
+            const int q = u * 32 + lane, r = q / G, p = 1 + q % G;
+            if (r % TJ < TJ - 1 && p < G) store(r, p);
+        }
         // 6. the residual, off the chain: the leaves of the part [m, m + G) are the carried differences, then
         //    this window's; squared where k lies in the loop, -0.0 elsewhere
         if (res) {
@@ -862,8 +884,174 @@ __global__ void __launch_bounds__(NT) kSorHyp(double *A, HGeo g, const double *w
     }
 }
 
+// CTA tiles: TIc x TJc rows, one thread per row (TIc * TJc / 32 warps), one tile per CTA.  Fewer, larger
+// tiles shorten the chain of tile planes (a + b + c) a sweep has to go through; the tile's warps take their
+// steps in lockstep (a CTA barrier per step), each on its own SM sub-partition.
+template <int G, int TIc, int TJc>
+struct HypC {
+    static constexpr int NTc = TIc * TJc;
+    static constexpr int SIc = TIc + 2, SJc = TJc + 2;
+    static constexpr int SKP = G + 3;  // window: positions 0 .. G + 1 (odd stride: banks)
+    static constexpr int BOX = SIc * SJc * SKP;
+    static constexpr int SQS = 2 * G + 1;
+    static constexpr size_t SMEM = sizeof(double) * (BOX + NTc * SQS);
+};
+
+template <int G, int TIc, int TJc>
+__global__ void __launch_bounds__(TIc * TJc, 4) kSorHypCta(double *A, HGeo g, const double *wPtr, int *flags,
+                                                        unsigned *counter, const unsigned long long *table,
+                                                        double *carry, double *items, int *status, Bound bound) {
+    using H = HypC<G, TIc, TJc>;
+    constexpr int SKP = H::SKP, SJc = H::SJc, RS = SJc * SKP, NTc = H::NTc;
+    extern __shared__ double sm[];  // box [SIc][SJc][SKP], then leaves [NTc][SQS]
+    __shared__ long tileIdx;
+    const int tid = threadIdx.x, li = tid / TJc, lj = tid % TJc;
+    double *box = sm;
+    double *sq = sm + H::BOX + tid * H::SQS;
+    const double w = *wPtr;
+    const double c1 = 1.0 - w, c2 = w / 6.0;  // loop invariants, rounded as in the source expression
+    const int nk = (int)g.nk;
+    while (true) {
+        if (tid == 0) tileIdx = (long)atomicAdd(counter, 1u) + bound.firstIndex;  // >= 2^31 once a CTA has failed
+        __syncthreads();  // the index; and the previous tile's last box reads are done
+        const long idx = tileIdx;
+        if (idx >= g.ntiles) break;
+        const unsigned long long tv = table[idx];
+        const long a = (long)(tv >> 42), b = (long)((tv >> 21) & 0x1fffff), c = (long)(tv & 0x1fffff);
+        const long ra = TIc * a, rb = TJc * b, hc = G * c;
+        // 1. before the wait: rows qi 1..TIc+1, qj 1..TJc+1, positions 1 .. G+1 (old values)
+        {
+            constexpr int NV = (H::SIc - 1) * (SJc - 1) * (G + 1), NL = (NV + NTc - 1) / NTc;
+            double v[NL];
+#pragma unroll
+            for (int u = 0; u < NL; u++) {
+                const int q = u * NTc + tid, r = q / (G + 1), p = 1 + q % (G + 1);
+                const int qi = 1 + r / (SJc - 1), qj = 1 + r % (SJc - 1);
+                const long fi = ra - 1 + qi, fj = rb - 1 + qj;
+                v[u] = q < NV ? ldH(A, g, g.lo0 + fi, g.lo1 + fj, g.lo2 + hc - fi - fj - 1 + p) : 0.0;
+            }
+#pragma unroll
+            for (int u = 0; u < NL; u++) {
+                const int q = u * NTc + tid, r = q / (G + 1), p = 1 + q % (G + 1);
+                const int qi = 1 + r / (SJc - 1), qj = 1 + r % (SJc - 1);
+                if (q < NV) box[(qi * SJc + qj) * SKP + p] = v[u];
+            }
+        }
+        // 2. wait for the five predecessors (bounded); the barrier orders the acquiring threads' loads
+        //    before every thread's face loads
+        int fail = 0;
+        if (tid < 5) {
+            // threads 0..4: (a-1,b,c), (a-1,b,c-1), (a,b-1,c), (a,b-1,c-1), (a,b,c-1)
+            const long pa = a - (tid < 2), pb = b - (tid == 2 || tid == 3), pc = c - (tid == 1 || tid == 3 || tid == 4);
+            if (pa >= 0 && pb >= 0 && pc >= hypCmin<G>(g, pa, pb) && pc <= hypCmax<G>(g, pa, pb) &&
+                !hypWait(flags + (pa * g.nb + pb) * g.ncg + pc, 1, status, counter, bound.pollLimit))
+                fail = 1;
+        }
+        if (__syncthreads_or(fail)) return;
+        const long ri = ra + li, rj = rb + lj, i = g.lo0 + ri, j = g.lo1 + rj;
+        const bool row = i <= g.hi0 && j <= g.hi1;
+        const int rk0 = (int)(hc - ri - rj);
+        const long k0 = g.lo2 + rk0;
+        const long m = (k0 + 4 * G) / G * G - 4 * G;
+        const int dl = (int)(k0 - m);
+        const long rowIdx = row ? (i - g.lo0) * g.nj + (j - g.lo1) : 0;
+        const bool first = c == hypCmin<G>(g, a, b);
+        const bool res = row && k0 <= g.hi2;
+        // 3. the -i face rows (0, 1..TJc), the -j face rows (1..TIc, 0) at positions 0 .. G-1, the own rows at
+        //    0, and the carried differences
+        double cin[G - 1];
+        {
+            constexpr int NV = (TIc + TJc) * G, NL = (NV + NTc - 1) / NTc;
+            double v[NL];
+#pragma unroll
+            for (int u = 0; u < NL; u++) {
+                const int q = u * NTc + tid, r = q / G, p = q % G;
+                const int qi = r < TJc ? 0 : r - TJc + 1, qj = r < TJc ? r + 1 : 0;
+                const long fi = ra - 1 + qi, fj = rb - 1 + qj;
+                v[u] = q < NV ? ldH(A, g, g.lo0 + fi, g.lo1 + fj, g.lo2 + hc - fi - fj - 1 + p) : 0.0;
+            }
+            const double k0v = ldH(A, g, i, j, k0 - 1);
+#pragma unroll
+            for (int q = 0; q < G - 1; q++)
+                cin[q] = res && !first && q < dl ? __ldcg(carry + q * g.rows + rowIdx) : 0.0;
+#pragma unroll
+            for (int u = 0; u < NL; u++) {
+                const int q = u * NTc + tid, r = q / G, p = q % G;
+                const int qi = r < TJc ? 0 : r - TJc + 1, qj = r < TJc ? r + 1 : 0;
+                if (q < NV) box[(qi * SJc + qj) * SKP + p] = v[u];
+            }
+            box[((li + 1) * SJc + lj + 1) * SKP] = k0v;
+        }
+        __syncthreads();
+        double *x = box + ((li + 1) * SJc + (lj + 1)) * SKP + 1;  // x[t]: position t + 1
+        double dv[G];
+        // 4. the dependent chain: G steps, one thread per row, the CTA in lockstep
+#pragma unroll
+        for (int t = 0; t < G; t++) {
+            const int rk = rk0 + t;
+            dv[t] = 0.0;
+            if (row && rk >= 0 && rk < nk) {
+                const double old = x[t];
+                // A[i-1] + A[i+1] + A[j-1] + A[j+1] + A[k-1] + A[k+1], left to right
+                const double s = ((((x[t - RS - 1] + x[t + RS + 1]) + x[t - SKP - 1]) + x[t + SKP + 1]) + x[t - 1]) +
+                                 x[t + 1];
+                const double nv = c1 * old + c2 * s;
+                x[t] = nv;
+                dv[t] = nv - old;
+            }
+            __syncthreads();
+        }
+        // 5. store what the successors read (rows li = TIc-1 and lj = TJc-1, the last position of the others,
+        //    the carried differences), release the successors, then store the other cells
+        auto store = [&](int r, int p) {
+            const int qi = r / TJc, qj = r % TJc;
+            const long ii = ra + qi, jj = rb + qj, rk = hc - ii - jj + p - 1;
+            if (g.lo0 + ii <= g.hi0 && g.lo1 + jj <= g.hi1 && rk >= 0 && rk < nk)
+                A[(g.lo0 + ii) * g.s0 + (g.lo1 + jj) * g.s1 + g.lo2 + rk] = box[((qi + 1) * SJc + qj + 1) * SKP + p];
+        };
+        {
+            constexpr int N1 = TJc * G, N2 = N1 + (TIc - 1) * G, NE = N2 + (TIc - 1) * (TJc - 1);
+#pragma unroll
+            for (int u = 0; u < (NE + NTc - 1) / NTc; u++) {
+                const int e = u * NTc + tid;
+                if (e < N1) store((TIc - 1) * TJc + e / G, 1 + e % G);
+                else if (e < N2) store(((e - N1) / G) * TJc + TJc - 1, 1 + (e - N1) % G);
+                else if (e < NE) store(((e - N2) / (TJc - 1)) * TJc + (e - N2) % (TJc - 1), G);
+            }
+        }
+#pragma unroll
+        for (int t = 1; t < G; t++)  // position t is leaf t - G + dl of the next part
+            if (res && t - G + dl >= 0) carry[(t - G + dl) * g.rows + rowIdx] = dv[t];
+        // the CTA barrier orders every thread's stores before thread 0's release at GPU scope
+        __syncthreads();
+        if (tid == 0) stRelease(flags + (a * g.nb + b) * g.ncg + c, 1);
+#pragma unroll
+        for (int u = 0; u < G; u++) {  // rows li < TIc-1, lj < TJc-1 at positions 1 .. G-1
+            const int q = u * NTc + tid, r = q / G, p = 1 + q % G;
+            if (r / TJc < TIc - 1 && r % TJc < TJc - 1 && p < G) store(r, p);
+        }
+        // 6. the residual, off the chain (per thread, as in the warp tiles)
+        if (res) {
+#pragma unroll
+            for (int q = 0; q < G - 1; q++)
+                if (q < dl) sq[q] = cin[q];
+#pragma unroll
+            for (int t = 0; t < G; t++) sq[dl + t] = dv[t];
+            const long P = m / G - g.kc0;
+            double *it = items + rowIdx * g.nparts;
+            if (first)
+                for (long q = 0; q < P && q < g.nparts; q++) it[q] = -0.0;
+            if (P >= 0 && P < g.nparts) it[P] = hypTree<G>(sq, m, g.lo2, g.hi2);
+            if (k0 + G - 1 >= g.hi2) {
+                if (P + 1 >= 0 && P + 1 < g.nparts) it[P + 1] = hypTree<G>(sq + G, m + G, g.lo2, g.hi2);
+                for (long q = P + 2 > 0 ? P + 2 : 0; q < g.nparts; q++) it[q] = -0.0;
+            }
+        }
+    }
+}
+
 template <int G>
-bool hypGeo(const long st[3], const long ext[3], const long lo[3], const long hi[3], HGeo &g) {
+bool hypGeo(const long st[3], const long ext[3], const long lo[3], const long hi[3], long ti, long tj, HGeo &g) {
     if (hi[0] < lo[0] || hi[1] < lo[1] || hi[2] < lo[2] || lo[0] < 0 || lo[1] < 0 || lo[2] < 0 || (st && st[2] != 1))
         return false;
     if (ext && (hi[0] >= ext[0] || hi[1] >= ext[1] || hi[2] >= ext[2])) return false;  // cells stored in the array
@@ -878,10 +1066,12 @@ bool hypGeo(const long st[3], const long ext[3], const long lo[3], const long hi
     g.hi0 = hi[0];
     g.hi1 = hi[1];
     g.hi2 = hi[2];
-    g.na = (hi[0] - lo[0] + TI) / TI;
-    g.nb = (hi[1] - lo[1] + TJ) / TJ;
+    g.ti = ti;
+    g.tj = tj;
+    g.na = (hi[0] - lo[0] + ti) / ti;
+    g.nb = (hi[1] - lo[1] + tj) / tj;
     g.nk = hi[2] - lo[2] + 1;
-    g.ncg = hypCmax<G>(g.na - 1, g.nb - 1, g.nk) + 1;
+    g.ncg = hypCmax<G>(g, g.na - 1, g.nb - 1) + 1;
     g.nj = hi[1] - lo[1] + 1;
     g.rows = (hi[0] - lo[0] + 1) * g.nj;
     g.kc0 = Hyp<G>::PARTS * (lo[2] / 64);
@@ -891,7 +1081,7 @@ bool hypGeo(const long st[3], const long ext[3], const long lo[3], const long hi
         return false;
     long n = 0;
     for (long a = 0; a < g.na; a++)
-        for (long b = 0; b < g.nb; b++) n += hypCmax<G>(a, b, g.nk) - hypCmin<G>(a, b) + 1;
+        for (long b = 0; b < g.nb; b++) n += hypCmax<G>(g, a, b) - hypCmin<G>(g, a, b) + 1;
     g.ntiles = n;
     g.nlev = g.na + g.nb + g.ncg - 2;
     return true;
@@ -911,12 +1101,14 @@ HypScratch hypScratch(const HGeo &g) {
     return s;
 }
 
+// one hyperplane sweep: the tile list, then the persistent wavefront.  cta: tiles of CTA_TI x CTA_TJ rows, one
+// per CTA (kSorHypCta); else tiles of 4 x 8 rows, one per warp (kSorHyp)
+constexpr int CTA_TI = 16, CTA_TJ = 8;
 template <int G>
 int sweepHyp(double *A, const long st[3], const long ext[3], const long lo[3], const long hi[3], const double *wDev,
-             double *items, void *scratch, int *status, Bound bound, cudaStream_t s) {
-    using H = Hyp<G>;
+             double *items, void *scratch, int *status, Bound bound, bool cta, cudaStream_t s) {
     HGeo g;
-    if (!hypGeo<G>(st, ext, lo, hi, g)) return -1;
+    if (!hypGeo<G>(st, ext, lo, hi, cta ? CTA_TI : TI, cta ? CTA_TJ : TJ, g)) return -1;
     const HypScratch sc = hypScratch<G>(g);
     char *base = (char *)scratch;
     unsigned *counter = (unsigned *)base;
@@ -925,12 +1117,25 @@ int sweepHyp(double *A, const long st[3], const long ext[3], const long lo[3], c
     double *carry = (double *)(base + sc.carryOff);
     if (cudaMemsetAsync(scratch, 0, sc.tableOff, s) != cudaSuccess) return -1;
     kHypTable<G><<<(unsigned)g.nlev, 256, 0, s>>>(g, table);
-    static std::atomic<int> occCache[gbdev::MAX_DEVICES];
-    const int occ = gbdev::residentCtas(occCache, kSorHyp<G>, NT, H::SMEM);
-    long grid = (long)occ * gbdev::smCount();  // all CTAs resident at once: waits always resolve
-    const long gridCap = (g.ntiles + WPB - 1) / WPB;
-    if (grid > gridCap) grid = gridCap;
-    kSorHyp<G><<<(unsigned)grid, NT, H::SMEM, s>>>(A, g, wDev, flags, counter, table, carry, items, status, bound);
+    long grid;
+    if (cta) {
+        using H = HypC<G, CTA_TI, CTA_TJ>;
+        static std::atomic<int> occCache[gbdev::MAX_DEVICES];
+        const int occ = gbdev::residentCtas(occCache, kSorHypCta<G, CTA_TI, CTA_TJ>, H::NTc, H::SMEM);
+        grid = (long)occ * gbdev::smCount();  // all CTAs resident at once: waits always resolve
+        if (grid > g.ntiles) grid = g.ntiles;
+        kSorHypCta<G, CTA_TI, CTA_TJ><<<(unsigned)grid, H::NTc, H::SMEM, s>>>(A, g, wDev, flags, counter, table,
+                                                                             carry, items, status, bound);
+    } else {
+        using H = Hyp<G>;
+        static std::atomic<int> occCache[gbdev::MAX_DEVICES];
+        const int occ = gbdev::residentCtas(occCache, kSorHyp<G>, NT, H::SMEM);
+        grid = (long)occ * gbdev::smCount();
+        const long gridCap = (g.ntiles + WPB - 1) / WPB;
+        if (grid > gridCap) grid = gridCap;
+        kSorHyp<G><<<(unsigned)grid, NT, H::SMEM, s>>>(A, g, wDev, flags, counter, table, carry, items, status,
+                                                        bound);
+    }
     dvmhgb_count_launches(2);
     return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }
@@ -948,9 +1153,10 @@ long dvmhgb_sor3d_items(const long lo[3], const long hi[3], int variant) {
 long dvmhgb_sor3d_scratch_bytes(const long lo[3], const long hi[3], int variant) {
     const int tk = tkOf(variant);
     if (!tk) return -1;
-    if (variant == 4) {
+    if (variant >= 4) {
         HGeo g;
-        if (!hypGeo<8>(nullptr, nullptr, lo, hi, g)) return -1;
+        if (!hypGeo<8>(nullptr, nullptr, lo, hi, variant == 5 ? CTA_TI : TI, variant == 5 ? CTA_TJ : TJ, g))
+            return -1;
         return (long)hypScratch<8>(g).bytes;
     }
     long ntiles = ((hi[0] - lo[0] + TI) / TI) * ((hi[1] - lo[1] + TJ) / TJ) * (64 / tk) * (hi[2] / 64 - lo[2] / 64 + 1);
@@ -966,7 +1172,7 @@ int dvmhgb_sor3d_sweep_bounded(double *A, const long st[3], const long ext[3], c
     if (pollLimit < 1 || firstIndex < 0 || firstIndex >= (1L << 30)) return -1;
     const Bound bound{pollLimit, (unsigned)firstIndex};
     cudaStream_t s = (cudaStream_t)stream;
-    if (variant == 4) return sweepHyp<8>(A, st, ext, lo, hi, wDev, items, scratch, status, bound, s);
+    if (variant >= 4) return sweepHyp<8>(A, st, ext, lo, hi, wDev, items, scratch, status, bound, variant == 5, s);
     switch (tk) {
         case 64: return sweepStream(A, g, wDev, items, scratch, status, bound, s);
         case 32: return sweepT<32>(A, g, wDev, items, scratch, status, bound, s);

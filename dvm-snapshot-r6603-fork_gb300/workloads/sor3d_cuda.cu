@@ -12,12 +12,13 @@
 #include "dvmh_gb.h"
 #include "dvmh_gb_kernels.h"
 
-#define SOR_DEFAULT_VARIANT 1
+#define SOR_DEFAULT_VARIANT 4
 
 // the variants as the tuner's variant model sees them: family 3 (this program),
 // the tile depth along k (64: streaming columns; hyperplanes per tile for the
-// hyperplane tiles), tile kind (0 box, 1 streaming column, 2 hyperplane tile)
-static const float sorDesc[5 * 3] = {3, 32, 0, 3, 16, 0, 3, 8, 0, 3, 64, 1, 3, 8, 2};
+// hyperplane tiles), tile kind (0 box, 1 streaming column, 2 / 3 hyperplane
+// tile per warp / per CTA)
+static const float sorDesc[6 * 3] = {3, 32, 0, 3, 16, 0, 3, 8, 0, 3, 64, 1, 3, 8, 2, 3, 8, 3};
 
 extern "C" void loop_sor3d_cuda(DvmType *pLoopRef, DvmType A_hdr[], double *s_ptr, double *w_ptr) {
     (void)s_ptr;

@@ -108,14 +108,15 @@ int dvmhgb_jac2d_fused(double *A, const double *B, double *Bnew, const long st[2
 /* ---- SOR 3-D ACROSS (1:1,1:1,1:1), FP64: one sweep as a persistent tiled
  * wavefront of 4 x 8 x TK tiles, TK = 32, 16, 8 for variant 0, 1, 2, or
  * (variant 3) as 4 x 8-row columns streamed along k by one warp each, or
- * (variant 4) as tiles of 4 x 8 rows cut along the hyperplanes i + j + k,
- * 8 hyperplanes each (a first launch lists the tiles); items = canonical
- * partials of SUM (nv-old)^2, one per row and TK-wide part of each 64-wide
- * chunk (row, chunk, part order; TK = 8 for variant 4; one per row and chunk
- * for variant 3); wDev = device address of omega; scratch =
- * dvmhgb_sor3d_scratch_bytes() bytes; status = dvmhgb_status_word().  -1 for
- * an unknown variant or invalid arguments ---- */
-#define DVMHGB_SOR3D_VARIANTS 5
+ * (variants 4, 5) as tiles cut along the hyperplanes i + j + k, 8
+ * hyperplanes each, of 4 x 8 rows per warp (4) or 16 x 8 rows per CTA (5)
+ * (a first launch lists the tiles); items = canonical partials of SUM
+ * (nv-old)^2, one per row and TK-wide part of each 64-wide chunk (row, chunk,
+ * part order; TK = 8 for variants 4, 5; one per row and chunk for variant 3);
+ * wDev = device address of omega; scratch = dvmhgb_sor3d_scratch_bytes()
+ * bytes; status = dvmhgb_status_word().  -1 for an unknown variant or invalid
+ * arguments ---- */
+#define DVMHGB_SOR3D_VARIANTS 6
 long dvmhgb_sor3d_items(const long lo[3], const long hi[3], int variant);
 long dvmhgb_sor3d_scratch_bytes(const long lo[3], const long hi[3], int variant);
 int dvmhgb_sor3d_sweep(double *A, const long st[3], const long ext[3], const long lo[3], const long hi[3],

@@ -39,7 +39,7 @@ def close_sum(a, b, n):
     return np.all(np.abs(a - b) <= 2 * gamma * np.abs(b) + 1e-300)
 
 
-@pytest.mark.parametrize("variant", [0, 1, 2, 3, 4])
+@pytest.mark.parametrize("variant", [0, 1, 2, 3, 4, 5])
 @pytest.mark.parametrize("mode", MODES)
 def test_sor_golden(g, golden, mode, variant):
     g.set_mode(mode)
@@ -96,7 +96,7 @@ def test_sor_generated_hyperplane_handler(g, golden, mode, tfm):
         rt.dvmhgb_set_autotransform(1)
 
 
-@pytest.mark.parametrize("variant", [0, 1, 2, 3, 4])
+@pytest.mark.parametrize("variant", [0, 1, 2, 3, 4, 5])
 @pytest.mark.parametrize("n", [4, 9, 17, 66, 75, 131])
 def test_sor_sizes_vs_oracle(g, n, variant):
     seq, canon, A_ref = orc.sor_run(n, 3, 1.5, 77 + n)

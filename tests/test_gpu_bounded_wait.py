@@ -47,7 +47,7 @@ CHILD = textwrap.dedent("""
 """)
 
 
-@pytest.mark.parametrize("variant", [1, 3, 4])
+@pytest.mark.parametrize("variant", [1, 3, 4, 5])
 def test_expired_wait_is_reported(variant):
     root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
     r = subprocess.run([sys.executable, "-c", CHILD % (root, variant)], capture_output=True, text=True, timeout=600)

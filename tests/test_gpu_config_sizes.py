@@ -48,7 +48,7 @@ def sor_ref():
     return orc.sor_run(384, 2, 1.5, SEED + 2)
 
 
-@pytest.mark.parametrize("variant", [1, 3, 4])
+@pytest.mark.parametrize("variant", [1, 3, 4, 5])
 @pytest.mark.parametrize("mode", ["plain", "batched"])
 def test_sor_384(g, sor_ref, mode, variant):
     seq, canon, A_ref = sor_ref

@@ -38,7 +38,7 @@ def special_grid(n, seed):
     return A.ravel().copy()
 
 
-@pytest.mark.parametrize("variant", [0, 1, 2, 3, 4])
+@pytest.mark.parametrize("variant", [0, 1, 2, 3, 4, 5])
 @pytest.mark.parametrize("omega", [1.5, 1.25, 1.0])
 def test_sor_kernel_special_values(g, variant, omega):
     import torch
@@ -98,7 +98,7 @@ def _sub_box_reference(A, lo, hi, omega, tk):
     return np.array(items)
 
 
-@pytest.mark.parametrize("variant", [1, 2, 4])
+@pytest.mark.parametrize("variant", [1, 2, 4, 5])
 @pytest.mark.parametrize("box", [((2, 3, 40), (9, 13, 121)), ((1, 1, 1), (6, 17, 5)), ((3, 1, 70), (3, 9, 71))])
 def test_sor_kernel_sub_box(g, variant, box):
     """A loop box that is not the array's interior: k starting past the first 64-wide chunk, rows that
@@ -109,7 +109,7 @@ def test_sor_kernel_sub_box(g, variant, box):
     rng = np.random.default_rng(11 + variant)
     A0 = rng.random(shape) * 2.0 - 0.5
     ref = A0.copy()
-    tk = {1: 16, 2: 8, 4: 8}[variant]
+    tk = {1: 16, 2: 8, 4: 8, 5: 8}[variant]
     want = _sub_box_reference(ref, lo, hi, 1.5, tk)
     rt = g.runtime()
     L_lo, L_hi = L3(*lo), L3(*hi)
