@@ -643,10 +643,12 @@ __device__ __forceinline__ unsigned long long hypPack(long a, long b, long c) {
 
 // One CTA per plane d: the plane's first index (tiles on planes < d, summed
 // over the columns in closed form) and its tiles in the order (c, then a).
+// Thread u takes the diagonal s = a + b = smax - u of the plane (c = d - s:
+// ascending with u), counts its tiles, and writes them, a ascending, at its
+// place in the CTA's scan.
 template <int G>
 __global__ void __launch_bounds__(256) kHypTable(HGeo g, unsigned long long *table) {
     __shared__ long long part[8];
-    __shared__ int wsum[8];
     const long d = blockIdx.x;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     long long before = 0;
@@ -661,25 +663,35 @@ __global__ void __launch_bounds__(256) kHypTable(HGeo g, unsigned long long *tab
     __syncthreads();
     long long pos = 0;
     for (int w = 0; w < 8; w++) pos += part[w];
-    // s = a + b from high to low (c = d - s ascending), a ascending inside
+    __syncthreads();  // part is reused by the scans below
     const long smax = g.na + g.nb - 2 < d ? g.na + g.nb - 2 : d;
-    for (long s = smax; s >= 0; s--) {
+    for (long s0 = smax; s0 >= 0; s0 -= 256) {
+        const long s = s0 - tid, c = d - s;
         const long amin = s - (g.nb - 1) > 0 ? s - (g.nb - 1) : 0, amax = s < g.na - 1 ? s : g.na - 1;
-        for (long a0 = amin; a0 <= amax; a0 += 256) {
-            const long a = a0 + tid, b = s - a, c = d - s;
-            const bool in = a <= amax && c >= hypCmin<G>(g, a, b) && c <= hypCmax<G>(g, a, b);
-            const unsigned m = __ballot_sync(0xffffffffu, in);
-            if (lane == 0) wsum[warp] = __popc(m);
-            __syncthreads();
-            int off = 0, tot = 0;
-            for (int w = 0; w < 8; w++) {
-                off += w < warp ? wsum[w] : 0;
-                tot += wsum[w];
-            }
-            if (in) table[pos + off + __popc(m & ((1u << lane) - 1u))] = hypPack(a, b, c);
-            pos += tot;
-            __syncthreads();  // wsum is rewritten by the next round
+        long long cnt = 0;
+        if (s >= 0)
+            for (long a = amin; a <= amax; a++) cnt += c >= hypCmin<G>(g, a, s - a) && c <= hypCmax<G>(g, a, s - a);
+        // exclusive scan of cnt over the CTA's threads
+        long long inc = cnt;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const long long y = __shfl_up_sync(0xffffffffu, inc, o);
+            if (lane >= o) inc += y;
         }
+        if (lane == 31) part[warp] = inc;
+        __syncthreads();
+        long long off = inc - cnt, tot = 0;
+        for (int w = 0; w < 8; w++) {
+            off += w < warp ? part[w] : 0;
+            tot += part[w];
+        }
+        if (s >= 0) {
+            long long at = pos + off;
+            for (long a = amin; a <= amax; a++)
+                if (c >= hypCmin<G>(g, a, s - a) && c <= hypCmax<G>(g, a, s - a)) table[at++] = hypPack(a, s - a, c);
+        }
+        pos += tot;
+        __syncthreads();  // part is rewritten by the next round
     }
 }
 

@@ -73,15 +73,12 @@ static long uncapturedFlushes = 0;    // flushes run eagerly since tuning was re
 static std::vector<Record> vdb;       // the variant database
 
 // timed executions of each variant tried (the fastest counts): one run of a
-// variant can carry first-use costs (a second buffer, a stream) or noise
+// variant can carry first-use costs (a second buffer, a stream) or noise.
+// Read at every query, so that a tuning session can set it for itself.
 static int tuneReps() {
-    static int r = 0;
-    if (r == 0) {
-        const char *e = getenv("DVMH_GB_TUNE_REPS");
-        r = e ? atoi(e) : 2;
-        if (r < 1) r = 1;
-    }
-    return r;
+    const char *e = getenv("DVMH_GB_TUNE_REPS");
+    const int r = e ? atoi(e) : 2;
+    return r < 1 ? 1 : r;
 }
 
 static double tuneFrac() {

@@ -16,6 +16,7 @@
    (rts/dvmh/loop.cpp:1464-1485) and k random candidates.
 """
 import ctypes
+import os
 import math
 import time
 
@@ -276,8 +277,23 @@ def _main_record(recs, handler=None):
     return max(recs, key=lambda r: (r["explore_seconds"], r["nvariants"]))
 
 
-def configs_eval(g, seed=20261203, epochs=300, log=print):
-    """The learned tuner on the configurations' own loops (the bench's configs.tune)."""
+def configs_eval(g, seed=20261203, epochs=300, log=print, reps=4):
+    """The learned tuner on the configurations' own loops (the bench's configs.tune).  Every variant a
+    tuning session tries runs `reps` times (the fastest counts) in the training runs, the exhaustive
+    reference and the model-guided runs alike: the configurations' smallest loops take tens of
+    microseconds, where two runs leave their order to chance."""
+    old = os.environ.get("DVMH_GB_TUNE_REPS")
+    os.environ["DVMH_GB_TUNE_REPS"] = str(reps)
+    try:
+        return _configs_eval(g, seed, epochs, log)
+    finally:
+        if old is None:
+            os.environ.pop("DVMH_GB_TUNE_REPS", None)
+        else:
+            os.environ["DVMH_GB_TUNE_REPS"] = old
+
+
+def _configs_eval(g, seed, epochs, log):
     rt = g.runtime()
     rt.dvmhgb_tuner_vdb_size.restype = ctypes.c_long
     rt.dvmhgb_tuner_vdb_export.restype = ctypes.c_long
