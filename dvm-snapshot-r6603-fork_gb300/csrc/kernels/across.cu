@@ -32,6 +32,8 @@
 // values.  Items are laid out (row, chunk, part), so the reduction engine's
 // pairwise fold over items first joins the parts of each 64-position chunk:
 // the result is the canonical chunk tree, then the canonical tree over chunks.
+// The default tiles (variants 4 and 5, at the end of this file) are cut along
+// the hyperplanes i + j + k instead, so that no lane idles on the skew.
 #include <cuda_runtime.h>
 
 #include <cstdint>
