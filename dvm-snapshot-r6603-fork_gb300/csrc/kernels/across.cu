@@ -716,6 +716,12 @@ __device__ __forceinline__ double ldH(const double *A, const HGeo &g, long i, lo
                                                                              : 0.0;
 }
 
+// the multiple of G at or below x (x may be negative: a row's first windows start before the loop box)
+template <int G>
+__device__ __forceinline__ long hypFloor(long x) {
+    return (x >= 0 ? x / G : -((-x + G - 1) / G)) * G;
+}
+
 // pairwise tree over the G leaves of the part starting at array index k = kf: leaf p is d[p]^2 where
 // k = kf + p lies in the loop, -0.0 elsewhere (every lane at the same leaf: warp-uniform)
 template <int G>
@@ -792,7 +798,7 @@ __global__ void __launch_bounds__(NT) kSorHyp(double *A, HGeo g, const double *w
         const bool row = i <= g.hi0 && j <= g.hi1;
         const int rk0 = (int)(hc - ri - rj);                // the row's rk at step 0
         const long k0 = g.lo2 + rk0;                          // ... and its array index k
-        const long m = (k0 + 4 * G) / G * G - 4 * G;          // floor to a part boundary (k0 > -3G)
+        const long m = hypFloor<G>(k0);                       // the part boundary at or below k0
         const int dl = (int)(k0 - m);                         // positions of the part before the window
         const long rowIdx = row ? (i - g.lo0) * g.nj + (j - g.lo1) : 0;
         const bool first = c == hypCmin<G>(g, a, b);
@@ -966,7 +972,7 @@ __global__ void __launch_bounds__(TIc * TJc, 4) kSorHypCta(double *A, HGeo g, co
         const bool row = i <= g.hi0 && j <= g.hi1;
         const int rk0 = (int)(hc - ri - rj);
         const long k0 = g.lo2 + rk0;
-        const long m = (k0 + 4 * G) / G * G - 4 * G;
+        const long m = hypFloor<G>(k0);                       // the part boundary at or below k0
         const int dl = (int)(k0 - m);
         const long rowIdx = row ? (i - g.lo0) * g.nj + (j - g.lo1) : 0;
         const bool first = c == hypCmin<G>(g, a, b);
