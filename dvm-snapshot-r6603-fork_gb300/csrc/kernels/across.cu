@@ -56,7 +56,6 @@ struct Tile {
     static constexpr int OSTR = TK + 1;          // a lane's saved old values (padded: no bank conflicts)
     static constexpr int WSM = BOX + 32 * OSTR;  // doubles of shared memory per warp
     static constexpr size_t SMEM = sizeof(double) * WSM * WPB;
-    static constexpr int PARTS = 64 / TK;        // items per 64-wide chunk
     static constexpr int RPL = 32 / TK;          // rows per warp load
     static constexpr int LOG = TK == 32 ? 5 : (TK == 16 ? 4 : 3);
 };
