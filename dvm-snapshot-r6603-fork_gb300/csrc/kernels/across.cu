@@ -692,7 +692,7 @@ __global__ void __launch_bounds__(256) kHypTable(HGeo g, unsigned long long *tab
                 if (c >= hypCmin<G>(g, a, s - a) && c <= hypCmax<G>(g, a, s - a)) table[at++] = hypPack(a, s - a, c);
         }
         pos += tot;
-        __syncthreads();  // part is rewritten by the next round
+        __syncthreads();  // part is rewritten by the next pass over the diagonals
     }
 }
 
